@@ -1,0 +1,196 @@
+// Candidate kernels of the spatial search: range gate, greedy separated peaks, the
+// per-candidate quasi-Newton direction and the trial step (reference:
+// dsplat/kernels/search.slang:1-109).
+#include <cuda_runtime.h>
+#include <math.h>
+#include "dsplat_gb300.h"
+
+namespace {
+
+__global__ void range_gate_kernel(const float* __restrict__ points, int count,
+                                  const float* __restrict__ positions, int apertures,
+                                  const int* __restrict__ intervals, int bins, float spacing,
+                                  int required, int* __restrict__ output) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float px = points[3 * i], py = points[3 * i + 1], pz = points[3 * i + 2];
+  int matches = 0;
+  for (int a = 0; a < apertures; ++a) {
+    const float dx = px - positions[3 * a], dy = py - positions[3 * a + 1],
+                dz = pz - positions[3 * a + 2];
+    const float x = sqrtf(dx * dx + dy * dy + dz * dz) / spacing;
+    const int k = (int)rintf(x);  // round half to even
+    if (k >= 0 && k < bins && intervals[(size_t)a * bins + k] != 0) ++matches;
+  }
+  output[i] = matches >= required ? 1 : 0;
+}
+
+constexpr int kPeakThreads = 1024;
+
+// Best finite score, ties to the lowest index; suppress everything within separation.
+__global__ void __launch_bounds__(kPeakThreads) peaks_kernel(float* __restrict__ scores,
+                                                             const float* __restrict__ centers,
+                                                             int count, int dimension, int peaks,
+                                                             float separation,
+                                                             int* __restrict__ output) {
+  __shared__ float best_v[kPeakThreads / 32];
+  __shared__ int best_i[kPeakThreads / 32];
+  __shared__ int chosen;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float sep2 = separation * separation;
+  for (int p = 0; p < peaks; ++p) {
+    float bv = -INFINITY;
+    int bi = -1;
+    for (int i = tid; i < count; i += kPeakThreads) {
+      const float v = scores[i];
+      if (isfinite(v) && (bi < 0 || v > bv)) {  // i increases, so ties keep the first
+        bv = v;
+        bi = i;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_down_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      best_v[warp] = bv;
+      best_i[warp] = bi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      bv = lane < kPeakThreads / 32 ? best_v[lane] : -INFINITY;
+      bi = lane < kPeakThreads / 32 ? best_i[lane] : -1;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_down_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        chosen = bi;
+        output[p] = bi;
+      }
+    }
+    __syncthreads();
+    const int index = chosen;
+    if (index < 0) return;
+    float c[8];
+    for (int j = 0; j < dimension && j < 8; ++j) c[j] = centers[(size_t)index * dimension + j];
+    for (int i = tid; i < count; i += kPeakThreads) {
+      float d2 = 0.0f;
+      for (int j = 0; j < dimension && j < 8; ++j) {
+        const float d = centers[(size_t)i * dimension + j] - c[j];
+        d2 += d * d;
+      }
+      if (i == index || d2 < sep2) scores[i] = -INFINITY;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void direction_kernel(const float* __restrict__ inverse,
+                                 const float* __restrict__ gradient,
+                                 const float* __restrict__ normals, const float* __restrict__ mask,
+                                 int count, int width, float radius, float* __restrict__ output) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float d[6], g[6];
+  for (int j = 0; j < width; ++j) g[j] = gradient[i * width + j];
+  float descent = 0.0f;
+  for (int j = 0; j < width; ++j) {
+    float v = 0.0f;
+    for (int k = 0; k < width; ++k) v -= inverse[((size_t)i * width + j) * width + k] * g[k];
+    d[j] = v;
+    descent += v * g[j];
+  }
+  for (int j = 0; j < width; ++j) d[j] = (descent >= 0.0f ? -g[j] : d[j]) * mask[j];
+  if (width == 6) {
+    float proj = 0.0f;
+    for (int j = 0; j < 3; ++j) proj += d[3 + j] * normals[3 * i + j];
+    for (int j = 0; j < 3; ++j) d[3 + j] -= proj * normals[3 * i + j];
+  }
+  float len2 = 0.0f;
+  for (int j = 0; j < width; ++j) len2 += d[j] * d[j];
+  const float scale = fminf(1.0f, radius / fmaxf(sqrtf(len2), 1e-30f));
+  for (int j = 0; j < width; ++j) output[i * width + j] = d[j] * scale;
+}
+
+__global__ void trial_kernel(const float* __restrict__ centers, const float* __restrict__ normals,
+                             const float* __restrict__ direction,
+                             const float* __restrict__ controls, int count, int width,
+                             float fraction, float* __restrict__ out_centers,
+                             float* __restrict__ out_normals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float n[3], len2 = 0.0f;
+  for (int j = 0; j < 3; ++j) {
+    const float c = centers[3 * i + j] + fraction * controls[j] * direction[i * width + j];
+    const float lo = controls[12 + j], hi = controls[18 + j];
+    out_centers[3 * i + j] = controls[6 + j] > 0.0f ? fminf(fmaxf(c, lo), hi) : centers[3 * i + j];
+    n[j] = normals[3 * i + j] +
+           (width == 6 ? fraction * controls[3 + j] * direction[i * width + 3 + j] : 0.0f);
+    len2 += n[j] * n[j];
+  }
+  const float inv = width == 6 ? 1.0f / sqrtf(len2) : 1.0f;
+  for (int j = 0; j < 3; ++j) out_normals[3 * i + j] = width == 6 ? n[j] * inv : normals[3 * i + j];
+}
+
+int status() { return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH; }
+
+}  // namespace
+
+extern "C" {
+
+int dsg_range_gate(const float* points, int32_t count, const float* positions,
+                   int32_t apertures, const int32_t* intervals, int32_t bins, float spacing,
+                   int32_t required, int32_t* output, void* stream) {
+  if (count < 0 || apertures < 0 || bins < 0 || !(spacing > 0.0f)) return DSG_ERR_ARGUMENT;
+  if (count == 0) return DSG_OK;
+  if (!points || !output || (apertures > 0 && (!positions || !intervals))) return DSG_ERR_ARGUMENT;
+  range_gate_kernel<<<(count + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
+      points, count, positions, apertures, intervals, bins, spacing, required, output);
+  return status();
+}
+
+int dsg_peaks(float* scores, const float* centers, int32_t count, int32_t dimension,
+              int32_t peaks, float separation, int32_t* output, void* stream) {
+  if (count < 0 || peaks < 0 || dimension < 1 || dimension > 8) return DSG_ERR_ARGUMENT;
+  if (peaks == 0) return DSG_OK;
+  if (!output || (count > 0 && (!scores || !centers))) return DSG_ERR_ARGUMENT;
+  cudaMemsetAsync(output, 0xff, (size_t)peaks * sizeof(int32_t), (cudaStream_t)stream);
+  if (count == 0) return status();
+  peaks_kernel<<<1, kPeakThreads, 0, (cudaStream_t)stream>>>(scores, centers, count, dimension,
+                                                            peaks, separation, output);
+  return status();
+}
+
+int dsg_direction(const float* inverse, const float* gradient, const float* normals,
+                  const float* mask, int32_t count, int32_t width, float radius, float* output,
+                  void* stream) {
+  if (count < 0 || (width != 3 && width != 6)) return DSG_ERR_ARGUMENT;
+  if (count == 0) return DSG_OK;
+  if (!inverse || !gradient || !normals || !mask || !output) return DSG_ERR_ARGUMENT;
+  direction_kernel<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+      inverse, gradient, normals, mask, count, width, radius, output);
+  return status();
+}
+
+int dsg_trial(const float* centers, const float* normals, const float* direction,
+              const float* controls, int32_t count, int32_t width, float fraction,
+              float* out_centers, float* out_normals, void* stream) {
+  if (count < 0 || (width != 3 && width != 6)) return DSG_ERR_ARGUMENT;
+  if (count == 0) return DSG_OK;
+  if (!centers || !normals || !direction || !controls || !out_centers || !out_normals)
+    return DSG_ERR_ARGUMENT;
+  trial_kernel<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+      centers, normals, direction, controls, count, width, fraction, out_centers, out_normals);
+  return status();
+}
+
+}  // extern "C"

@@ -1,0 +1,1194 @@
+// FMCW surfel kernels: range profiles, JVP, the aperture-reduced family (VJP,
+// correlations and their gradients), dictionary rows, the explicit Jacobian and the
+// normal-bank scores. See common.cuh for the kernel algebra.
+//
+// Warp layout of the bin-parallel kernels: a warp is four quarters of eight lanes.
+// Lane l of a quarter owns the bins k = l + 8 i, i < K / 8, so for one pair the bin
+// offset m = k - lobe has the same residue modulo P (P divides 8) on all of a lane's
+// bins, and its numerator class is fixed per pair. The 32 lanes first compute the
+// geometry of 32 (or 128) pairs in parallel into shared memory, then every quarter
+// sweeps its pairs' bins reading the geometry by broadcast.
+#include <cuda_runtime.h>
+#include <math.h>
+#include "common.cuh"
+
+namespace dsg {
+
+constexpr int kWarps = 4;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
+
+// ------------------------------------------------------------------------------------
+// Range profiles: out[seg][a][k] = sum over the segment's surfels of w c D(k - k0).
+// Reference: dsplat/kernels/surfel.slang:87-142 (render_bins), :61-85 (pair_geometry).
+// ------------------------------------------------------------------------------------
+template <int BPL, int P>
+__global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __restrict__ pos,
+                                                     int A, const float* __restrict__ cen,
+                                                     const float* __restrict__ nrm,
+                                                     const float2* __restrict__ w, int S,
+                                                     int seg_len, float2* __restrict__ out) {
+  constexpr int REC = 2 + 2 * P;
+  extern __shared__ float smem[];
+  const int tbl_n = c.N + 8 * BPL;
+  const int tbl_pad = (tbl_n + 3) & ~3;
+  float* tbl = smem;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int qd = lane >> 3, lp = lane & 7;
+  float* recs = smem + tbl_pad + warp * (32 * 4 * REC);
+  for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) tbl[i] = tan_entry(i, c.N, false);
+  __syncthreads();
+
+  const int a_base = (blockIdx.x * kWarps + warp) * 4;
+  float apx[4], apy[4], apz[4];
+  bool aok[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    int a = a_base + t;
+    aok[t] = a < A;
+    int ac = aok[t] ? a : 0;
+    apx[t] = __ldg(pos + 3 * ac);
+    apy[t] = __ldg(pos + 3 * ac + 1);
+    apz[t] = __ldg(pos + 3 * ac + 2);
+  }
+  float2 acc[BPL];
+#pragma unroll
+  for (int i = 0; i < BPL; ++i) acc[i] = make_float2(0.f, 0.f);
+  float2 gsum = make_float2(0.f, 0.f);
+
+  const int s_begin = blockIdx.y * seg_len;
+  const int s_end = min(S, s_begin + seg_len);
+  for (int s0 = s_begin; s0 < s_end; s0 += 32) {
+    const int s = s0 + lane;
+    const bool sv = s < s_end;
+    float cx = 0.f, cy = 0.f, cz = 0.f, nx = 0.f, ny = 0.f, nz = 1.f;
+    float2 ws = make_float2(0.f, 0.f);
+    if (sv) {
+      cx = __ldg(cen + 3 * s);
+      cy = __ldg(cen + 3 * s + 1);
+      cz = __ldg(cen + 3 * s + 2);
+      nx = __ldg(nrm + 3 * s);
+      ny = __ldg(nrm + 3 * s + 1);
+      nz = __ldg(nrm + 3 * s + 2);
+      ws = ldg2(w + s);
+    }
+    bool any = false;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      Pair q;
+      pair_setup(c, apx[t], apy[t], apz[t], cx, cy, cz, nx, ny, nz, q);
+      const bool ok = sv && aok[t] && q.amp > 0.0f && (ws.x != 0.0f || ws.y != 0.0f);
+      float* r = recs + (lane * 4 + t) * REC;
+      if (ok) {
+        float2 cw = cscale(cmul(q.rot, ws), q.amp * c.inv_S);
+        float2 nu[P];
+        numerators<P>(q.off, nu);
+        r[0] = q.tl;
+        r[1] = __int_as_float(q.lobe);
+#pragma unroll
+        for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 + 2 * k) = cmul(cw, nu[k]);
+      } else {
+        r[0] = 1.0f;
+        r[1] = __int_as_float(0);
+#pragma unroll
+        for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 + 2 * k) = make_float2(0.f, 0.f);
+      }
+      any |= ok;
+    }
+    const unsigned mask = __ballot_sync(kFull, any);
+    __syncwarp();
+    const int nb = min(32, s_end - s0);
+    for (int j = 0; j < nb; ++j) {
+      if (!((mask >> j) & 1u)) continue;
+      const float* r = recs + (j * 4 + qd) * REC;
+      const float tl = r[0];
+      const int lobe = __float_as_int(r[1]);
+      const int cls = (lp - lobe) & (P - 1);
+      const float2 g = *reinterpret_cast<const float2*>(r + 2 + 2 * cls);
+      gsum.x += g.x;
+      gsum.y += g.y;
+      const float* tb = tbl + (lp - lobe + c.N - 1);
+#pragma unroll
+      for (int i = 0; i < BPL; ++i) {
+        const float cot = cot_from(tb[8 * i], tl);
+        acc[i].x = fmaf(g.x, cot, acc[i].x);
+        acc[i].y = fmaf(g.y, cot, acc[i].y);
+      }
+    }
+    __syncwarp();
+  }
+  const int a = a_base + qd;
+  if (a < A) {
+    float2* o = out + ((size_t)blockIdx.y * A + a) * c.K;
+#pragma unroll
+    for (int i = 0; i < BPL; ++i) o[lp + 8 * i] = make_float2(acc[i].x - gsum.y, acc[i].y + gsum.x);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// JVP: out[a][k] = sum_s e1 D(k - k0) + e2 D'(k - k0) (reference:
+// dsplat/kernels/surfel.slang:144-221, jvp_bins). With the big-centre table the bin
+// nearest each peak first receives a finite stand-in; the quarter's owner lane replaces
+// it by the directly evaluated term through a per-warp correction row, in pair order.
+// ------------------------------------------------------------------------------------
+template <int BPL, int P>
+__global__ void __launch_bounds__(128) jvp_kernel(Consts c, const float* __restrict__ pos, int A,
+                                                  const float* __restrict__ cen,
+                                                  const float* __restrict__ nrm,
+                                                  const float2* __restrict__ w,
+                                                  const float* __restrict__ dcen,
+                                                  const float* __restrict__ dnrm,
+                                                  const float2* __restrict__ dw, int S,
+                                                  int seg_len, float2* __restrict__ out) {
+  constexpr int REC = 4 + 4 * P;  // tl, lobe, h1[P], h2[P], delta
+  extern __shared__ float smem[];
+  const int tbl_n = c.N + 8 * BPL;
+  const int tbl_pad = (tbl_n + 3) & ~3;
+  float* tbl = smem;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int qd = lane >> 3, lp = lane & 7;
+  float* recs = smem + tbl_pad + warp * (32 * 4 * REC + 4 * 2 * c.K);
+  float2* corr = reinterpret_cast<float2*>(recs + 32 * 4 * REC);  // [4][K]
+  for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) tbl[i] = tan_entry(i, c.N, true);
+  for (int i = lane; i < 4 * c.K; i += 32) corr[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+
+  const int a_base = (blockIdx.x * kWarps + warp) * 4;
+  float apx[4], apy[4], apz[4];
+  bool aok[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    int a = a_base + t;
+    aok[t] = a < A;
+    int ac = aok[t] ? a : 0;
+    apx[t] = __ldg(pos + 3 * ac);
+    apy[t] = __ldg(pos + 3 * ac + 1);
+    apz[t] = __ldg(pos + 3 * ac + 2);
+  }
+  float2 acc[BPL];
+#pragma unroll
+  for (int i = 0; i < BPL; ++i) acc[i] = make_float2(0.f, 0.f);
+  float2 csum = make_float2(0.f, 0.f);
+
+  const int s_begin = blockIdx.y * seg_len;
+  const int s_end = min(S, s_begin + seg_len);
+  for (int s0 = s_begin; s0 < s_end; s0 += 32) {
+    const int s = s0 + lane;
+    const bool sv = s < s_end;
+    float cx = 0.f, cy = 0.f, cz = 0.f, nx = 0.f, ny = 0.f, nz = 1.f;
+    float dcx = 0.f, dcy = 0.f, dcz = 0.f, dnx = 0.f, dny = 0.f, dnz = 0.f;
+    float2 ws = make_float2(0.f, 0.f), dws = make_float2(0.f, 0.f);
+    if (sv) {
+      cx = __ldg(cen + 3 * s); cy = __ldg(cen + 3 * s + 1); cz = __ldg(cen + 3 * s + 2);
+      nx = __ldg(nrm + 3 * s); ny = __ldg(nrm + 3 * s + 1); nz = __ldg(nrm + 3 * s + 2);
+      dcx = __ldg(dcen + 3 * s); dcy = __ldg(dcen + 3 * s + 1); dcz = __ldg(dcen + 3 * s + 2);
+      dnx = __ldg(dnrm + 3 * s); dny = __ldg(dnrm + 3 * s + 1); dnz = __ldg(dnrm + 3 * s + 2);
+      ws = ldg2(w + s);
+      dws = ldg2(dw + s);
+    }
+    bool any = false;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      Pair q;
+      pair_setup(c, apx[t], apy[t], apz[t], cx, cy, cz, nx, ny, nz, q);
+      const bool ok = sv && aok[t] && q.amp > 0.0f;
+      float* r = recs + (lane * 4 + t) * REC;
+      if (ok) {
+        const float dr = -(q.ux * dcx + q.uy * dcy + q.uz * dcz);
+        const float dcos = ((q.cosv * q.ux - nx) * dcx + (q.cosv * q.uy - ny) * dcy +
+                            (q.cosv * q.uz - nz) * dcz) * q.inv_r +
+                           q.ux * dnx + q.uy * dny + q.uz * dnz;
+        const float damp = -q.amp * dr * q.inv_r + q.amp_cos * dcos;
+        const float dphi = q.rate * dr;
+        // e1 = rot (w (damp + i amp dphi) + amp dw), e2 = -rot w amp kpm dr
+        float2 inner = cadd(cmul(ws, make_float2(damp, q.amp * dphi)), cscale(dws, q.amp));
+        const float2 e1 = cmul(q.rot, inner);
+        const float2 e2 = cscale(cmul(q.rot, ws), -q.amp * c.kpm * dr);
+        float2 nu[P];
+        numerators<P>(q.off, nu);
+        r[0] = q.tl;
+        r[1] = __int_as_float(q.lobe);
+        float2 h1_0 = make_float2(0.f, 0.f), h2_0 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+          const float2 qv = q_from_nu(nu[k]);
+          float2 h1 = cscale(cadd(cmul(e1, nu[k]), cscale(cmul(e2, qv), c.pi_P)), c.inv_S);
+          float2 h2 = cscale(cmul(e2, nu[k]), -c.pi_N * c.inv_S);
+          *reinterpret_cast<float2*>(r + 2 + 2 * k) = h1;
+          *reinterpret_cast<float2*>(r + 2 + 2 * P + 2 * k) = h2;
+          if (k == 0) { h1_0 = h1; h2_0 = h2; }
+        }
+        float2 delta = make_float2(0.f, 0.f);
+        if (q.lobe < c.K) {
+          float2 d0, d1;
+          dirichlet_near(q.off, c.S, c.N, d0, d1);
+          const float cg = cot_from(kBig, q.tl);
+          // stand-in the sweep adds at the nearest bin: h1 (cg + i) + h2 (1 + cg^2)
+          float2 stand = cadd(cmul(h1_0, make_float2(cg, 1.0f)), cscale(h2_0, 1.0f + cg * cg));
+          delta = csub(cadd(cmul(e1, d0), cmul(e2, d1)), stand);
+        }
+        *reinterpret_cast<float2*>(r + 2 + 4 * P) = delta;
+      } else {
+        r[0] = 1.0f;
+        r[1] = __int_as_float(c.N - 1);  // m = k - lobe never 0 on observed bins
+#pragma unroll
+        for (int k = 0; k < 2 * P + 1; ++k) *reinterpret_cast<float2*>(r + 2 + 2 * k) = make_float2(0.f, 0.f);
+      }
+      any |= ok;
+    }
+    const unsigned mask = __ballot_sync(kFull, any);
+    __syncwarp();
+    const int nb = min(32, s_end - s0);
+    for (int j = 0; j < nb; ++j) {
+      if (!((mask >> j) & 1u)) continue;
+      const float* r = recs + (j * 4 + qd) * REC;
+      const float tl = r[0];
+      const int lobe = __float_as_int(r[1]);
+      const int cls = (lp - lobe) & (P - 1);
+      const float2 h1 = *reinterpret_cast<const float2*>(r + 2 + 2 * cls);
+      const float2 h2 = *reinterpret_cast<const float2*>(r + 2 + 2 * P + 2 * cls);
+      csum.x += h2.x - h1.y;
+      csum.y += h2.y + h1.x;
+      const float* tb = tbl + (lp - lobe + c.N - 1);
+#pragma unroll
+      for (int i = 0; i < BPL; ++i) {
+        const float cot = cot_from(tb[8 * i], tl);
+        const float cot2 = cot * cot;
+        acc[i].x = fmaf(h1.x, cot, fmaf(h2.x, cot2, acc[i].x));
+        acc[i].y = fmaf(h1.y, cot, fmaf(h2.y, cot2, acc[i].y));
+      }
+      if (lobe < c.K && (lobe & 7) == lp) {
+        const float2 d = *reinterpret_cast<const float2*>(r + 2 + 4 * P);
+        float2 cur = corr[qd * c.K + lobe];
+        corr[qd * c.K + lobe] = cadd(cur, d);
+      }
+    }
+    __syncwarp();
+  }
+  const int a = a_base + qd;
+  if (a < A) {
+    float2* o = out + ((size_t)blockIdx.y * A + a) * c.K;
+#pragma unroll
+    for (int i = 0; i < BPL; ++i) {
+      const int k = lp + 8 * i;
+      const float2 cr = corr[qd * c.K + k];
+      o[k] = make_float2(acc[i].x + csum.x + cr.x, acc[i].y + csum.y + cr.y);
+    }
+  }
+}
+
+// Sum of segment partials [segments][n] into out[n], in segment order.
+__global__ void segment_sum_kernel(const float2* __restrict__ partial, int segments, int64_t n,
+                                   float2* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 s = partial[i];
+  for (int g = 1; g < segments; ++g) {
+    float2 v = partial[(int64_t)g * n + i];
+    s.x += v.x;
+    s.y += v.y;
+  }
+  out[i] = s;
+}
+
+// ------------------------------------------------------------------------------------
+// Aperture-reduced family. Per pair the sufficient statistics over all bins
+//   Z0 = sum conj(D) r, Z1 = sum conj(D') r, N0 = sum |D|^2, N1 = sum Re(conj(D) D')
+// are chained to the outputs and summed over the CTA's aperture chunk in order.
+// MODE 0: correlate (corr, norm). 1/2: correlate_gradient, width 3/6. 3: vjp.
+// Reference: dsplat/kernels/correlate.slang:75-108 (surfel_correlate), :171-235
+// (surfel_correlate_gradient), dsplat/kernels/surfel.slang:223-311 (vjp_bins).
+// ------------------------------------------------------------------------------------
+template <int MODE>
+struct ModeInfo;
+template <> struct ModeInfo<0> { static constexpr int NV = 3; static constexpr int W = 0; };
+template <> struct ModeInfo<1> { static constexpr int NV = 12; static constexpr int W = 3; };
+template <> struct ModeInfo<2> { static constexpr int NV = 21; static constexpr int W = 6; };
+template <> struct ModeInfo<3> { static constexpr int NV = 8; static constexpr int W = 0; };
+
+template <int P>
+__host__ __device__ constexpr int reduce_record() { return 16 + 2 * P; }
+
+template <int BPL, int P, int MODE>
+__global__ void __launch_bounds__(128) reduce_kernel(Consts c, const float* __restrict__ pos, int A,
+                                                     const float* __restrict__ cen,
+                                                     const float* __restrict__ nrm,
+                                                     const float2* __restrict__ w, int S,
+                                                     const float2* __restrict__ res,
+                                                     int chunk_len, int chunks,
+                                                     float* __restrict__ partial) {
+  constexpr int NV = ModeInfo<MODE>::NV;
+  constexpr bool kGrad = MODE == 1 || MODE == 2;
+  constexpr bool kNorm = MODE != 3;
+  constexpr bool kDeriv = MODE != 0;
+  // record: tl, lobe, nu[P], d0, d1, amp, amp_cos, ux, uy, uz, cos, inv_r, rate, rot
+  constexpr int R_NU = 2, R_D0 = 2 + 2 * P, R_D1 = R_D0 + 2, R_AMP = R_D1 + 2;
+  constexpr int R_AMPC = R_AMP + 1, R_U = R_AMPC + 1, R_COS = R_U + 3, R_INVR = R_COS + 1;
+  constexpr int R_RATE = R_INVR + 1, R_ROT = R_RATE + 1;
+  constexpr int REC = reduce_record<P>();
+  static_assert(REC >= R_ROT + 2, "record layout");
+  extern __shared__ float smem[];
+  const int tbl_n = c.N + 8 * BPL;
+  const int tbl_pad = (tbl_n + 3) & ~3;
+  float* tbl = smem;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int qd = lane >> 3, lp = lane & 7;
+  float* recs = smem + tbl_pad + warp * (32 * REC);
+  for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) tbl[i] = tan_entry(i, c.N, true);
+  __syncthreads();
+
+  const int s = (blockIdx.x * kWarps + warp) * 4 + qd;
+  const bool s_ok = s < S;
+  const int sc = s_ok ? s : 0;
+  const float cx = __ldg(cen + 3 * sc), cy = __ldg(cen + 3 * sc + 1), cz = __ldg(cen + 3 * sc + 2);
+  const float nx = __ldg(nrm + 3 * sc), ny = __ldg(nrm + 3 * sc + 1), nz = __ldg(nrm + 3 * sc + 2);
+  float2 ws = make_float2(0.f, 0.f);
+  if (MODE == 3) ws = ldg2(w + sc);
+
+  float accv[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) accv[v] = 0.0f;
+
+  const int a_begin = blockIdx.y * chunk_len;
+  const int a_end = min(A, a_begin + chunk_len);
+  const float pi_P = c.pi_P, pi_N = c.pi_N, inv_S = c.inv_S;
+  for (int a0 = a_begin; a0 < a_end; a0 += 8) {
+    {  // pair geometry: lane (lp, qd) takes aperture a0 + lp with its quarter's surfel
+      const int aa = a0 + lp;
+      const bool ok = s_ok && aa < a_end;
+      float* r = recs + (lp * 4 + qd) * REC;
+      Pair q;
+      const int ac = ok ? aa : 0;
+      pair_setup(c, __ldg(pos + 3 * ac), __ldg(pos + 3 * ac + 1), __ldg(pos + 3 * ac + 2), cx, cy,
+                 cz, nx, ny, nz, q);
+      if (ok && q.amp > 0.0f) {
+        float2 nu[P];
+        numerators<P>(q.off, nu);
+        r[0] = q.tl;
+        r[1] = __int_as_float(q.lobe);
+#pragma unroll
+        for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + R_NU + 2 * k) = nu[k];
+        float2 d0 = make_float2(0.f, 0.f), d1 = make_float2(0.f, 0.f);
+        if (q.lobe < c.K) dirichlet_near(q.off, c.S, c.N, d0, d1);
+        *reinterpret_cast<float2*>(r + R_D0) = d0;
+        *reinterpret_cast<float2*>(r + R_D1) = d1;
+        r[R_AMP] = q.amp;
+        r[R_AMPC] = q.amp_cos;
+        r[R_U] = q.ux;
+        r[R_U + 1] = q.uy;
+        r[R_U + 2] = q.uz;
+        r[R_COS] = q.cosv;
+        r[R_INVR] = q.inv_r;
+        r[R_RATE] = q.rate;
+        r[R_ROT] = q.rot.x;
+        r[R_ROT + 1] = q.rot.y;
+      } else {
+        for (int k = 0; k < REC; ++k) r[k] = 0.0f;
+        r[0] = 1.0f;
+        r[1] = __int_as_float(c.N - 1);
+      }
+    }
+    __syncwarp();
+    const int nb = min(8, a_end - a0);
+    for (int j = 0; j < nb; ++j) {
+      const float* r = recs + (j * 4 + qd) * REC;
+      const float amp = r[R_AMP];
+      if (__ballot_sync(kFull, amp > 0.0f) == 0u) continue;
+      const float2* row = res + (size_t)(a0 + j) * c.K;
+      float2 u[BPL];
+      float2 ru = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int i = 0; i < BPL; ++i) {
+        u[i] = ldg2(row + lp + 8 * i);
+        ru.x += u[i].x;
+        ru.y += u[i].y;
+      }
+      const float tl = r[0];
+      const int lobe = __float_as_int(r[1]);
+      const int cls = (lp - lobe) & (P - 1);
+      const float* tb = tbl + (lp - lobe + c.N - 1);
+      float2 sa = make_float2(0.f, 0.f), sb = make_float2(0.f, 0.f);
+      float c1 = 0.f, c2 = 0.f, c3 = 0.f;
+#pragma unroll
+      for (int i = 0; i < BPL; ++i) {
+        const float cot = cot_from(tb[8 * i], tl);
+        sa.x = fmaf(cot, u[i].x, sa.x);
+        sa.y = fmaf(cot, u[i].y, sa.y);
+        if (kDeriv) {
+          const float cot2 = cot * cot;
+          sb.x = fmaf(cot2, u[i].x, sb.x);
+          sb.y = fmaf(cot2, u[i].y, sb.y);
+          if (kGrad) {
+            c1 += cot;
+            c3 = fmaf(cot2, cot, c3);
+          }
+        }
+        if (kNorm) c2 = fmaf(cot, cot, c2);
+      }
+      float nc = (float)BPL;
+      const bool near = lobe < c.K;
+      const float2 ul = near ? ldg2(row + lobe) : make_float2(0.f, 0.f);
+      if (near && (lobe & 7) == lp) {  // remove the stand-in of the nearest bin
+        const float cg = cot_from(kBig, tl);
+        const float cg2 = cg * cg;
+        sa.x -= cg * ul.x; sa.y -= cg * ul.y;
+        sb.x -= cg2 * ul.x; sb.y -= cg2 * ul.y;
+        c1 -= cg; c2 -= cg2; c3 -= cg2 * cg;
+        ru.x -= ul.x; ru.y -= ul.y;
+        nc -= 1.0f;
+      }
+#pragma unroll
+      for (int o = P; o < 8; o <<= 1) {
+        sa.x += __shfl_xor_sync(kFull, sa.x, o);
+        sa.y += __shfl_xor_sync(kFull, sa.y, o);
+        ru.x += __shfl_xor_sync(kFull, ru.x, o);
+        ru.y += __shfl_xor_sync(kFull, ru.y, o);
+        if (kDeriv) {
+          sb.x += __shfl_xor_sync(kFull, sb.x, o);
+          sb.y += __shfl_xor_sync(kFull, sb.y, o);
+        }
+        if (kNorm) {
+          c2 += __shfl_xor_sync(kFull, c2, o);
+          nc += __shfl_xor_sync(kFull, nc, o);
+        }
+        if (kGrad) {
+          c1 += __shfl_xor_sync(kFull, c1, o);
+          c3 += __shfl_xor_sync(kFull, c3, o);
+        }
+      }
+      const float2 nu = *reinterpret_cast<const float2*>(r + R_NU + 2 * cls);
+      const float2 qv = q_from_nu(nu);
+      const float2 amir = make_float2(sa.x + ru.y, sa.y - ru.x);  // A - i R
+      float2 z0 = cscale(cmulc(nu, amir), inv_S);
+      float2 z1 = make_float2(0.f, 0.f);
+      float n0 = 0.f, n1 = 0.f;
+      if (kDeriv) {
+        const float2 rb = make_float2(ru.x + sb.x, ru.y + sb.y);
+        z1 = cscale(csub(cscale(cmulc(qv, amir), pi_P), cscale(cmulc(nu, rb), pi_N)), inv_S);
+      }
+      const float nn = nu.x * nu.x + nu.y * nu.y;
+      if (kNorm) n0 = nn * (c2 + nc) * inv_S * inv_S;
+      if (kGrad) {
+        const float re_nq = nu.x * qv.x + nu.y * qv.y;
+        n1 = (pi_P * re_nq * (c2 + nc) - pi_N * nn * (c1 + c3)) * inv_S * inv_S;
+      }
+#pragma unroll
+      for (int o = 1; o < P; o <<= 1) {
+        z0.x += __shfl_xor_sync(kFull, z0.x, o);
+        z0.y += __shfl_xor_sync(kFull, z0.y, o);
+        if (kDeriv) {
+          z1.x += __shfl_xor_sync(kFull, z1.x, o);
+          z1.y += __shfl_xor_sync(kFull, z1.y, o);
+        }
+        if (kNorm) n0 += __shfl_xor_sync(kFull, n0, o);
+        if (kGrad) n1 += __shfl_xor_sync(kFull, n1, o);
+      }
+      if (near) {
+        const float2 d0 = *reinterpret_cast<const float2*>(r + R_D0);
+        const float2 d1 = *reinterpret_cast<const float2*>(r + R_D1);
+        z0 = cadd(z0, cmulc(d0, ul));
+        if (kDeriv) z1 = cadd(z1, cmulc(d1, ul));
+        if (kNorm) n0 += d0.x * d0.x + d0.y * d0.y;
+        if (kGrad) n1 += d0.x * d1.x + d0.y * d1.y;
+      }
+      // chain to the outputs
+      const float2 rot = make_float2(r[R_ROT], r[R_ROT + 1]);
+      const float2 e0 = cmulc(rot, z0);
+      if (MODE == 0) {
+        accv[0] += amp * e0.x;
+        accv[1] += amp * e0.y;
+        accv[2] += amp * amp * n0;
+      } else {
+        const float2 e1 = cmulc(rot, z1);
+        const float amp_cos = r[R_AMPC], cosv = r[R_COS], inv_r = r[R_INVR], rate = r[R_RATE];
+        const float uu[3] = {r[R_U], r[R_U + 1], r[R_U + 2]};
+        const float nv[3] = {nx, ny, nz};
+        // kpm E1 + i rate E0
+        const float2 inner = make_float2(c.kpm * e1.x - rate * e0.y, c.kpm * e1.y + rate * e0.x);
+        if (kGrad) {
+          constexpr int W = ModeInfo<MODE>::W;
+          accv[0] += amp * e0.x;
+          accv[1] += amp * e0.y;
+          accv[2] += amp * amp * n0;
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            const float da = (amp * uu[jj] + amp_cos * (cosv * uu[jj] - nv[jj])) * inv_r;
+            const float au = amp * uu[jj];
+            accv[3 + jj] += da * e0.x + au * inner.x;
+            accv[3 + W + jj] += da * e0.y + au * inner.y;
+            accv[3 + 2 * W + jj] += 2.0f * amp * (da * n0 + au * c.kpm * n1);
+            if (W == 6) {
+              const float acu = amp_cos * uu[jj];
+              accv[6 + jj] += acu * e0.x;
+              accv[3 + W + 3 + jj] += acu * e0.y;
+              accv[3 + 2 * W + 3 + jj] += 2.0f * amp * acu * n0;
+            }
+          }
+        } else {  // VJP: Re(conj(w) dcorr) per coordinate, and corr for the weight
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            const float da = (amp * uu[jj] + amp_cos * (cosv * uu[jj] - nv[jj])) * inv_r;
+            const float au = amp * uu[jj];
+            const float2 dcj = make_float2(da * e0.x + au * inner.x, da * e0.y + au * inner.y);
+            accv[jj] += ws.x * dcj.x + ws.y * dcj.y;
+            const float acu = amp_cos * uu[jj];
+            accv[3 + jj] += acu * (ws.x * e0.x + ws.y * e0.y);
+          }
+          accv[6] += amp * e0.x;
+          accv[7] += amp * e0.y;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (lp == 0 && s_ok) {
+    float* p = partial + ((size_t)s * chunks + blockIdx.y) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) p[v] = accv[v];
+  }
+}
+
+// Double-precision, fixed-order sum of chunk partials; scatters to the outputs.
+template <int MODE>
+__global__ void chunk_sum_kernel(const float* __restrict__ partial, int S, int chunks,
+                                 float* __restrict__ o0, float* __restrict__ o1,
+                                 float* __restrict__ o2, float* __restrict__ o3) {
+  constexpr int NV = ModeInfo<MODE>::NV;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  double t[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) t[v] = 0.0;
+  for (int g = 0; g < chunks; ++g) {
+    const float* p = partial + ((size_t)s * chunks + g) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) t[v] += (double)p[v];
+  }
+  if (MODE == 0) {  // corr [S,2], norm [S]
+    o0[2 * s] = (float)t[0];
+    o0[2 * s + 1] = (float)t[1];
+    o1[s] = (float)t[2];
+  } else if (MODE == 3) {  // grad centers [S,3], normals [S,3], weights [S,2]
+    for (int j = 0; j < 3; ++j) {
+      o0[3 * s + j] = (float)t[j];
+      o1[3 * s + j] = (float)t[3 + j];
+    }
+    o2[2 * s] = (float)t[6];
+    o2[2 * s + 1] = (float)t[7];
+  } else {  // corr, norm, dcorr [S,W,2], dnorm [S,W]
+    constexpr int W = ModeInfo<MODE>::W;
+    o0[2 * s] = (float)t[0];
+    o0[2 * s + 1] = (float)t[1];
+    o1[s] = (float)t[2];
+    for (int j = 0; j < W; ++j) {
+      o2[(s * W + j) * 2] = (float)t[3 + j];
+      o2[(s * W + j) * 2 + 1] = (float)t[3 + W + j];
+      o3[s * W + j] = (float)t[3 + 2 * W + j];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Dictionary rows c sqrt(area) D(k - k0) (reference: dsplat/kernels/surfel.slang:313-378).
+// Thread = (surfel, aperture); adjacent threads take adjacent surfels, so every bin's
+// store is coalesced. real: row (2k + part) A + a; else [a K + k, s] complex.
+// ------------------------------------------------------------------------------------
+template <int P>
+__global__ void __launch_bounds__(128) design_kernel(Consts c, const float* __restrict__ pos, int A,
+                                                     const float* __restrict__ cen,
+                                                     const float* __restrict__ nrm,
+                                                     const float* __restrict__ areas, int S,
+                                                     int real, float* __restrict__ out) {
+  extern __shared__ float smem[];
+  const int tbl_n = c.N + c.K;
+  for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) smem[i] = tan_entry(i, c.N, false);
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  if (s >= S) return;
+  Pair q;
+  pair_setup(c, __ldg(pos + 3 * a), __ldg(pos + 3 * a + 1), __ldg(pos + 3 * a + 2),
+             __ldg(cen + 3 * s), __ldg(cen + 3 * s + 1), __ldg(cen + 3 * s + 2),
+             __ldg(nrm + 3 * s), __ldg(nrm + 3 * s + 1), __ldg(nrm + 3 * s + 2), q);
+  float2 g[P];
+  const bool vis = q.amp > 0.0f;
+  if (vis) {
+    float2 cw = cscale(q.rot, q.amp * sqrtf(__ldg(areas + s)) * c.inv_S);
+    float2 nu[P];
+    numerators<P>(q.off, nu);
+#pragma unroll
+    for (int k = 0; k < P; ++k) g[k] = cmul(cw, nu[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < P; ++k) g[k] = make_float2(0.f, 0.f);
+  }
+  const float* tb = smem + (c.N - 1 - q.lobe);
+  for (int k0 = 0; k0 < c.K; k0 += P) {
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      const int k = k0 + j;
+      float2 term = make_float2(0.f, 0.f);
+      if (vis) {
+        const float cot = cot_from(tb[k], q.tl);
+        const float2 gg = g[(k - q.lobe) & (P - 1)];
+        term = make_float2(gg.x * cot - gg.y, gg.y * cot + gg.x);
+      }
+      if (real) {
+        out[((size_t)(2 * k) * A + a) * S + s] = term.x;
+        out[((size_t)(2 * k + 1) * A + a) * S + s] = term.y;
+      } else {
+        reinterpret_cast<float2*>(out)[((size_t)a * c.K + k) * S + s] = term;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Explicit columns and their center/normal derivatives, without area (reference:
+// dsplat/kernels/correlate.slang:237-281). Thread = (surfel, aperture), loop over bins.
+// ------------------------------------------------------------------------------------
+template <int P>
+__global__ void __launch_bounds__(128) jacobian_kernel(Consts c, const float* __restrict__ pos,
+                                                       int A, const float* __restrict__ cen,
+                                                       const float* __restrict__ nrm, int S,
+                                                       float2* __restrict__ cols,
+                                                       float2* __restrict__ jac) {
+  extern __shared__ float smem[];
+  const int tbl_n = c.N + c.K;
+  for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) smem[i] = tan_entry(i, c.N, true);
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  if (s >= S) return;
+  const float nv[3] = {__ldg(nrm + 3 * s), __ldg(nrm + 3 * s + 1), __ldg(nrm + 3 * s + 2)};
+  Pair q;
+  pair_setup(c, __ldg(pos + 3 * a), __ldg(pos + 3 * a + 1), __ldg(pos + 3 * a + 2),
+             __ldg(cen + 3 * s), __ldg(cen + 3 * s + 1), __ldg(cen + 3 * s + 2), nv[0], nv[1],
+             nv[2], q);
+  const bool vis = q.amp > 0.0f;
+  float2 nu[P];
+  numerators<P>(q.off, nu);
+  float2 d0 = make_float2(0.f, 0.f), d1 = make_float2(0.f, 0.f);
+  dirichlet_near(q.off, c.S, c.N, d0, d1);
+  const float uu[3] = {q.ux, q.uy, q.uz};
+  float da[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) da[j] = (q.amp * uu[j] + q.amp_cos * (q.cosv * uu[j] - nv[j])) * q.inv_r;
+  const float* tb = smem + (c.N - 1 - q.lobe);
+  for (int k = 0; k < c.K; ++k) {
+    const size_t e = ((size_t)a * c.K + k) * S + s;
+    if (!vis) {
+      cols[e] = make_float2(0.f, 0.f);
+      for (int j = 0; j < 6; ++j) jac[e * 6 + j] = make_float2(0.f, 0.f);
+      continue;
+    }
+    float2 D, Dp;
+    if (k == q.lobe) {
+      D = d0;
+      Dp = d1;
+    } else {
+      const float cot = cot_from(tb[k], q.tl);
+      const int cls = (k - q.lobe) & (P - 1);
+      const float2 n = nu[cls], qv = q_from_nu(n);
+      const float2 ci = make_float2(cot, 1.0f);
+      D = cscale(cmul(n, ci), c.inv_S);
+      Dp = cscale(csub(cscale(cmul(qv, ci), c.pi_P), cscale(n, c.pi_N * (1.0f + cot * cot))), c.inv_S);
+    }
+    const float2 z = cmul(D, q.rot);
+    const float2 dz = cmul(Dp, q.rot);
+    cols[e] = cscale(z, q.amp);
+    // d col / d c_j = da_j z + amp u_j (kpm dz - i rate z)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float au = q.amp * uu[j];
+      float2 v = make_float2(da[j] * z.x + au * (c.kpm * dz.x + q.rate * z.y),
+                             da[j] * z.y + au * (c.kpm * dz.y - q.rate * z.x));
+      jac[e * 6 + j] = v;
+      jac[e * 6 + 3 + j] = cscale(z, q.amp_cos * uu[j]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Normal-bank scores (reference: dsplat/kernels/correlate.slang:110-169). Thread =
+// candidate; the aperture loop is sequential, so every sum has a fixed order. The
+// per-aperture correlation comes either from the exact bin sum or from Catmull-Rom
+// interpolation of an oversampled FFT range table.
+// ------------------------------------------------------------------------------------
+constexpr int kBankChunk = 32;
+
+template <int P>
+__global__ void __launch_bounds__(128) orientations_kernel(
+    Consts c, const float* __restrict__ pos, int A, const float* __restrict__ cen,
+    const float* __restrict__ nrm, int C, const float* __restrict__ bank, int bank_size,
+    int j_begin, const float2* __restrict__ res, const float2* __restrict__ table,
+    const float* __restrict__ norm_table, int oversample, float* __restrict__ out) {
+  extern __shared__ float smem[];
+  const int tbl_n = c.N + c.K;
+  float* tbl = smem;
+  float* bk = smem + ((tbl_n + 3) & ~3);
+  const int nj = min(kBankChunk, bank_size + 1 - j_begin);
+  if (table == nullptr)
+    for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) tbl[i] = tan_entry(i, c.N, true);
+  for (int i = threadIdx.x; i < 3 * nj; i += blockDim.x) {
+    const int j = j_begin + i / 3;
+    bk[i] = j == 0 ? 0.0f : __ldg(bank + 3 * (j - 1) + i % 3);
+  }
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= C) return;
+  const float cx = __ldg(cen + 3 * s), cy = __ldg(cen + 3 * s + 1), cz = __ldg(cen + 3 * s + 2);
+  const float own[3] = {__ldg(nrm + 3 * s), __ldg(nrm + 3 * s + 1), __ldg(nrm + 3 * s + 2)};
+  float acc[kBankChunk][3];
+#pragma unroll
+  for (int j = 0; j < kBankChunk; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0f;
+  const int size = c.N * oversample;
+  for (int a = 0; a < A; ++a) {
+    Pair q;
+    pair_setup(c, __ldg(pos + 3 * a), __ldg(pos + 3 * a + 1), __ldg(pos + 3 * a + 2), cx, cy, cz,
+               own[0], own[1], own[2], q);
+    float2 corr;
+    float norm;
+    if (table != nullptr) {
+      // x = k0 * oversample with k0 = lobe - off
+      const float x = ((float)q.lobe - q.off) * (float)oversample;
+      const float fb = floorf(x);
+      const float t = x - fb;
+      const int base = (int)fb;
+      const float t2 = t * t, t3 = t2 * t;
+      const float wts[4] = {-0.5f * t + t2 - 0.5f * t3, 1.0f - 2.5f * t2 + 1.5f * t3,
+                            0.5f * t + 2.0f * t2 - 1.5f * t3, -0.5f * t2 + 0.5f * t3};
+      float2 v = make_float2(0.f, 0.f);
+      float nn = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int k = (base + j - 1) % size;
+        if (k < 0) k += size;
+        const float2 tv = ldg2(table + (size_t)a * size + k);
+        v.x += wts[j] * tv.x;
+        v.y += wts[j] * tv.y;
+        nn += wts[j] * __ldg(norm_table + k);
+      }
+      corr = cmulc(q.rot, v);  // value * conj(rot)... conj(rot) * v
+      norm = fmaxf(nn, 0.0f);
+    } else {
+      float2 nu[P];
+      numerators<P>(q.off, nu);
+      float2 z = make_float2(0.f, 0.f);
+      float n0 = 0.0f;
+      const float* tb = tbl + (c.N - 1 - q.lobe);
+      const float2* row = res + (size_t)a * c.K;
+      for (int k = 0; k < c.K; ++k) {
+        float2 D;
+        if (k == q.lobe) {
+          float2 d1;
+          dirichlet_near(q.off, c.S, c.N, D, d1);
+        } else {
+          const float cot = cot_from(tb[k], q.tl);
+          D = cscale(cmul(nu[(k - q.lobe) & (P - 1)], make_float2(cot, 1.0f)), c.inv_S);
+        }
+        z = cadd(z, cmulc(D, ldg2(row + k)));
+        n0 += D.x * D.x + D.y * D.y;
+      }
+      corr = cmulc(q.rot, z);
+      norm = n0;
+    }
+#pragma unroll
+    for (int j = 0; j < kBankChunk; ++j) {
+      if (j < nj) {
+        const bool self = (j_begin + j) == 0;
+        const float ex = self ? own[0] : bk[3 * j];
+        const float ey = self ? own[1] : bk[3 * j + 1];
+        const float ez = self ? own[2] : bk[3 * j + 2];
+        const float cosv = q.ux * ex + q.uy * ey + q.uz * ez;
+        float amp, amp_cos;
+        scattering(c, cosv, q.inv_r, amp, amp_cos);
+        acc[j][0] += amp * corr.x;
+        acc[j][1] += amp * corr.y;
+        acc[j][2] += amp * amp * norm;
+      }
+    }
+  }
+  float* o = out + (size_t)s * (bank_size + 1) * 3;
+#pragma unroll
+  for (int j = 0; j < kBankChunk; ++j) {
+    if (j < nj) {
+      o[3 * (j_begin + j)] = acc[j][0];
+      o[3 * (j_begin + j) + 1] = acc[j][1];
+      o[3 * (j_begin + j) + 2] = acc[j][2];
+    }
+  }
+}
+
+}  // namespace dsg
+
+// ======================================================================================
+// Host side
+// ======================================================================================
+using namespace dsg;
+
+namespace {
+
+constexpr int kTargetCtas = 152 * 6;
+
+bool chirp_ok(const DsgChirp* c) {
+  if (!c) return false;
+  if (c->samples <= 0 || c->pad <= 0 || c->n_fft != c->samples * c->pad) return false;
+  if (c->num_bins != c->n_fft / 2) return false;
+  if (!(c->pad == 1 || c->pad == 2 || c->pad == 4)) return false;
+  const int K = c->num_bins;
+  return K == 32 || K == 64 || K == 128 || K == 256;
+}
+
+int render_segments(const DsgChirp* c, int A, int S) {
+  const int tiles = (A + 15) / 16;
+  int seg = (kTargetCtas + tiles - 1) / tiles;
+  const int max_seg = (S + 31) / 32;
+  if (seg > max_seg) seg = max_seg;
+  if (seg < 1) seg = 1;
+  (void)c;
+  return seg;
+}
+
+int reduce_chunks(int A, int S) {
+  const int tiles = (S + 15) / 16;
+  int ch = (kTargetCtas + tiles - 1) / tiles;
+  const int max_ch = (A + 7) / 8;
+  if (ch > max_ch) ch = max_ch;
+  if (ch < 1) ch = 1;
+  return ch;
+}
+
+int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
+}
+
+template <typename F>
+int dispatch_kp(int K, int P, F&& f) {
+  // f.template operator()<BPL, P>()
+  switch (K) {
+    case 32:
+      if (P == 1) return f.template run<4, 1>();
+      if (P == 2) return f.template run<4, 2>();
+      return f.template run<4, 4>();
+    case 64:
+      if (P == 1) return f.template run<8, 1>();
+      if (P == 2) return f.template run<8, 2>();
+      return f.template run<8, 4>();
+    case 128:
+      if (P == 1) return f.template run<16, 1>();
+      if (P == 2) return f.template run<16, 2>();
+      return f.template run<16, 4>();
+    case 256:
+      if (P == 1) return f.template run<32, 1>();
+      if (P == 2) return f.template run<32, 2>();
+      return f.template run<32, 4>();
+  }
+  return DSG_ERR_UNSUPPORTED;
+}
+
+template <typename F>
+int dispatch_p(int P, F&& f) {
+  if (P == 1) return f.template run<1>();
+  if (P == 2) return f.template run<2>();
+  if (P == 4) return f.template run<4>();
+  return DSG_ERR_UNSUPPORTED;
+}
+
+size_t table_floats(int N, int K) { return (size_t)((N + K + 8 + 3) & ~3); }
+
+struct RenderLaunch {
+  Consts c; const float* pos; int A; const float* cen; const float* nrm; const float2* w; int S;
+  float2* out; float2* partial; int seg; cudaStream_t st;
+  template <int BPL, int P>
+  int run() {
+    constexpr int REC = 2 + 2 * P;
+    const size_t smem = (table_floats(c.N, 8 * BPL) + kWarps * 32 * 4 * REC) * sizeof(float);
+    auto kern = render_kernel<BPL, P>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int seg_len = ((S + seg - 1) / seg + 31) / 32 * 32;
+    const int nseg = (S + seg_len - 1) / seg_len;
+    dim3 grid((A + 15) / 16, nseg > 0 ? nseg : 1);
+    float2* dst = grid.y == 1 ? out : partial;
+    kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, seg_len, dst);
+    if (grid.y > 1) {
+      const int64_t n = (int64_t)A * c.K;
+      segment_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(partial, grid.y, n, out);
+    }
+    return launch_status();
+  }
+};
+
+struct JvpLaunch {
+  Consts c; const float* pos; int A; const float* cen; const float* nrm; const float2* w;
+  const float* dcen; const float* dnrm; const float2* dw; int S; float2* out; float2* partial;
+  int seg; cudaStream_t st;
+  template <int BPL, int P>
+  int run() {
+    constexpr int REC = 4 + 4 * P;
+    const size_t smem = (table_floats(c.N, 8 * BPL) + kWarps * (32 * 4 * REC + 8 * c.K)) * sizeof(float);
+    auto kern = jvp_kernel<BPL, P>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int seg_len = ((S + seg - 1) / seg + 31) / 32 * 32;
+    const int nseg = (S + seg_len - 1) / seg_len;
+    dim3 grid((A + 15) / 16, nseg > 0 ? nseg : 1);
+    float2* dst = grid.y == 1 ? out : partial;
+    kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, dcen, dnrm, dw, S, seg_len, dst);
+    if (grid.y > 1) {
+      const int64_t n = (int64_t)A * c.K;
+      segment_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(partial, grid.y, n, out);
+    }
+    return launch_status();
+  }
+};
+
+template <int MODE>
+struct ReduceLaunch {
+  Consts c; const float* pos; int A; const float* cen; const float* nrm; const float2* w; int S;
+  const float2* res; float* partial; float* o0; float* o1; float* o2; float* o3; cudaStream_t st;
+  template <int BPL, int P>
+  int run() {
+    constexpr int REC = reduce_record<P>();
+    const size_t smem = (table_floats(c.N, 8 * BPL) + kWarps * 32 * REC) * sizeof(float);
+    auto kern = reduce_kernel<BPL, P, MODE>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int chunks = reduce_chunks(A, S);
+    const int chunk_len = ((A + chunks - 1) / chunks + 7) / 8 * 8;
+    const int nch = (A + chunk_len - 1) / chunk_len;
+    dim3 grid((S + 15) / 16, nch);
+    kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, res, chunk_len, nch, partial);
+    chunk_sum_kernel<MODE><<<(S + 127) / 128, 128, 0, st>>>(partial, S, nch, o0, o1, o2, o3);
+    return launch_status();
+  }
+};
+
+struct DesignLaunch {
+  Consts c; const float* pos; int A; const float* cen; const float* nrm; const float* areas; int S;
+  int real; float* out; cudaStream_t st;
+  template <int P>
+  int run() {
+    const size_t smem = table_floats(c.N, c.K) * sizeof(float);
+    dim3 grid((S + 127) / 128, A);
+    design_kernel<P><<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, areas, S, real, out);
+    return launch_status();
+  }
+};
+
+struct JacobianLaunch {
+  Consts c; const float* pos; int A; const float* cen; const float* nrm; int S;
+  float2* cols; float2* jac; cudaStream_t st;
+  template <int P>
+  int run() {
+    const size_t smem = table_floats(c.N, c.K) * sizeof(float);
+    dim3 grid((S + 127) / 128, A);
+    jacobian_kernel<P><<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, S, cols, jac);
+    return launch_status();
+  }
+};
+
+struct OrientLaunch {
+  Consts c; const float* pos; int A; const float* cen; const float* nrm; int C; const float* bank;
+  int nb; const float2* res; const float2* table; const float* ntab; int ov; float* out;
+  cudaStream_t st;
+  template <int P>
+  int run() {
+    const size_t smem = (table_floats(c.N, c.K) + 3 * kBankChunk) * sizeof(float);
+    for (int j0 = 0; j0 < nb + 1; j0 += kBankChunk) {
+      orientations_kernel<P><<<(C + 127) / 128, 128, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
+                                                                 j0, res, table, ntab, ov, out);
+    }
+    return launch_status();
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+size_t dsg_surfel_render_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels) {
+  if (!chirp_ok(chirp) || apertures <= 0 || surfels <= 0) return 0;
+  const int seg = render_segments(chirp, apertures, surfels);
+  if (seg <= 1) return 0;
+  return (size_t)seg * apertures * chirp->num_bins * 2 * sizeof(float);
+}
+
+int dsg_surfel_render(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                      const float* centers, const float* normals, const float* weights,
+                      int32_t surfels, float* out, void* workspace, size_t workspace_bytes,
+                      void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || surfels < 0 || (apertures > 0 && (!positions || !out))) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (apertures == 0) return DSG_OK;
+  if (surfels == 0) {
+    cudaMemsetAsync(out, 0, (size_t)apertures * chirp->num_bins * 2 * sizeof(float), st);
+    return launch_status();
+  }
+  if (!centers || !normals || !weights) return DSG_ERR_ARGUMENT;
+  const size_t need = dsg_surfel_render_workspace_bytes(chirp, apertures, surfels);
+  if (need > 0 && (workspace == nullptr || workspace_bytes < need)) return DSG_ERR_WORKSPACE;
+  RenderLaunch L{make_consts(*chirp), positions, apertures, centers, normals,
+                 reinterpret_cast<const float2*>(weights), surfels, reinterpret_cast<float2*>(out),
+                 reinterpret_cast<float2*>(workspace), render_segments(chirp, apertures, surfels), st};
+  return dispatch_kp(chirp->num_bins, chirp->pad, L);
+}
+
+int dsg_surfel_jvp(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                   const float* centers, const float* normals, const float* weights,
+                   const float* delta_centers, const float* delta_normals,
+                   const float* delta_weights, int32_t surfels, float* out, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || surfels < 0 || (apertures > 0 && (!positions || !out))) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (apertures == 0) return DSG_OK;
+  if (surfels == 0) {
+    cudaMemsetAsync(out, 0, (size_t)apertures * chirp->num_bins * 2 * sizeof(float), st);
+    return launch_status();
+  }
+  if (!centers || !normals || !weights || !delta_centers || !delta_normals || !delta_weights)
+    return DSG_ERR_ARGUMENT;
+  const size_t need = dsg_surfel_render_workspace_bytes(chirp, apertures, surfels);
+  if (need > 0 && (workspace == nullptr || workspace_bytes < need)) return DSG_ERR_WORKSPACE;
+  JvpLaunch L{make_consts(*chirp), positions, apertures, centers, normals,
+              reinterpret_cast<const float2*>(weights), delta_centers, delta_normals,
+              reinterpret_cast<const float2*>(delta_weights), surfels,
+              reinterpret_cast<float2*>(out), reinterpret_cast<float2*>(workspace),
+              render_segments(chirp, apertures, surfels), st};
+  return dispatch_kp(chirp->num_bins, chirp->pad, L);
+}
+
+size_t dsg_surfel_reduce_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels,
+                                         int32_t values_per_surfel) {
+  if (!chirp_ok(chirp) || apertures <= 0 || surfels <= 0 || values_per_surfel <= 0) return 0;
+  return (size_t)surfels * reduce_chunks(apertures, surfels) * values_per_surfel * sizeof(float);
+}
+
+static int reduce_common(int mode, const DsgChirp* chirp, const float* positions, int32_t A,
+                         const float* centers, const float* normals, const float* weights,
+                         int32_t S, const float* residual, float* o0, float* o1, float* o2,
+                         float* o3, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (A < 0 || S < 0) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nv = mode == 0 ? 3 : mode == 1 ? 12 : mode == 2 ? 21 : 8;
+  if (S == 0) return DSG_OK;
+  if (!centers || !normals || !o0 || !o1) return DSG_ERR_ARGUMENT;
+  if (A == 0) {  // empty sums
+    size_t n0 = (size_t)S * (mode == 3 ? 3 : 2), n1 = (size_t)S * (mode == 3 ? 3 : 1);
+    cudaMemsetAsync(o0, 0, n0 * sizeof(float), st);
+    cudaMemsetAsync(o1, 0, n1 * sizeof(float), st);
+    const int W = mode == 1 ? 3 : 6;
+    if (mode == 3) cudaMemsetAsync(o2, 0, (size_t)S * 2 * sizeof(float), st);
+    if (mode == 1 || mode == 2) {
+      cudaMemsetAsync(o2, 0, (size_t)S * W * 2 * sizeof(float), st);
+      cudaMemsetAsync(o3, 0, (size_t)S * W * sizeof(float), st);
+    }
+    return launch_status();
+  }
+  if (!positions || !residual) return DSG_ERR_ARGUMENT;
+  const size_t need = dsg_surfel_reduce_workspace_bytes(chirp, A, S, nv);
+  if (workspace == nullptr || workspace_bytes < need) return DSG_ERR_WORKSPACE;
+  const Consts c = make_consts(*chirp);
+  const float2* w = reinterpret_cast<const float2*>(weights);
+  const float2* res = reinterpret_cast<const float2*>(residual);
+  float* part = reinterpret_cast<float*>(workspace);
+  switch (mode) {
+    case 0: { ReduceLaunch<0> L{c, positions, A, centers, normals, w, S, res, part, o0, o1, o2, o3, st};
+              return dispatch_kp(c.K, c.P, L); }
+    case 1: { ReduceLaunch<1> L{c, positions, A, centers, normals, w, S, res, part, o0, o1, o2, o3, st};
+              return dispatch_kp(c.K, c.P, L); }
+    case 2: { ReduceLaunch<2> L{c, positions, A, centers, normals, w, S, res, part, o0, o1, o2, o3, st};
+              return dispatch_kp(c.K, c.P, L); }
+    default: { ReduceLaunch<3> L{c, positions, A, centers, normals, w, S, res, part, o0, o1, o2, o3, st};
+               return dispatch_kp(c.K, c.P, L); }
+  }
+}
+
+int dsg_surfel_vjp(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                   const float* centers, const float* normals, const float* weights,
+                   int32_t surfels, const float* upstream, float* grad_centers,
+                   float* grad_normals, float* grad_weights, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  if (surfels > 0 && (!weights || !grad_weights)) return DSG_ERR_ARGUMENT;
+  return reduce_common(3, chirp, positions, apertures, centers, normals, weights, surfels, upstream,
+                       grad_centers, grad_normals, grad_weights, nullptr, workspace,
+                       workspace_bytes, stream);
+}
+
+int dsg_surfel_correlate(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                         const float* centers, const float* normals, int32_t candidates,
+                         const float* residual, float* corr, float* norm, void* workspace,
+                         size_t workspace_bytes, void* stream) {
+  return reduce_common(0, chirp, positions, apertures, centers, normals, nullptr, candidates,
+                       residual, corr, norm, nullptr, nullptr, workspace, workspace_bytes, stream);
+}
+
+int dsg_surfel_correlate_gradient(const DsgChirp* chirp, const float* positions,
+                                  int32_t apertures, const float* centers, const float* normals,
+                                  int32_t candidates, const float* residual, int32_t width,
+                                  float* corr, float* norm, float* dcorr, float* dnorm,
+                                  void* workspace, size_t workspace_bytes, void* stream) {
+  if (width != 3 && width != 6) return DSG_ERR_ARGUMENT;
+  if (candidates > 0 && (!dcorr || !dnorm)) return DSG_ERR_ARGUMENT;
+  return reduce_common(width == 3 ? 1 : 2, chirp, positions, apertures, centers, normals, nullptr,
+                       candidates, residual, corr, norm, dcorr, dnorm, workspace,
+                       workspace_bytes, stream);
+}
+
+int dsg_surfel_correlate_orientations(const DsgChirp* chirp, const float* positions,
+                                      int32_t apertures, const float* centers,
+                                      const float* normals, int32_t candidates, const float* bank,
+                                      int32_t bank_size, const float* residual,
+                                      const float* range_table, const float* norm_table,
+                                      int32_t oversample, float* out, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || candidates < 0 || bank_size < 0) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (candidates == 0) return DSG_OK;
+  if (!centers || !normals || !out || (bank_size > 0 && !bank)) return DSG_ERR_ARGUMENT;
+  if (apertures == 0) {
+    cudaMemsetAsync(out, 0, (size_t)candidates * (bank_size + 1) * 3 * sizeof(float), st);
+    return launch_status();
+  }
+  if (!positions) return DSG_ERR_ARGUMENT;
+  const bool use_table = range_table != nullptr;
+  if (use_table && (!norm_table || oversample < 1)) return DSG_ERR_ARGUMENT;
+  if (!use_table && !residual) return DSG_ERR_ARGUMENT;
+  OrientLaunch L{make_consts(*chirp), positions, apertures, centers, normals, candidates, bank,
+                 bank_size, reinterpret_cast<const float2*>(residual),
+                 reinterpret_cast<const float2*>(range_table), norm_table,
+                 use_table ? oversample : 1, out, st};
+  return dispatch_p(chirp->pad, L);
+}
+
+int dsg_surfel_design(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                      const float* centers, const float* normals, const float* areas,
+                      int32_t surfels, int32_t real, float* out, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || surfels < 0) return DSG_ERR_ARGUMENT;
+  if (apertures == 0 || surfels == 0) return DSG_OK;
+  if (!positions || !centers || !normals || !areas || !out) return DSG_ERR_ARGUMENT;
+  if (apertures > 65535) return DSG_ERR_ARGUMENT;
+  DesignLaunch L{make_consts(*chirp), positions, apertures, centers, normals, areas, surfels, real,
+                 out, (cudaStream_t)stream};
+  return dispatch_p(chirp->pad, L);
+}
+
+int dsg_surfel_jacobian(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                        const float* centers, const float* normals, int32_t surfels,
+                        float* columns, float* derivatives, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || surfels < 0) return DSG_ERR_ARGUMENT;
+  if (apertures == 0 || surfels == 0) return DSG_OK;
+  if (!positions || !centers || !normals || !columns || !derivatives) return DSG_ERR_ARGUMENT;
+  if (apertures > 65535) return DSG_ERR_ARGUMENT;
+  JacobianLaunch L{make_consts(*chirp), positions, apertures, centers, normals, surfels,
+                   reinterpret_cast<float2*>(columns), reinterpret_cast<float2*>(derivatives),
+                   (cudaStream_t)stream};
+  return dispatch_p(chirp->pad, L);
+}
+
+}  // extern "C"

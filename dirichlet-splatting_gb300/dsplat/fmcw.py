@@ -1,0 +1,341 @@
+"""FMCW sensor: chirp configuration, scans and the surfel measurement model.
+
+A linear chirp (carrier fc, bandwidth B) sampled by adc_samples ADC samples and
+zero-padded to n_fft gives, per aperture, the positive range bins
+data[A, K] = FFT(ADC, n_fft)[:K] / adc_samples. A surfel at range r appears at bin
+r / spacing (spacing = c / (2 B pad)) as the Dirichlet kernel of the range FFT times
+the chirp phase. FMCWModel is the measurement model of the solver: rendering and
+derivatives on the CUDA kernels, streamed least-squares blocks projected onto the
+row basis of the range response, seeded aperture subsets, the range gate and the
+FFT range table of the spatial search. Behaviour follows the reference's
+dsplat/fmcw.py:62-388.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field, replace
+from math import ceil, floor
+from typing import NamedTuple
+
+import torch
+import torch.nn.functional as F
+
+from . import surfel
+from .kernels import search
+from .kernels.response import range_response
+
+
+@dataclass(frozen=True)
+class FMCWConfig:
+    fc_hz: float = 120e9
+    bandwidth_hz: float = 15e9
+    adc_samples: int = 128
+    sweep_time_s: float = 1e-5
+    adc_start_time_s: float = 0.0
+    pad_factor: int = 2
+    c0_m_s: float = 299792458.0
+
+    @property
+    def lambda_m(self):
+        return self.c0_m_s / self.fc_hz
+
+    @property
+    def slope_hz_s(self):
+        return self.bandwidth_hz / self.sweep_time_s
+
+    @property
+    def sample_rate_hz(self):
+        return self.adc_samples / self.sweep_time_s
+
+    @property
+    def n_fft(self):
+        return self.adc_samples * self.pad_factor
+
+    @property
+    def num_range_bins(self):
+        return self.n_fft // 2
+
+    @property
+    def range_bin_spacing_m(self):
+        return self.c0_m_s / (2 * self.bandwidth_hz * self.pad_factor)
+
+    @property
+    def range_resolution_m(self):
+        return self.c0_m_s / (2 * self.bandwidth_hz)
+
+
+@dataclass(frozen=True)
+class Scan:
+    """Range profiles data [A, K] measured at scan positions [A, 3], metres."""
+
+    data: torch.Tensor
+    scan_positions_m: torch.Tensor
+    fmcw_config: FMCWConfig
+
+
+# --- Row basis of the range response ---------------------------------------------------------
+
+PEAKS_PER_BIN = 16  # peak positions per range bin sampled for the response SVD
+
+
+@dataclass(frozen=True)
+class RowBasis:
+    """Orthonormal projection of observation rows stored as consecutive aperture blocks."""
+
+    adjoint: torch.Tensor  # complex [rank, bins] = U^H
+    interleaved: torch.Tensor  # real [2 rank, 2 bins] acting on (re, im) row pairs
+
+    def reduce(self, values):
+        """Complex rows [blocks * bins, ...] to [blocks * rank, ...]."""
+        tail = values.shape[1:]
+        rows = values.reshape(-1, self.adjoint.shape[1], tail.numel())
+        return (self.adjoint @ rows).reshape(-1, *tail)
+
+    def reduce_major(self, rows):
+        """Real rows ordered bin by bin, (2 k + part) * blocks + block, in one product."""
+        tail = rows.shape[1:]
+        flat = rows.reshape(self.interleaved.shape[1], -1)
+        return (self.interleaved @ flat).reshape(-1, *tail)
+
+
+def response_basis(config, low, high, device):
+    """Row basis of all peak positions in [low, high] bins, or None when it spans every bin.
+
+    Singular values below eps / 128 of the largest are dropped, so the normal
+    equations keep float32 precision. The SVD runs on the host in float64.
+    """
+    count = max(2 * config.adc_samples, int(PEAKS_PER_BIN * (high - low)) + 1)
+    response = range_response(config, low, high, count, device).cpu()
+    vectors, values, _ = torch.linalg.svd(response, full_matrices=False)
+    rank = int((values > torch.finfo(torch.float32).eps / 128 * values[0]).sum())
+    if rank >= config.num_range_bins:
+        return None
+    adjoint = vectors[:, :rank].mH
+    interleaved = torch.zeros((2 * rank, 2 * config.num_range_bins), dtype=torch.float64)
+    interleaved[0::2, 0::2] = adjoint.real
+    interleaved[0::2, 1::2] = -adjoint.imag
+    interleaved[1::2, 0::2] = adjoint.imag
+    interleaved[1::2, 1::2] = adjoint.real
+    return RowBasis(adjoint.to(device, torch.complex64), interleaved.to(device, torch.float32))
+
+
+class RangeTable(NamedTuple):
+    """FFT-interpolated range correlations of a residual; they only rank proposals."""
+
+    correlation: torch.Tensor  # [apertures, n_fft * oversample, 2]
+    norm: torch.Tensor  # [n_fft * oversample]; carries the observed-bin mask
+    oversample: int
+
+
+# --- Measurement model -----------------------------------------------------------------------
+
+
+@dataclass(frozen=True)
+class FMCWModel:
+    """Surfels measured by an FMCW scan.
+
+    params = {centers [S, 3], normals [S, 3], areas [S]}; the coefficients are
+    reflectivities. prepare returns a copy carrying the row basis of the centers'
+    box; block_bases memoizes the narrower bases of aperture blocks.
+    """
+
+    scan: Scan
+    fresnel_n: float = 0.0  # known refractive index of the surfels; <= 1 for none
+    basis: RowBasis | None = None
+    bands: tuple | None = None  # host arrays: per-aperture lowest and highest peak bin
+    block_bases: dict = field(default_factory=dict, repr=False)
+
+    @property
+    def shape(self):
+        return tuple(self.scan.data.shape)
+
+    @property
+    def size(self):
+        return self.scan.data.numel()
+
+    @property
+    def apertures(self):
+        return self.shape[0]
+
+    @property
+    def row_alignment(self):
+        """Streamed blocks hold whole aperture profiles."""
+        return self.shape[1]
+
+    @property
+    def sensor(self):
+        """The chirp configuration and the sensor positions [A, 3]."""
+        return self.scan.fmcw_config, self.scan.scan_positions_m
+
+    def sample_apertures(self, count, seed):
+        """Sorted ids of a seeded set of whole apertures and the model restricted to them.
+
+        The subset keeps sensor, material and the shared row basis, not the
+        per-aperture bands. The same seed selects the same apertures as
+        sample_rows with count * bins rows.
+        """
+        order = torch.randperm(self.shape[0], generator=torch.Generator().manual_seed(seed))
+        ids = order[: max(1, count)].sort().values.to(self.scan.data.device)
+        scan = replace(
+            self.scan,
+            data=self.scan.data[ids].contiguous(),
+            scan_positions_m=self.scan.scan_positions_m[ids].contiguous(),
+        )
+        return ids, replace(self, scan=scan, bands=None, block_bases={})
+
+    def sample_rows(self, count, seed, device):
+        bins = self.shape[1]
+        order = torch.randperm(self.shape[0], generator=torch.Generator().manual_seed(seed))
+        chosen = order[: max(1, count // bins)].to(device)
+        return (chosen[:, None] * bins + torch.arange(bins, device=device)).flatten()
+
+    def prepare(self, specs):
+        """This model with the row basis of every center inside the centers' box.
+
+        The band of range bins runs from the nearest to the farthest box point seen by
+        any aperture, widened by one bin. Without a finite box, or when the band would
+        wrap around the FFT, the basis covers every peak position.
+        """
+        lower, upper = specs["centers"].lower, specs["centers"].upper
+        config, positions = self.sensor
+        low, high, bands = 0.0, float(config.n_fft), None
+        if lower is not None and upper is not None:
+            lo = positions.new_tensor(lower).expand(3)
+            hi = positions.new_tensor(upper).expand(3)
+            nearest_point = torch.minimum(torch.maximum(positions, lo), hi)
+            farthest_point = torch.where((positions - lo).abs() > (positions - hi).abs(), lo, hi)
+            spacing = config.range_bin_spacing_m
+            near_bins = ((positions - nearest_point).norm(dim=1) / spacing - 1).clamp(min=0)
+            far_bins = (positions - farthest_point).norm(dim=1) / spacing + 1
+            near, far = float(near_bins.min()), float(far_bins.max())
+            if far - near < config.n_fft:
+                low, high = near, far
+                bands = (near_bins.cpu().numpy(), far_bins.cpu().numpy())
+        basis = response_basis(config, low, high, positions.device)
+        return replace(self, basis=basis, bands=bands, block_bases={})
+
+    def block_basis(self, rows):
+        """Row basis of a block of whole apertures, never larger than the shared one.
+
+        The block's band is the union of its apertures' bands rounded outward to
+        whole critical range samples, so few distinct bases arise; they are built from
+        host-side bands and never wait on the device.
+        """
+        if self.bands is None or self.basis is None:
+            return self.basis
+        bins, step = self.shape[1], self.scan.fmcw_config.pad_factor
+        first, last = rows.start // bins, -(-rows.stop // bins)
+        key = (
+            floor(self.bands[0][first:last].min() / step) * step,
+            ceil(self.bands[1][first:last].max() / step) * step,
+        )
+        if key not in self.block_bases:
+            config, positions = self.sensor
+            basis = response_basis(config, float(key[0]), float(key[1]), positions.device)
+            narrower = basis is not None and len(basis.adjoint) < len(self.basis.adjoint)
+            self.block_bases[key] = basis if narrower else self.basis
+        return self.block_bases[key]
+
+    def blocks(self, params, target, real, chunk):
+        """Least-squares blocks of whole apertures, projected onto the row basis.
+
+        Real blocks are ordered bin by bin so that one product projects them.
+        """
+        config, positions = self.sensor
+        bins = self.shape[1]
+        flat = target.flatten()
+        for start in range(0, self.size, chunk):
+            rows = slice(start, min(start + chunk, self.size))
+            basis = self.block_basis(rows)
+            if real:
+                block = positions[rows.start // bins : rows.stop // bins]
+                a = surfel.design(config, block, params, self.fresnel_n, real=True)
+                y = torch.view_as_real(flat[rows]).reshape(len(block), 2 * bins).T.reshape(-1)
+                yield (a, y) if basis is None else (basis.reduce_major(a), basis.reduce_major(y))
+            else:
+                a, y = self.design(params, rows), flat[rows]
+                yield (a, y) if basis is None else (basis.reduce(a), basis.reduce(y))
+
+    def _apertures(self, rows):
+        """Apertures of arbitrary row ids, each row's index among them, and its bin."""
+        apertures, inverse = torch.unique(rows // self.shape[1], return_inverse=True)
+        return self.scan.scan_positions_m[apertures], inverse, rows % self.shape[1]
+
+    def design(self, params, rows):
+        """Complex dictionary rows [rows, S]; a slice must cover whole apertures."""
+        config, positions = self.sensor
+        bins = self.shape[1]
+        if isinstance(rows, slice):
+            block = positions[rows.start // bins : -(-rows.stop // bins)]
+            return surfel.design(config, block, params, self.fresnel_n)
+        block, inverse, ids = self._apertures(rows)
+        a = surfel.design(config, block, params, self.fresnel_n)
+        return a.reshape(len(block), bins, -1)[inverse, ids]
+
+    def jacobian(self, params, rows, atoms, keys):
+        """Column derivatives [rows, atoms, D] for the given parameter keys and row ids."""
+        block, inverse, ids = self._apertures(rows)
+        selected = {key: value[atoms] for key, value in params.items()}
+        derivatives = surfel.jacobian(self.scan.fmcw_config, block, selected, self.fresnel_n)
+        return {key: derivatives[key][inverse, ids] for key in keys}
+
+    def render(self, params, coefficients):
+        return surfel.render(*self.sensor, params, coefficients, self.fresnel_n)
+
+    def jvp(self, params, coefficients, tangent, delta_coefficients):
+        return surfel.jvp(
+            *self.sensor, params, coefficients, tangent, delta_coefficients, self.fresnel_n
+        )
+
+    def vjp(self, params, coefficients, upstream):
+        return surfel.vjp(*self.sensor, params, coefficients, upstream, self.fresnel_n)
+
+    def correlate(self, params, residual):
+        return surfel.correlate(*self.sensor, params, residual.reshape(self.shape), self.fresnel_n)
+
+    def correlate_gradient(self, params, residual, include_normals=False):
+        return surfel.correlate_gradient(
+            *self.sensor, params, residual.reshape(self.shape), self.fresnel_n, include_normals
+        )
+
+    def correlate_orientations(self, params, residual, bank, table=None):
+        return surfel.correlate_orientations(
+            *self.sensor, params, bank, residual.reshape(self.shape), self.fresnel_n, table
+        )
+
+    @torch.no_grad()
+    def range_gate(self, points, measurement, relative_power, margin_cells, min_fraction):
+        """Points whose spherical range falls in a measured range interval at enough apertures.
+
+        32 evenly spaced apertures threshold their profile relative to its own peak,
+        dilate every interval above it by margin_cells range resolutions, and a point
+        must hit an interval at min_fraction of the apertures with signal.
+        """
+        config, positions = self.sensor
+        count = min(32, len(measurement))
+        ids = torch.linspace(0, len(measurement) - 1, count, device=points.device).long()
+        power = measurement[ids].abs().square()
+        peak = power.max(-1).values
+        informative = peak > peak.max() * 1e-6
+        power, peak = power[informative], peak[informative]
+        spacing = config.range_bin_spacing_m
+        radius = math.ceil(margin_cells * config.range_resolution_m / spacing)
+        above = (power >= relative_power * peak[:, None]).float()[:, None]
+        intervals = F.max_pool1d(above, 2 * radius + 1, stride=1, padding=radius)[:, 0].int()
+        return search.range_gate(points, positions[ids][informative], intervals, spacing, min_fraction)
+
+    @torch.no_grad()
+    def range_table(self, residual, oversample=8):
+        """Oversampled FFT range correlations of the residual for proposal scores."""
+        config = self.scan.fmcw_config
+        n, samples = config.n_fft, config.adc_samples
+        size = n * oversample
+        residual = residual.reshape(self.shape)
+        coefficients = torch.fft.ifft(residual, n=n, dim=-1)[..., :samples] * (n / samples)
+        correlation = torch.fft.fft(coefficients, n=size, dim=-1)
+        kernel = torch.fft.fft(residual.real.new_ones(samples), n=size) / samples
+        mask = residual.real.new_zeros(size)
+        mask[: config.num_range_bins * oversample : oversample] = 1
+        norm = torch.fft.ifft(torch.fft.fft(mask) * torch.fft.fft(kernel.abs().square())).real
+        return RangeTable(torch.view_as_real(correlation).contiguous(), norm.contiguous(), oversample)

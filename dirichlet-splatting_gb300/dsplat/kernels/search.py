@@ -1,0 +1,66 @@
+"""Range gating, separated peaks and quasi-Newton steps of the spatial search (replaces
+the reference's dsplat/kernels/search.py bindings of search.slang)."""
+
+from __future__ import annotations
+
+import math
+
+import torch
+
+from . import _lib
+from ._lib import call, f32, ptr
+
+
+def range_gate(points, positions, intervals, spacing, min_fraction):
+    """Points whose spherical range bin lies in a marked interval at min_fraction of apertures."""
+    points, positions = f32(points), f32(positions)
+    intervals = intervals.to(torch.int32).contiguous()
+    output = torch.empty(len(points), device=points.device, dtype=torch.int32)
+    required = math.ceil(min_fraction * len(positions) - 1e-7)
+    call(
+        "dsg_range_gate", ptr(points), len(points), ptr(positions) if len(positions) else None,
+        len(positions), ptr(intervals) if intervals.numel() else None, intervals.shape[1],
+        float(spacing), required, ptr(output), _lib.stream(points.device),
+    )  # fmt: skip
+    return output.bool()
+
+
+def peaks(scores, centers, count, separation):
+    """Greedy best-first indices at least separation apart."""
+    work = scores.float().clone().contiguous()
+    centers = f32(centers)
+    wanted = min(count, len(scores))
+    output = torch.empty((wanted,), device=centers.device, dtype=torch.int32)
+    call(
+        "dsg_peaks", ptr(work) if len(work) else None, ptr(centers) if len(centers) else None,
+        len(work), centers.shape[1], wanted, float(separation), ptr(output),
+        _lib.stream(centers.device),
+    )  # fmt: skip
+    return output[output >= 0].long()
+
+
+def direction(inverse, gradient, normals, mask, radius):
+    """Quasi-Newton descent per candidate: tangent to unit normals, inside the trust radius."""
+    count, width = gradient.shape
+    gradient = f32(gradient)
+    output = torch.empty_like(gradient)
+    call(
+        "dsg_direction", ptr(f32(inverse)), ptr(gradient), ptr(f32(normals)), ptr(f32(mask)),
+        count, width, float(radius), ptr(output), _lib.stream(gradient.device),
+    )  # fmt: skip
+    return output
+
+
+def trial(centers, normals, direction, controls, fraction):
+    """Step fraction along direction, clamped to the box and renormalized; frozen axes kept.
+
+    controls rows: per-coordinate scale, trainable mask, lower and upper bounds.
+    """
+    count, width = direction.shape
+    centers, normals = f32(centers), f32(normals)
+    out_centers, out_normals = torch.empty_like(centers), torch.empty_like(normals)
+    call(
+        "dsg_trial", ptr(centers), ptr(normals), ptr(f32(direction)), ptr(f32(controls)), count,
+        width, float(fraction), ptr(out_centers), ptr(out_normals), _lib.stream(centers.device),
+    )  # fmt: skip
+    return out_centers, out_normals

@@ -1,0 +1,200 @@
+"""FMCW surfel kernels behind the reference's binding signatures.
+
+Replaces dsplat/kernels/surfel.py of the reference (slangtorch launches of
+surfel.slang and correlate.slang) with calls into libdsplat_gb300.so. config is an
+FMCWConfig, positions the sensor positions [A, 3]; weights are per-surfel complex
+amplitudes (reflectivity times sqrt(area)); the area chain lives in dsplat.surfel.
+Complex gradients follow PyTorch: dL/dx = Re(conj(upstream) dy/dx).
+"""
+
+from __future__ import annotations
+
+import torch
+from torch.autograd.function import once_differentiable
+
+from . import _lib
+from ._lib import call, f32, ptr, real_view
+
+
+def _outputs(centers, *shape, dtype=torch.float32):
+    return torch.empty(shape, dtype=dtype, device=centers.device)
+
+
+def _profiles(config, positions, centers, normals, weights, fresnel_n):
+    """Range profiles [A, K, 2] of weights [S, 2] (interleaved complex)."""
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    weights = weights.contiguous()
+    chirp = _lib.chirp(config, fresnel_n)
+    count, apertures = len(centers), len(positions)
+    out = _outputs(centers, apertures, config.num_range_bins, 2)
+    nbytes = _lib.query("dsg_surfel_render_workspace_bytes", chirp, apertures, count)
+    work, nbytes = _lib.workspace(nbytes, centers.device)
+    call(
+        "dsg_surfel_render", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
+        ptr(weights), count, ptr(out), ptr(work), nbytes, _lib.stream(centers.device),
+    )  # fmt: skip
+    return out
+
+
+def vjp(config, positions, centers, normals, weights, upstream, fresnel_n):
+    """Gradients of Re(conj(upstream) . profiles) for centers, normals and complex weights."""
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    w, u = real_view(weights), real_view(upstream)
+    chirp = _lib.chirp(config, fresnel_n)
+    count, apertures = len(centers), len(positions)
+    gc, gn, gw = (_outputs(centers, count, 3), _outputs(centers, count, 3),
+                  _outputs(centers, count, 2))  # fmt: skip
+    nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 8)
+    work, nbytes = _lib.workspace(nbytes, centers.device)
+    call(
+        "dsg_surfel_vjp", chirp, ptr(positions), apertures, ptr(centers), ptr(normals), ptr(w),
+        count, ptr(u), ptr(gc), ptr(gn), ptr(gw), ptr(work), nbytes,
+        _lib.stream(centers.device),
+    )  # fmt: skip
+    return gc, gn, torch.view_as_complex(gw)
+
+
+def jvp(config, positions, centers, normals, weights, delta_centers, delta_normals,
+        delta_weights, fresnel_n):  # fmt: skip
+    """Directional derivative of the profiles [A, K]."""
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    dc, dn = f32(delta_centers), f32(delta_normals)
+    w, dw = real_view(weights), real_view(delta_weights)
+    chirp = _lib.chirp(config, fresnel_n)
+    count, apertures = len(centers), len(positions)
+    out = _outputs(centers, apertures, config.num_range_bins, 2)
+    nbytes = _lib.query("dsg_surfel_render_workspace_bytes", chirp, apertures, count)
+    work, nbytes = _lib.workspace(nbytes, centers.device)
+    call(
+        "dsg_surfel_jvp", chirp, ptr(positions), apertures, ptr(centers), ptr(normals), ptr(w),
+        ptr(dc), ptr(dn), ptr(dw), count, ptr(out), ptr(work), nbytes,
+        _lib.stream(centers.device),
+    )  # fmt: skip
+    return torch.view_as_complex(out)
+
+
+class _Render(torch.autograd.Function):
+    """Profiles forward; the backward is the hand-written adjoint kernel (dsg_surfel_vjp)."""
+
+    @staticmethod
+    def forward(ctx, centers, normals, weights, positions, config, fresnel_n):
+        ctx.save_for_backward(centers, normals, weights, positions)
+        ctx.config, ctx.fresnel_n = config, fresnel_n
+        return _profiles(config, positions, centers, normals, weights, fresnel_n)
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        centers, normals, weights, positions = ctx.saved_tensors
+        upstream = torch.view_as_complex(grad.contiguous())
+        gc, gn, gw = vjp(
+            ctx.config, positions, centers, normals, torch.view_as_complex(weights), upstream,
+            ctx.fresnel_n,
+        )  # fmt: skip
+        return gc, gn, torch.view_as_real(gw), None, None, None
+
+
+def render(config, positions, centers, normals, weights, fresnel_n):
+    """Range profiles [A, K]; differentiable in centers, normals and weights."""
+    output = _Render.apply(
+        centers.contiguous(), normals.contiguous(), real_view(weights), positions, config, fresnel_n
+    )
+    return torch.view_as_complex(output)
+
+
+def design(config, positions, centers, normals, areas, fresnel_n, real):
+    """Dictionary rows of whole apertures including sqrt(area).
+
+    Complex rows are [A * K, S]; real rows are [2 * A * K, S] ordered bin by bin,
+    row (2 k + part) * A + a, so one product projects every aperture onto a row basis.
+    """
+    positions, centers, normals, areas = f32(positions), f32(centers), f32(normals), f32(areas)
+    chirp = _lib.chirp(config, fresnel_n)
+    count, rows = len(centers), len(positions) * config.num_range_bins
+    out = _outputs(centers, 2 * rows, count) if real else _outputs(centers, rows, count, 2)
+    call(
+        "dsg_surfel_design", chirp, ptr(positions), len(positions), ptr(centers), ptr(normals),
+        ptr(areas), count, int(bool(real)), ptr(out), _lib.stream(centers.device),
+    )  # fmt: skip
+    return out if real else torch.view_as_complex(out)
+
+
+def jacobian(config, positions, centers, normals, fresnel_n):
+    """Columns [A, K, S] and their center and normal derivatives [A, K, S, 3], without area."""
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    chirp = _lib.chirp(config, fresnel_n)
+    shape = (len(positions), config.num_range_bins, len(centers))
+    cols = _outputs(centers, *shape, 2)
+    jac = _outputs(centers, *shape, 6, 2)
+    call(
+        "dsg_surfel_jacobian", chirp, ptr(positions), len(positions), ptr(centers), ptr(normals),
+        len(centers), ptr(cols), ptr(jac), _lib.stream(centers.device),
+    )  # fmt: skip
+    jac = torch.view_as_complex(jac)
+    return torch.view_as_complex(cols), jac[..., :3], jac[..., 3:]
+
+
+def correlate(config, positions, centers, normals, residual, fresnel_n):
+    """conj(column) . residual and |column|^2 per candidate, without area."""
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    r = real_view(residual)
+    chirp = _lib.chirp(config, fresnel_n)
+    count, apertures = len(centers), len(positions)
+    corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
+    nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3)
+    work, nbytes = _lib.workspace(nbytes, centers.device)
+    call(
+        "dsg_surfel_correlate", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
+        count, ptr(r), ptr(corr), ptr(norm), ptr(work), nbytes, _lib.stream(centers.device),
+    )  # fmt: skip
+    return torch.view_as_complex(corr), norm
+
+
+def correlate_orientations(config, positions, centers, normals, bank, residual, fresnel_n,
+                           table=None):  # fmt: skip
+    """Correlations and norms [S, 1 + bank] for the current normal and every bank normal.
+
+    table, an fmcw.RangeTable, replaces the per-bin sum by FFT-interpolated range
+    correlations; it only ranks proposals. Without area.
+    """
+    positions, centers, normals, bank = f32(positions), f32(centers), f32(normals), f32(bank)
+    chirp = _lib.chirp(config, fresnel_n)
+    count = len(centers)
+    out = _outputs(centers, count, len(bank) + 1, 3)
+    if table is None:
+        r, rt, nt, oversample = real_view(residual), None, None, 1
+    else:
+        r, rt, nt = None, f32(table.correlation), f32(table.norm)
+        oversample = table.oversample
+    call(
+        "dsg_surfel_correlate_orientations", chirp, ptr(positions), len(positions), ptr(centers),
+        ptr(normals), count, ptr(bank) if len(bank) else None, len(bank), ptr(r), ptr(rt),
+        ptr(nt), oversample, ptr(out), _lib.stream(centers.device),
+    )  # fmt: skip
+    return torch.complex(out[..., 0], out[..., 1]), out[..., 2]
+
+
+def correlate_gradient(config, positions, centers, normals, residual, fresnel_n, include_normals):
+    """Correlation, norm and their center (and normal) derivatives [S, 3 or 6], without area."""
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    r = real_view(residual)
+    width = 6 if include_normals else 3
+    chirp = _lib.chirp(config, fresnel_n)
+    count, apertures = len(centers), len(positions)
+    corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
+    dcorr, dnorm = _outputs(centers, count, width, 2), _outputs(centers, count, width)
+    nbytes = _lib.query(
+        "dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3 + 3 * width
+    )
+    work, nbytes = _lib.workspace(nbytes, centers.device)
+    call(
+        "dsg_surfel_correlate_gradient", chirp, ptr(positions), apertures, ptr(centers),
+        ptr(normals), count, ptr(r), width, ptr(corr), ptr(norm), ptr(dcorr), ptr(dnorm),
+        ptr(work), nbytes, _lib.stream(centers.device),
+    )  # fmt: skip
+    return (
+        torch.view_as_complex(corr),
+        norm,
+        torch.view_as_complex(dcorr),
+        dnorm,
+    )

@@ -1,0 +1,209 @@
+/*
+ * dsplat_gb300.h -- C ABI of the GB300 (sm_103a) kernels of the Dirichlet-splatting
+ * render-and-fit path.
+ *
+ * Every entry point takes plain device pointers and sizes, launches on the given
+ * CUDA stream (a cudaStream_t passed as void*, 0 = legacy default stream) and returns
+ * 0 on success or a DSG_ERR_* code; nothing traps, nothing synchronises the stream,
+ * and nothing allocates device memory. Buffers that hold intermediate partial sums
+ * are passed in by the caller as `workspace`; the *_workspace_bytes queries give
+ * their size. Complex values are interleaved float pairs (re, im), the layout of a
+ * torch complex64 tensor viewed as real. All tensors are C-contiguous.
+ *
+ * Each declaration names the reference binding it replaces (path:line within the
+ * Asixa/Dirichlet-Splatting project). The reference bindings are Python functions
+ * that launch Slang kernels through slangtorch; the Python layer of this project
+ * (dirichlet-splatting_gb300/dsplat/kernels/) keeps their signatures and calls these.
+ */
+#ifndef DSPLAT_GB300_H
+#define DSPLAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  DSG_OK = 0,
+  DSG_ERR_ARGUMENT = 1,      /* a size, pointer or configuration value is invalid   */
+  DSG_ERR_UNSUPPORTED = 2,   /* a configuration this build does not handle           */
+  DSG_ERR_WORKSPACE = 3,     /* workspace missing or smaller than the query result   */
+  DSG_ERR_LAUNCH = 4,        /* cudaGetLastError reported a launch failure            */
+  DSG_ERR_LIBRARY = 5        /* a cuBLAS call failed                                  */
+};
+
+/* FMCW chirp and sensor constants (reference: dsplat/fmcw.py:62-98, FMCWConfig).
+ * num_bins = n_fft / 2, n_fft = samples * pad. pad must divide 8. */
+typedef struct DsgChirp {
+  int32_t num_bins;
+  int32_t n_fft;
+  int32_t samples;
+  int32_t pad;
+  double k0_per_meter;  /* 1 / range_bin_spacing_m                          */
+  double fc;            /* carrier, Hz                                      */
+  double slope;         /* chirp slope, Hz / s                              */
+  double t_start;       /* ADC start time, s                                */
+  double lambda_m;      /* c0 / fc                                          */
+  double c0;            /* wave speed, m / s                                */
+  double fresnel_n;     /* refractive index; <= 1 disables the Fresnel term */
+} DsgChirp;
+
+/* Spectral grid (reference: dsplat/spectral.py:16-34, SpectralGrid; taps as built in
+ * dsplat/kernels/spectral.py:22-27). window: 0 rect, 1 hann, 2 hamming, 3 kaiser. */
+typedef struct DsgGrid {
+  int32_t dim;          /* 1..3 axes                                        */
+  int32_t nfft[3];
+  int32_t samples[3];
+  int32_t window;
+  int32_t max_taps;     /* row stride of the taps array (kaiser)            */
+  float radius;         /* 0: untruncated                                   */
+} DsgGrid;
+
+const char* dsg_version(void);
+const char* dsg_error_string(int code);
+
+/* ---- FMCW surfels: range profiles and derivatives ------------------------------- */
+
+/* Workspace of dsg_surfel_render / dsg_surfel_jvp (segment partials), in bytes. */
+size_t dsg_surfel_render_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels);
+
+/* out[A,K] = sum_s weights_s * column_s (reference: dsplat/kernels/surfel.py:58-108
+ * _profiles, and :186-196 render). positions [A,3], centers/normals [S,3],
+ * weights [S] complex, out [A,K] complex. */
+int dsg_surfel_render(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                      const float* centers, const float* normals, const float* weights,
+                      int32_t surfels, float* out, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
+/* Directional derivative of the profiles (reference: dsplat/kernels/surfel.py:140-164 jvp).
+ * delta_centers/delta_normals [S,3], delta_weights [S] complex, out [A,K] complex. */
+int dsg_surfel_jvp(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                   const float* centers, const float* normals, const float* weights,
+                   const float* delta_centers, const float* delta_normals,
+                   const float* delta_weights, int32_t surfels, float* out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* Workspace of the aperture-reduced kernels (vjp, correlate, correlate_gradient). */
+size_t dsg_surfel_reduce_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels,
+                                         int32_t values_per_surfel);
+
+/* Gradients of Re(conj(upstream) . profiles) (reference: dsplat/kernels/surfel.py:123-137
+ * vjp). upstream [A,K] complex; grad_centers/grad_normals [S,3]; grad_weights [S] complex.
+ * Summed over apertures in a fixed order, in double precision across aperture chunks. */
+int dsg_surfel_vjp(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                   const float* centers, const float* normals, const float* weights,
+                   int32_t surfels, const float* upstream, float* grad_centers,
+                   float* grad_normals, float* grad_weights, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* conj(column) . residual and |column|^2 per candidate, without area (reference:
+ * dsplat/kernels/surfel.py:242-260 correlate). corr [C] complex, norm [C]. */
+int dsg_surfel_correlate(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                         const float* centers, const float* normals, int32_t candidates,
+                         const float* residual, float* corr, float* norm, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/* correlate plus derivatives by centers (and normals) (reference:
+ * dsplat/kernels/surfel.py:293-315 correlate_gradient). width = 3 or 6.
+ * corr [C] complex, norm [C], dcorr [C,width] complex, dnorm [C,width]. */
+int dsg_surfel_correlate_gradient(const DsgChirp* chirp, const float* positions,
+                                  int32_t apertures, const float* centers, const float* normals,
+                                  int32_t candidates, const float* residual, int32_t width,
+                                  float* corr, float* norm, float* dcorr, float* dnorm,
+                                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Scores of each candidate's own normal and every bank normal (reference:
+ * dsplat/kernels/surfel.py:263-290 correlate_orientations). bank [Nb,3];
+ * out [C, 1+Nb, 3] = (Re corr, Im corr, norm). range_table [A, n_fft*oversample, 2] and
+ * norm_table [n_fft*oversample] select the FFT-interpolated mode when non-null. */
+int dsg_surfel_correlate_orientations(const DsgChirp* chirp, const float* positions,
+                                      int32_t apertures, const float* centers,
+                                      const float* normals, int32_t candidates, const float* bank,
+                                      int32_t bank_size, const float* residual,
+                                      const float* range_table, const float* norm_table,
+                                      int32_t oversample, float* out, void* stream);
+
+/* Dictionary rows including sqrt(area) (reference: dsplat/kernels/surfel.py:199-220 design).
+ * real != 0: out [2*A*K, S] with row (2k+part)*A + a; else out [A*K, S] complex. */
+int dsg_surfel_design(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                      const float* centers, const float* normals, const float* areas,
+                      int32_t surfels, int32_t real, float* out, void* stream);
+
+/* Explicit columns [A,K,S] complex and their center/normal derivatives [A,K,S,6] complex,
+ * without area (reference: dsplat/kernels/surfel.py:223-239 jacobian). */
+int dsg_surfel_jacobian(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                        const float* centers, const float* normals, int32_t surfels,
+                        float* columns, float* derivatives, void* stream);
+
+/* ---- Spectral atoms --------------------------------------------------------------- */
+
+/* out[M] = sum_s a_ms coeff_s (reference: dsplat/kernels/spectral.py:168-189). */
+int dsg_spectral_render(const DsgGrid* grid, const float* taps, const float* centers,
+                        int32_t count, const float* coeff, const float* bins, int32_t size,
+                        float* out, void* stream);
+/* Directional derivative (reference: dsplat/kernels/spectral.py:192-201 jvp). */
+int dsg_spectral_jvp(const DsgGrid* grid, const float* taps, const float* centers,
+                     int32_t count, const float* coeff, const float* delta_centers,
+                     const float* delta_coeff, const float* bins, int32_t size, float* out,
+                     void* stream);
+/* Workspace of dsg_spectral_vjp, in bytes. */
+size_t dsg_spectral_vjp_workspace_bytes(const DsgGrid* grid, int32_t count, int32_t size);
+/* Gradients for centers [S,D] and complex coefficients [S] (reference:
+ * dsplat/kernels/spectral.py:157-165,204-209). Deterministic two-stage sum. */
+int dsg_spectral_vjp(const DsgGrid* grid, const float* taps, const float* centers,
+                     int32_t count, const float* coeff, const float* upstream,
+                     const float* bins, int32_t size, float* grad_centers, float* grad_coeff,
+                     void* workspace, size_t workspace_bytes, void* stream);
+/* Dictionary [M,S] complex and optionally d/dcenters [M,S,D] complex
+ * (reference: dsplat/kernels/spectral.py:146-154 design). jacobian may be null. */
+int dsg_spectral_design(const DsgGrid* grid, const float* taps, const float* centers,
+                        int32_t count, const float* bins, int32_t size, float* out,
+                        float* jacobian, void* stream);
+
+/* ---- Search ----------------------------------------------------------------------- */
+
+/* Range gate (reference: dsplat/kernels/search.py:10-24). intervals [Ap, bins] int32,
+ * output [count] int32 0/1. */
+int dsg_range_gate(const float* points, int32_t count, const float* positions,
+                   int32_t apertures, const int32_t* intervals, int32_t bins, float spacing,
+                   int32_t required, int32_t* output, void* stream);
+/* Greedy separated peaks (reference: dsplat/kernels/search.py:27-39). scores is
+ * overwritten (suppressed entries become -inf); output [peaks] int32, -1 past the end. */
+int dsg_peaks(float* scores, const float* centers, int32_t count, int32_t dimension,
+              int32_t peaks, float separation, int32_t* output, void* stream);
+/* Quasi-Newton direction per candidate (reference: dsplat/kernels/search.py:42-56). */
+int dsg_direction(const float* inverse, const float* gradient, const float* normals,
+                  const float* mask, int32_t count, int32_t width, float radius, float* output,
+                  void* stream);
+/* Trial step (reference: dsplat/kernels/search.py:59-77). controls [4,6]. */
+int dsg_trial(const float* centers, const float* normals, const float* direction,
+              const float* controls, int32_t count, int32_t width, float fraction,
+              float* out_centers, float* out_normals, void* stream);
+
+/* ---- Reductions and the row-basis response ----------------------------------------- */
+
+/* Workspace of dsg_energy, in bytes. */
+size_t dsg_energy_workspace_bytes(int64_t count);
+/* out[0] = sum |value - reference|^2 in double precision, fixed order
+ * (reference: dsplat/kernels/reduce.py:8-18 energy). out is one double. */
+int dsg_energy(const float* value, const float* reference, int64_t count, double* out,
+               void* workspace, size_t workspace_bytes, void* stream);
+
+/* Float64 Dirichlet responses [bins, count] complex of count peak positions spread
+ * evenly over [low, high] (reference: dsplat/kernels/response.py:8-20). */
+int dsg_range_response(double low, double high, int32_t count, int32_t bins, int32_t samples,
+                       int32_t nfft, double* out, void* stream);
+
+/* ---- Gram products of the streamed normal equations --------------------------------- */
+
+/* Plain FP32: add rows^T rows to the upper triangle of the row-major [n, n] matrix out
+ * (cuBLAS SSYRK; reference: dsplat/kernels/cublas.py:31-44 syrk). rows [m, n] row-major. */
+int dsg_syrk_f32(const float* rows, int64_t m, int32_t n, float* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DSPLAT_GB300_H */
