@@ -1,0 +1,370 @@
+"""Benchmark: DSFW steps/s of the 128^2-array, 2000-surfel sphere-cap fit (batch 256).
+
+Our arm (default): the drop-in dsplat package on libdsplat_gb300.so, mixed precision
+(split-BF16x3 tcgen05 Gram; --mode plain uses the FP32 SSYRK drop-in). Workload:
+the 128 x 128 array at 2.5 mm pitch, 2000 surfels on the front hemisphere of a 30 mm
+sphere at 0.35 m, scan synthesized in float64 from the ADC signal chain, fit from
+random surfels in the box plus 5 mm with SpatialSearchConfig() and
+DSFWConfig(batch=256). W untimed warm-up steps after initialize, then K timed steps
+with the inputs resident in HBM, then K steps end to end (pinned host copies of the
+step's inputs in and of its result out every step).
+
+Reference arm (--impl reference): the float64 CPU oracle (oracle/solver.py) on the
+host cores. A DSFW step refits the full data at least twice; the arm times that
+refit on a 1/64 aperture sample (every 8th aperture in each axis), scales it to the
+full array, adds a full-size float64 Cholesky solve, and reports 1 / (2 refits) as
+steps/s, an upper bound on the oracle's step rate.
+
+Prints one JSON line (rank 0).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _path in (ROOT, ROOT / "dirichlet-splatting_gb300"):
+    if str(_path) not in sys.path:
+        sys.path.insert(0, str(_path))
+
+import torch  # noqa: E402
+
+METRIC = "DSFW steps/s (128^2 array, 2k surfels, batch 256)"
+UNIT = "steps/s"
+WORKLOAD = "dsfw_sphere_cap_128x128_s2000_b256"
+
+
+def _peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return data, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def _distributed():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not torch.distributed.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        torch.distributed.init_process_group(backend)
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def _max_over_ranks(value, world, device):
+    if world == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")  # fmt: skip
+
+    def __init__(self, index):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)  # fmt: skip
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        lines = [ln.strip() for ln in Path(self.file.name).read_text().splitlines() if ln.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9], strict=True):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}  # fmt: skip
+
+
+def build_problem(device, seed=0):
+    """Scan, initial surfels and constraints of the sphere-cap fit (all on device)."""
+    from dsplat import FMCWConfig, FMCWModel, ParameterConfig
+    from dsplat.groundtruth import synthesize
+    from dsplat.workloads import box_of, random_start, sphere_cap
+
+    config = FMCWConfig()
+    positions, truth, reflectivity = sphere_cap(device=device, seed=seed)
+    amplitudes = reflectivity * truth["areas"].sqrt()
+    scan = synthesize(positions, truth["centers"], truth["normals"], amplitudes, config)
+    low, high = box_of(truth["centers"], 0.005)
+    start = random_start(len(truth["centers"]), low, high, float(truth["areas"][0]), seed=seed + 1,
+                         device=device)  # fmt: skip
+    parameters = dict(
+        centers=ParameterConfig(scale=5e-4, lower=low, upper=high),
+        normals=ParameterConfig(scale=0.1, normalize=True),
+        areas=ParameterConfig(trainable=False),
+    )
+    return FMCWModel(scan=scan), scan.data, start, parameters, truth
+
+
+def median_distance(params, truth, radius=0.03, depth=0.35):
+    c = params["centers"].double()
+    center = torch.tensor([0.0, 0.0, depth], dtype=torch.float64, device=c.device)
+    return float(((c - center).norm(dim=1) - radius).abs().median())
+
+
+def run_ours(args, world, rank, local):
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from dsplat import DSFWConfig, SpatialSearchConfig, initialize, step
+    from dsplat.kernels import _lib
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    lib = _lib.library()
+    model, target, start, parameters, truth = build_problem(device)
+    config = DSFWConfig(iterations=100, batch=256, gram="bf16x3" if args.mode == "mixed" else "fp32")
+    search = SpatialSearchConfig()
+    state = initialize(model, target, start, config, parameters=parameters)
+    for _ in range(args.warmup):
+        state = step(state, config, search)
+    torch.cuda.synchronize(device)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)  # 256 MiB > L2
+
+    # Device-resident steps, timed with CUDA events on the launching stream.
+    _lib.TIMERS = {}
+    launches0 = lib.dsg_launch_count()
+    times = []
+    with ClockSampler(local) as clocks:
+        _barrier(world)
+        torch.cuda.synchronize(device)
+        for _ in range(args.steps):
+            flush.zero_()
+            begin = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
+            begin.record()
+            state = step(state, config, search)
+            end.record()
+            times.append((begin, end))
+        torch.cuda.synchronize(device)
+        _barrier(world)
+    launches = lib.dsg_launch_count() - launches0
+    timers, _lib.TIMERS = _lib.TIMERS, None
+    step_ms = [b.elapsed_time(e) for b, e in times]
+    total_s = _max_over_ranks(sum(step_ms) / 1e3, world, device)
+    value = world * args.steps / total_s
+
+    # End to end: every step copies its inputs in from pinned host memory and its result out.
+    host_target = target.cpu().pin_memory()
+    e2e_times, h2d, d2h = [], 0, 0
+    _barrier(world)
+    for _ in range(args.steps):
+        host_params = {k: v.cpu().pin_memory() for k, v in state.params.items()}
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        dev_target = host_target.to(device, non_blocking=True)
+        dev_params = {k: v.to(device, non_blocking=True) for k, v in host_params.items()}
+        h2d = host_target.numel() * 8 + sum(v.numel() * 4 for v in host_params.values())
+        from dataclasses import replace
+
+        state = replace(state, target=dev_target, params=dev_params)
+        state = step(state, config, search)
+        out_params = {k: v.to("cpu") for k, v in state.params.items()}
+        out_coef = state.coefficients.to("cpu")
+        d2h = sum(v.numel() * 4 for v in out_params.values()) + out_coef.numel() * 4 + 8
+        torch.cuda.synchronize(device)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_total = _max_over_ranks(sum(e2e_times), world, device)
+    e2e_value = world * args.steps / e2e_total
+
+    # Roofline of the dominant library kernel over the timed steps.
+    totals = {name: sum(b.elapsed_time(e) for b, e in pairs) for name, pairs in timers.items()}
+    roofline = _roofline(totals, timers, args)
+    history = state.history[-1]
+    result = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_s * 1e3 / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+bf16x3" if args.mode == "mixed" else "f32",
+        "data": "synthetic (float64 ADC synthesis of a seeded sphere-cap scene)",
+        "config": {"workload": WORKLOAD, "apertures": 16384, "range_bins": 128, "surfels": 2000,
+                   "batch": 256, "search": "SpatialSearchConfig()", "mode": args.mode,
+                   "l2": "256 MiB buffer written between timed steps", "parallelism": "replicas"},
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "roofline": roofline,
+        "kernel_ms": {k: round(v, 3) for k, v in sorted(totals.items(), key=lambda kv: -kv[1])},
+        "fit": {"iteration": history["iteration"], "nmse": history["nmse"],
+                "median_center_to_surface_m": median_distance(state.params, truth)},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args.cpu_threads)
+    return result
+
+
+def _roofline(totals, timers, args):
+    peaks, source = _peaks()
+    if not totals:
+        return None
+    name = max(totals, key=totals.get)
+    launches = len(timers[name])
+    avg_ms = totals[name] / launches
+    if name == "dsg_gram_bf16x3":
+        # Logical FP32 work of the symmetric product, R S (S + 1) per launch, against the
+        # sustained bf16 tensor peak / 3 (three bf16 products per logical multiply-add).
+        flops = GRAM_WORK.get("flops_per_launch")
+        achieved = flops / (avg_ms * 1e-3) / 1e12 if flops else None
+        peak = peaks["bf16_tflops_sustained"] / 3
+        return {"kernel": name, "bound": "tensor", "achieved": achieved and round(achieved, 2),
+                "peak": round(peak, 2), "unit": "TFLOP/s",
+                "frac": achieved and round(achieved / peak, 4), "traffic": None,
+                "peak_source": f"{source} bf16_tflops_sustained / 3", "launches": launches,
+                "avg_ms": round(avg_ms, 4)}  # fmt: skip
+    return {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": None, "traffic": None, "launches": launches, "avg_ms": round(avg_ms, 4)}  # fmt: skip
+
+
+GRAM_WORK: dict = {}
+
+
+def _install_gram_counter():
+    """Record the logical flops of each Gram launch (R S (S + 1)) for the roofline."""
+    from dsplat.kernels import gram as gram_module
+
+    original = gram_module.GramRows.accumulate
+
+    def accumulate(self, total):
+        GRAM_WORK["flops_per_launch"] = float(self.rows) * self.columns * (self.columns + 1)
+        return original(self, total)
+
+    gram_module.GramRows.accumulate = accumulate
+
+
+def cpu_baseline(threads=None, sample_stride=8):
+    """Float64 oracle refit on a 1/stride^2 aperture sample, scaled to a DSFW step."""
+    from dsplat import FMCWConfig
+
+    from oracle import solver as osolver
+
+    threads = threads or os.cpu_count()
+    torch.set_num_threads(threads)
+    device = torch.device("cpu")
+    # The same scene as the GPU arm, built on the CPU without the CUDA library.
+    from dsplat.workloads import box_of, random_start, sphere_cap
+
+    from oracle import fmcw as ofmcw
+
+    config = FMCWConfig()
+    positions, truth, reflectivity = sphere_cap(device="cpu")
+    grid = positions.reshape(128, 128, 3)[::sample_stride, ::sample_stride].reshape(-1, 3)
+    amplitudes = reflectivity * truth["areas"].sqrt()
+    target = ofmcw.synthesize(grid, truth["centers"], truth["normals"], amplitudes, config)
+    low, high = box_of(truth["centers"], 0.005)
+    params = random_start(2000, low, high, float(truth["areas"][0]), seed=1, device=device)
+    adjoint = osolver.row_basis(config, grid, low, high)
+    sample_s = osolver.timed_refit(config, grid, params, target, adjoint)
+    solve_s = osolver.timed_solve(2000)
+    scale = 16384 / len(grid)
+    refit_s = sample_s * scale + solve_s
+    return {"value": 1.0 / (2 * refit_s), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"float64 VarPro refit (closed-form columns, row-basis projection, normal equations, "
+                       f"Cholesky, rendered objective) on every {sample_stride}th aperture per axis "
+                       f"({len(grid)} of 16384) x 2000 surfels: {sample_s:.2f} s, scaled x{scale:.0f} "
+                       f"+ {solve_s:.3f} s full-size solve; a DSFW step counted as 2 refits "
+                       f"(upper bound on the oracle's step rate)")}  # fmt: skip
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    start = time.perf_counter()
+    base = cpu_baseline(args.cpu_threads)
+    wall = time.perf_counter() - start
+    return {
+        "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / base["value"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "apertures": 16384, "surfels": 2000, "batch": 256},
+        "cpu_baseline": {**base, "wall_s": round(wall, 2)},
+        "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference Slang kernels need slangtorch, which is not installed (no network); the "
+                "reference arm is the float64 oracle restatement on the host cores",
+    }  # fmt: skip
+
+
+def main():
+    parser = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=5)
+    parser.add_argument("--warmup", type=int, default=3)
+    parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    parser.add_argument("--mode", choices=["mixed", "plain"], default="mixed")
+    parser.add_argument("--cpu-threads", type=int, default=None)
+    parser.add_argument("--no-cpu-baseline", action="store_true")
+    args = parser.parse_args()
+    world, rank, local = _distributed()
+    if args.impl == "reference":
+        result = run_reference(args, world, rank)
+    else:
+        _install_gram_counter()
+        result = run_ours(args, world, rank, local)
+    if rank == 0 and result is not None:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

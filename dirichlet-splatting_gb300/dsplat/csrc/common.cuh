@@ -23,6 +23,9 @@
 #include <stdint.h>
 #include "dsplat_gb300.h"
 
+// Host-side count of kernel launches made by the library (defined in misc.cu).
+void dsg_count_launches(int kernels);
+
 namespace dsg {
 
 constexpr float kPi = 3.14159265358979323846f;

@@ -3,6 +3,7 @@
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <atomic>
 #include <mutex>
 #include "dsplat_gb300.h"
 
@@ -68,11 +69,17 @@ __global__ void range_response_kernel(double low, double high, int count, int bi
 }
 
 std::mutex g_mutex;
+std::atomic<unsigned long long> g_launches{0};
 cublasHandle_t g_handles[64] = {};
 
 }  // namespace
 
+// Every launch site of the library adds its kernel count here (host side).
+void dsg_count_launches(int kernels) { g_launches.fetch_add((unsigned long long)kernels); }
+
 extern "C" {
+
+uint64_t dsg_launch_count(void) { return g_launches.load(); }
 
 const char* dsg_version(void) { return "dsplat-gb300 0.1.0 (sm_103a)"; }
 
@@ -108,6 +115,7 @@ int dsg_energy(const float* value, const float* reference, int64_t count, double
       reinterpret_cast<const float2*>(value), reinterpret_cast<const float2*>(reference), count,
       part);
   energy_final_kernel<<<1, kEnergyThreads, 0, st>>>(part, kEnergyBlocks, out);
+  dsg_count_launches(2);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 
@@ -117,6 +125,7 @@ int dsg_range_response(double low, double high, int32_t count, int32_t bins, int
   const int64_t n = (int64_t)count * bins;
   range_response_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       low, high, count, bins, samples, nfft, reinterpret_cast<double2*>(out));
+  dsg_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 

@@ -5,6 +5,8 @@
 #include <math.h>
 #include "dsplat_gb300.h"
 
+void dsg_count_launches(int kernels);
+
 namespace {
 
 __global__ void range_gate_kernel(const float* __restrict__ points, int count,
@@ -155,6 +157,7 @@ int dsg_range_gate(const float* points, int32_t count, const float* positions,
   if (!points || !output || (apertures > 0 && (!positions || !intervals))) return DSG_ERR_ARGUMENT;
   range_gate_kernel<<<(count + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
       points, count, positions, apertures, intervals, bins, spacing, required, output);
+  dsg_count_launches(1);
   return status();
 }
 
@@ -167,6 +170,7 @@ int dsg_peaks(float* scores, const float* centers, int32_t count, int32_t dimens
   if (count == 0) return status();
   peaks_kernel<<<1, kPeakThreads, 0, (cudaStream_t)stream>>>(scores, centers, count, dimension,
                                                             peaks, separation, output);
+  dsg_count_launches(1);
   return status();
 }
 
@@ -178,6 +182,7 @@ int dsg_direction(const float* inverse, const float* gradient, const float* norm
   if (!inverse || !gradient || !normals || !mask || !output) return DSG_ERR_ARGUMENT;
   direction_kernel<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
       inverse, gradient, normals, mask, count, width, radius, output);
+  dsg_count_launches(1);
   return status();
 }
 
@@ -190,6 +195,7 @@ int dsg_trial(const float* centers, const float* normals, const float* direction
     return DSG_ERR_ARGUMENT;
   trial_kernel<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
       centers, normals, direction, controls, count, width, fraction, out_centers, out_normals);
+  dsg_count_launches(1);
   return status();
 }
 

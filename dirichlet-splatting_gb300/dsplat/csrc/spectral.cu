@@ -250,6 +250,7 @@ int dsg_spectral_render(const DsgGrid* grid, const float* taps, const float* cen
   spectral_forward_kernel<<<(size + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
       g, taps, centers, count, reinterpret_cast<const float2*>(coeff), nullptr, nullptr, bins, size,
       reinterpret_cast<float2*>(out));
+  dsg_count_launches(1);
   return status();
 }
 
@@ -270,6 +271,7 @@ int dsg_spectral_jvp(const DsgGrid* grid, const float* taps, const float* center
   spectral_forward_kernel<<<(size + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
       g, taps, centers, count, reinterpret_cast<const float2*>(coeff), delta_centers,
       reinterpret_cast<const float2*>(delta_coeff), bins, size, reinterpret_cast<float2*>(out));
+  dsg_count_launches(1);
   return status();
 }
 
@@ -309,6 +311,7 @@ int dsg_spectral_vjp(const DsgGrid* grid, const float* taps, const float* center
                                             span, spans, part);
   spectral_vjp_sum_kernel<<<(count + 127) / 128, 128, 0, st>>>(part, count, spans, g.dim,
                                                                 grad_centers, grad_coeff);
+  dsg_count_launches(2);
   return status();
 }
 
@@ -324,6 +327,7 @@ int dsg_spectral_design(const DsgGrid* grid, const float* taps, const float* cen
   spectral_design_kernel<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
       g, taps, centers, count, bins, size, reinterpret_cast<float2*>(out),
       reinterpret_cast<float2*>(jacobian));
+  dsg_count_launches(1);
   return status();
 }
 

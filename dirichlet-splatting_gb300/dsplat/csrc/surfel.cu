@@ -913,9 +913,11 @@ struct RenderLaunch {
     dim3 grid((A + 15) / 16, nseg > 0 ? nseg : 1);
     float2* dst = grid.y == 1 ? out : partial;
     kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, seg_len, dst);
+    dsg_count_launches(1);
     if (grid.y > 1) {
       const int64_t n = (int64_t)A * c.K;
       segment_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(partial, grid.y, n, out);
+      dsg_count_launches(1);
     }
     return launch_status();
   }
@@ -936,9 +938,11 @@ struct JvpLaunch {
     dim3 grid((A + 15) / 16, nseg > 0 ? nseg : 1);
     float2* dst = grid.y == 1 ? out : partial;
     kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, dcen, dnrm, dw, S, seg_len, dst);
+    dsg_count_launches(1);
     if (grid.y > 1) {
       const int64_t n = (int64_t)A * c.K;
       segment_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(partial, grid.y, n, out);
+      dsg_count_launches(1);
     }
     return launch_status();
   }
@@ -960,6 +964,7 @@ struct ReduceLaunch {
     dim3 grid((S + 15) / 16, nch);
     kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, res, chunk_len, nch, partial);
     chunk_sum_kernel<MODE><<<(S + 127) / 128, 128, 0, st>>>(partial, S, nch, o0, o1, o2, o3);
+    dsg_count_launches(2);
     return launch_status();
   }
 };
@@ -972,6 +977,7 @@ struct DesignLaunch {
     const size_t smem = table_floats(c.N, c.K) * sizeof(float);
     dim3 grid((S + 127) / 128, A);
     design_kernel<P><<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, areas, S, real, out);
+    dsg_count_launches(1);
     return launch_status();
   }
 };
@@ -984,6 +990,7 @@ struct JacobianLaunch {
     const size_t smem = table_floats(c.N, c.K) * sizeof(float);
     dim3 grid((S + 127) / 128, A);
     jacobian_kernel<P><<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, S, cols, jac);
+    dsg_count_launches(1);
     return launch_status();
   }
 };
@@ -998,6 +1005,7 @@ struct OrientLaunch {
     for (int j0 = 0; j0 < nb + 1; j0 += kBankChunk) {
       orientations_kernel<P><<<(C + 127) / 128, 128, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
                                                                  j0, res, table, ntab, ov, out);
+      dsg_count_launches(1);
     }
     return launch_status();
   }

@@ -61,6 +61,7 @@ GP = ctypes.POINTER(Grid)
 SIGNATURES = {
     "dsg_version": (ctypes.c_char_p, []),
     "dsg_error_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "dsg_launch_count": (ctypes.c_uint64, []),
     "dsg_surfel_render_workspace_bytes": (SZ, [CP, I32, I32]),
     "dsg_surfel_render": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, SZ, P]),
     "dsg_surfel_jvp": (ctypes.c_int, [CP, P, I32, P, P, P, P, P, P, I32, P, P, SZ, P]),
@@ -90,6 +91,8 @@ SIGNATURES = {
     "dsg_energy": (ctypes.c_int, [P, P, I64, P, P, SZ, P]),
     "dsg_range_response": (ctypes.c_int, [F64, F64, I32, I32, I32, I32, P, P]),
     "dsg_syrk_f32": (ctypes.c_int, [P, I64, I32, P, P]),
+    "dsg_split_transpose_bf16": (ctypes.c_int, [P, I64, I32, I64, P, P, I64, P]),
+    "dsg_gram_bf16x3": (ctypes.c_int, [P, P, I32, I32, I64, I32, P, I32, P, P]),
 }
 
 _lock = threading.Lock()
@@ -114,9 +117,22 @@ def library() -> ctypes.CDLL:
         return lib
 
 
+# Optional per-entry-point timing: name -> list of (start, end) CUDA events. Set to a
+# dict to record; None (the default) records nothing.
+TIMERS: dict | None = None
+
+
 def call(name: str, *args) -> None:
     """Invoke one entry point and raise on a nonzero status."""
-    status = getattr(library(), name)(*args)
+    if TIMERS is not None:
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record()
+        status = getattr(library(), name)(*args)
+        end.record()
+        TIMERS.setdefault(name, []).append((start, end))
+    else:
+        status = getattr(library(), name)(*args)
     if status != 0:
         message = library().dsg_error_string(status).decode()
         raise DsplatKernelError(f"{name} failed with status {status}: {message}")

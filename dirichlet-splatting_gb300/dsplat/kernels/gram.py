@@ -1,0 +1,98 @@
+"""Split-BF16x3 Gram products on the tcgen05 tensor cores (the mixed-precision path).
+
+GramRows collects projected real design rows [m, S] block by block, each stored
+transposed and split into bf16 hi + lo (dsg_split_transpose_bf16); accumulate() then
+adds PT PT^T to a float64 [S, S] total in one tcgen05 launch (dsg_gram_bf16x3), so the
+whole streamed normal-equation Gram is one dense contraction. The plain path is
+cublas.syrk (FP32 SSYRK), as in the reference's dsplat/varpro.py:108-118.
+"""
+
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from ._lib import DsplatKernelError, call, ptr
+
+SM_COUNT = 152
+
+
+def _round_up(value, step):
+    return -(-value // step) * step
+
+
+def k_splits(n_pad, k_pad):
+    """CTAs per output tile: fill the GPU in whole waves, each share at least 16 stages."""
+    tiles = n_pad // 128
+    pairs = tiles * (tiles + 1) // 2
+    stages = k_pad // 64
+    best = 1
+    for splits in range(1, max(1, stages // 16) + 1):
+        ctas = pairs * splits
+        if ctas >= 4 * SM_COUNT:
+            break
+        best = splits
+    # round the CTA count up to a whole wave when that keeps every share >= 16 stages
+    ctas = pairs * best
+    waves = -(-ctas // SM_COUNT)
+    exact = waves * SM_COUNT
+    if exact % pairs == 0 and stages // (exact // pairs) >= 16:
+        best = exact // pairs
+    return max(1, best)
+
+
+class GramRows:
+    """Transposed bf16 hi/lo storage of up to `capacity` real rows of `columns` unknowns."""
+
+    def __init__(self, columns, capacity, device):
+        self.columns = columns
+        self.n_pad = _round_up(max(columns, 1), 128)
+        self.k_pad = _round_up(max(capacity, 1), 64)
+        self.hi = torch.empty((self.n_pad, self.k_pad), dtype=torch.bfloat16, device=device)
+        self.lo = torch.empty_like(self.hi)
+        self.rows = 0
+
+    def append(self, block):
+        """Store block [m, columns] (FP32) as the next m reduction indices."""
+        block = block.to(torch.float32).contiguous()
+        m = block.shape[0]
+        if self.rows + m > self.k_pad:
+            raise DsplatKernelError("GramRows capacity exceeded")
+        call(
+            "dsg_split_transpose_bf16", ptr(block), m, self.columns, self.rows, ptr(self.hi),
+            ptr(self.lo), self.k_pad, _lib.stream(block.device),
+        )  # fmt: skip
+        self.rows += m
+
+    def accumulate(self, total):
+        """total [S, S] float64 += upper tiles of the stored rows' Gram (unused tail is zeroed)."""
+        if self.rows < self.k_pad:
+            self.hi[:, self.rows :].zero_()
+            self.lo[:, self.rows :].zero_()
+        if self.n_pad > self.columns:
+            self.hi[self.columns :].zero_()
+            self.lo[self.columns :].zero_()
+        k_pad = _round_up(max(self.rows, 1), 64)
+        status = torch.zeros(1, dtype=torch.int32, device=total.device)
+        hi, lo = self.hi[:, :k_pad], self.lo[:, :k_pad]
+        if k_pad != self.k_pad:  # a narrower view needs contiguous rows for the tensor map
+            hi, lo = hi.contiguous(), lo.contiguous()
+        call(
+            "dsg_gram_bf16x3", ptr(hi), ptr(lo), self.columns, self.n_pad, k_pad,
+            k_splits(self.n_pad, k_pad), ptr(total), total.shape[1], ptr(status),
+            _lib.stream(total.device),
+        )  # fmt: skip
+        return status
+
+
+def check(status):
+    """Raise if the Gram kernel reported a bounded wait that ran out (reads one int)."""
+    if int(status.item()) != 0:
+        raise DsplatKernelError("dsg_gram_bf16x3: a bounded wait ran out")
+
+
+def gram_accumulate(rows, total):
+    """total [S, S] float64 += upper tiles of rows^T rows for one block rows [m, S]."""
+    store = GramRows(rows.shape[1], rows.shape[0], rows.device)
+    store.append(rows)
+    check(store.accumulate(total))

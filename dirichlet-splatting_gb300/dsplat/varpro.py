@@ -91,12 +91,26 @@ def _gram_mode(config):
     return getattr(config, "gram", "fp32")
 
 
+def projected_rows(model, chunk):
+    """Number of real rows model.blocks(..., real=True, chunk) yields, known before streaming."""
+    if hasattr(model, "block_basis"):
+        bins = model.shape[1]
+        total = 0
+        for start in range(0, model.size, chunk):
+            rows = slice(start, min(start + chunk, model.size))
+            basis = model.block_basis(rows)
+            width = 2 * bins if basis is None else basis.interleaved.shape[0]
+            total += width * (-(-rows.stop // bins) - rows.start // bins)
+        return total
+    return 2 * model.size
+
+
 def normal_equations(model, params, target, config):
     """G = A^H A / M and q = A^H y / M, streamed over projected row blocks.
 
     Real blocks accumulate the upper triangle in float32 (SYRK) and fold it into a
-    float64 total every FOLD blocks; the bf16x3 mode accumulates each block's
-    product on the tensor cores and folds every block.
+    float64 total every FOLD blocks. In the bf16x3 mode every block is stored split
+    and transposed, and one tcgen05 launch adds the whole Gram to the float64 total.
     """
     count = len(params["centers"])
     chunk = row_chunk(model, count, config)
@@ -109,23 +123,26 @@ def normal_equations(model, params, target, config):
             rhs.addmv_(a.H, y)
         return (gram + gram.H) / (2 * model.size), rhs / model.size
     device = target.device
-    part = torch.zeros((count, count), dtype=torch.float32, device=device)
     total = torch.zeros((count, count), dtype=torch.float64, device=device)
     rhs = torch.zeros(count, dtype=torch.float64, device=device)
-    mixed = _gram_mode(config) == "bf16x3"
-    if mixed:
-        from .kernels.gram import gram_accumulate
-    for index, (a, y) in enumerate(stream):
-        a = a.contiguous()
-        if mixed:
-            gram_accumulate(a, total)
-        else:
+    if _gram_mode(config) == "bf16x3":
+        from .kernels.gram import GramRows, check
+
+        store = GramRows(count, projected_rows(model, chunk), device)
+        for a, y in stream:
+            store.append(a)
+            rhs += a.T @ y
+        check(store.accumulate(total))
+    else:
+        part = torch.zeros((count, count), dtype=torch.float32, device=device)
+        for index, (a, y) in enumerate(stream):
+            a = a.contiguous()
             syrk(a, part)
-        rhs += a.T @ y
-        if not mixed and index % FOLD == FOLD - 1:
-            total += part
-            part.zero_()
-    total += part
+            rhs += a.T @ y
+            if index % FOLD == FOLD - 1:
+                total += part
+                part.zero_()
+        total += part
     gram = (torch.triu(total) + torch.triu(total, 1).T) / model.size
     return gram.float(), (rhs / model.size).float()
 

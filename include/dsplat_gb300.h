@@ -63,6 +63,8 @@ typedef struct DsgGrid {
 
 const char* dsg_version(void);
 const char* dsg_error_string(int code);
+/* Kernels launched by this library since it was loaded (a host-side counter). */
+uint64_t dsg_launch_count(void);
 
 /* ---- FMCW surfels: range profiles and derivatives ------------------------------- */
 
@@ -201,6 +203,22 @@ int dsg_range_response(double low, double high, int32_t count, int32_t bins, int
 /* Plain FP32: add rows^T rows to the upper triangle of the row-major [n, n] matrix out
  * (cuBLAS SSYRK; reference: dsplat/kernels/cublas.py:31-44 syrk). rows [m, n] row-major. */
 int dsg_syrk_f32(const float* rows, int64_t m, int32_t n, float* out, void* stream);
+
+/* Mixed precision: split FP32 rows [m, n] into bf16 hi + lo and store them transposed,
+ * hi[s * ld + column_offset + r] = bf16(rows[r, s]) and lo the bf16 of the remainder.
+ * Feeds dsg_gram_bf16x3 (replaces the FP32 operand of the reference's SYRK,
+ * dsplat/varpro.py:108-118). */
+int dsg_split_transpose_bf16(const float* rows, int64_t m, int32_t n, int64_t column_offset,
+                             void* hi, void* lo, int64_t ld, void* stream);
+
+/* Mixed precision: out[n, n] (float64, row-major, leading dimension ldo) += the upper
+ * 128 x 128 tiles of PT PT^T, PT = hi + lo of shape [n_pad, k_pad] bf16 (n_pad a multiple
+ * of 128, k_pad of 64, zero padded), on the tcgen05 tensor cores in split-BF16x3 with FP32
+ * accumulation; k_splits CTAs share each tile's reduction and add their parts atomically.
+ * status (one int32, zero before the call) becomes 1 if a bounded wait ran out.
+ * Replaces dsplat/kernels/cublas.py:31-44 (cublasSsyrk_v2) on the mixed path. */
+int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, int64_t k_pad,
+                    int32_t k_splits, double* out, int32_t ldo, int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,48 @@
+"""tcgen05 split-BF16x3 Gram against float64 products (parity tests)."""
+
+from __future__ import annotations
+
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("m,n", [(64, 128), (3000, 300), (20000, 1000)])
+def test_split_bf16x3_gram_matches_float64(m, n):
+    from dsplat.kernels.gram import GramRows
+
+    generator = torch.Generator().manual_seed(m + n)
+    rows = torch.randn(m, n, generator=generator) * (1 + torch.rand(n, generator=generator))
+    rows = rows.cuda()
+    total = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    store = GramRows(n, m, "cuda")
+    half = m // 2
+    store.append(rows[:half])
+    store.append(rows[half:])
+    status = store.accumulate(total)
+    assert int(status.item()) == 0
+    expected = rows.double().T @ rows.double()
+    upper = torch.triu(torch.ones(n, n, dtype=torch.bool, device="cuda"))
+    error = (total - expected)[upper].abs().max() / expected.abs().max()
+    assert float(error) < 3e-5, float(error)
+    # The strict lower triangle of off-diagonal tiles is never written.
+    if n > 128:
+        assert float(total[200:, :128].abs().max()) == 0.0
+
+
+def test_bf16x3_is_far_more_accurate_than_one_bf16_pass():
+    from dsplat.kernels.gram import GramRows
+
+    generator = torch.Generator().manual_seed(3)
+    rows = torch.randn(4096, 256, generator=generator).cuda()
+    total = torch.zeros((256, 256), dtype=torch.float64, device="cuda")
+    store = GramRows(256, 4096, "cuda")
+    store.append(rows)
+    store.accumulate(total)
+    expected = rows.double().T @ rows.double()
+    single = rows.bfloat16().double().T @ rows.bfloat16().double()
+    upper = torch.triu(torch.ones(256, 256, dtype=torch.bool, device="cuda"))
+    err3 = float((total - expected)[upper].abs().max())
+    err1 = float((single - expected)[upper].abs().max())
+    assert err3 < err1 / 50
