@@ -174,6 +174,9 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)  # 256 MiB > L2
 
     # Device-resident steps, timed with CUDA events on the launching stream.
+    from dsplat import tracing
+
+    tracing.enable()
     _lib.TIMERS = {}
     launches0 = lib.dsg_launch_count()
     times = []
@@ -192,6 +195,8 @@ def run_ours(args, world, rank, local):
         _barrier(world)
     launches = lib.dsg_launch_count() - launches0
     timers, _lib.TIMERS = _lib.TIMERS, None
+    stages = tracing.report()
+    tracing.disable()
     step_ms = [b.elapsed_time(e) for b, e in times]
     total_s = _max_over_ranks(sum(step_ms) / 1e3, world, device)
     value = world * args.steps / total_s
@@ -245,6 +250,7 @@ def run_ours(args, world, rank, local):
         "clocks": clocks.summary(),
         "roofline": roofline,
         "kernel_ms": {k: round(v, 3) for k, v in sorted(totals.items(), key=lambda kv: -kv[1])},
+        "stage_ms": stages,
         "fit": {"iteration": history["iteration"], "nmse": history["nmse"],
                 "median_center_to_surface_m": median_distance(state.params, truth)},
     }

@@ -88,10 +88,11 @@ def fibonacci_sphere(count, device="cuda"):
 
 
 @torch.no_grad()
-def orient_candidates(model, params, residual, count, mode, table=None, chunk=8192):
+def orient_candidates(model, params, residual, count, mode, table=None, chunk=1 << 21):
     """Give every position the best normal among its own and a count-normal sphere bank.
 
     Returns the candidates with the chosen normals and their squared certificates.
+    chunk only bounds the [chunk, 1 + count] score buffers; one launch scores a chunk.
     """
     centers = params["centers"]
     bank = fibonacci_sphere(count, centers.device)

@@ -28,71 +28,71 @@ __global__ void range_gate_kernel(const float* __restrict__ points, int count,
 }
 
 constexpr int kPeakThreads = 1024;
+constexpr int kMaxAccepted = 4096;  // peaks held in shared memory per launch
 
-// Best finite score, ties to the lowest index; suppress everything within separation.
-__global__ void __launch_bounds__(kPeakThreads) peaks_kernel(float* __restrict__ scores,
+// Greedy separated peaks over candidates visited in descending-score order (ties in
+// index order): a candidate is taken unless it lies within separation of one already
+// taken. This selects the same indices in the same order as repeatedly taking the best
+// remaining finite score (lowest index on ties) and suppressing its neighbourhood
+// (reference: dsplat/kernels/search.slang:26-64). Chunks of 1024 candidates are first
+// checked against the taken set in parallel; a chunk's survivors are then resolved in
+// order, each taken one suppressing the later ones within separation.
+__global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __restrict__ scores,
+                                                             const int* __restrict__ order,
                                                              const float* __restrict__ centers,
                                                              int count, int dimension, int peaks,
                                                              float separation,
                                                              int* __restrict__ output) {
-  __shared__ float best_v[kPeakThreads / 32];
-  __shared__ int best_i[kPeakThreads / 32];
-  __shared__ int chosen;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  extern __shared__ float taken_xyz[];  // [peaks][dimension]
+  __shared__ int alive[kPeakThreads];
+  __shared__ int n_taken;
+  const int tid = threadIdx.x;
   const float sep2 = separation * separation;
-  for (int p = 0; p < peaks; ++p) {
-    float bv = -INFINITY;
-    int bi = -1;
-    for (int i = tid; i < count; i += kPeakThreads) {
-      const float v = scores[i];
-      if (isfinite(v) && (bi < 0 || v > bv)) {  // i increases, so ties keep the first
-        bv = v;
-        bi = i;
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_down_sync(0xffffffffu, bv, o);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
-        bv = ov;
-        bi = oi;
-      }
-    }
-    if (lane == 0) {
-      best_v[warp] = bv;
-      best_i[warp] = bi;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      bv = lane < kPeakThreads / 32 ? best_v[lane] : -INFINITY;
-      bi = lane < kPeakThreads / 32 ? best_i[lane] : -1;
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_down_sync(0xffffffffu, bv, o);
-        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-        if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
-          bv = ov;
-          bi = oi;
-        }
-      }
-      if (lane == 0) {
-        chosen = bi;
-        output[p] = bi;
-      }
-    }
-    __syncthreads();
-    const int index = chosen;
-    if (index < 0) return;
+  if (tid == 0) n_taken = 0;
+  __syncthreads();
+  for (int base = 0; base < count; base += kPeakThreads) {
+    if (n_taken >= peaks) break;  // uniform: shared, stable between barriers
+    const int pos = base + tid;
+    int index = -1;
     float c[8];
-    for (int j = 0; j < dimension && j < 8; ++j) c[j] = centers[(size_t)index * dimension + j];
-    for (int i = tid; i < count; i += kPeakThreads) {
+    bool ok = false;
+    if (pos < count) {
+      index = order[pos];
+      ok = isfinite(scores[index]);
+      for (int j = 0; j < dimension; ++j) c[j] = centers[(size_t)index * dimension + j];
+    }
+    const int taken_now = n_taken;
+    for (int t = 0; ok && t < taken_now; ++t) {
       float d2 = 0.0f;
-      for (int j = 0; j < dimension && j < 8; ++j) {
-        const float d = centers[(size_t)i * dimension + j] - c[j];
+      for (int j = 0; j < dimension; ++j) {
+        const float d = c[j] - taken_xyz[t * dimension + j];
         d2 += d * d;
       }
-      if (i == index || d2 < sep2) scores[i] = -INFINITY;
+      if (d2 < sep2) ok = false;
     }
+    alive[tid] = ok ? 1 : 0;
     __syncthreads();
+    const int limit = min(kPeakThreads, count - base);
+    for (int k = 0; k < limit; ++k) {
+      if (!alive[k]) continue;       // uniform
+      const int slot = n_taken;      // uniform
+      if (slot >= peaks) break;
+      if (tid == k) {
+        for (int j = 0; j < dimension; ++j) taken_xyz[slot * dimension + j] = c[j];
+        output[slot] = index;
+      }
+      __syncthreads();
+      if (tid > k && tid < limit && alive[tid]) {
+        float d2 = 0.0f;
+        for (int j = 0; j < dimension; ++j) {
+          const float d = c[j] - taken_xyz[slot * dimension + j];
+          d2 += d * d;
+        }
+        if (d2 < sep2) alive[tid] = 0;
+      }
+      if (tid == 0) n_taken = slot + 1;
+      __syncthreads();
+    }
   }
 }
 
@@ -161,15 +161,21 @@ int dsg_range_gate(const float* points, int32_t count, const float* positions,
   return status();
 }
 
-int dsg_peaks(float* scores, const float* centers, int32_t count, int32_t dimension,
-              int32_t peaks, float separation, int32_t* output, void* stream) {
-  if (count < 0 || peaks < 0 || dimension < 1 || dimension > 8) return DSG_ERR_ARGUMENT;
+int dsg_peaks(const float* scores, const int32_t* order, const float* centers, int32_t count,
+              int32_t dimension, int32_t peaks, float separation, int32_t* output, void* stream) {
+  if (count < 0 || peaks < 0 || peaks > kMaxAccepted || dimension < 1 || dimension > 8)
+    return DSG_ERR_ARGUMENT;
   if (peaks == 0) return DSG_OK;
-  if (!output || (count > 0 && (!scores || !centers))) return DSG_ERR_ARGUMENT;
+  if (!output || (count > 0 && (!scores || !order || !centers))) return DSG_ERR_ARGUMENT;
   cudaMemsetAsync(output, 0xff, (size_t)peaks * sizeof(int32_t), (cudaStream_t)stream);
   if (count == 0) return status();
-  peaks_kernel<<<1, kPeakThreads, 0, (cudaStream_t)stream>>>(scores, centers, count, dimension,
-                                                            peaks, separation, output);
+  const size_t smem = (size_t)peaks * dimension * sizeof(float);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(peaks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return DSG_ERR_LAUNCH;
+  peaks_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(scores, order, centers, count,
+                                                               dimension, peaks, separation, output);
   dsg_count_launches(1);
   return status();
 }

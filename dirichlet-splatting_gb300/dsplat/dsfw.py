@@ -19,6 +19,7 @@ from .parameters import ParameterConfig
 from .refinement import dense_slide, joint_slide, trainable
 from .replacement import merge_support, replace_one
 from .spatial import propose
+from .tracing import stage
 from .varpro import varpro
 
 LM_WAIT_LIMIT = 8  # longest run of skipped geometry steps; see DSFWConfig.lm_gain_ratio
@@ -118,7 +119,8 @@ def step(state, config, search=None):
     before = state.objective
     pool, scores = state.candidates, None
     if search is not None:
-        pool, scores, cache = propose(state, config, search)
+        with stage("propose"):
+            pool, scores, cache = propose(state, config, search)
         state = replace(state, peak_cache=cache)
     screen = None
     if 0 < config.screen_apertures < state.model.apertures:
@@ -126,17 +128,19 @@ def step(state, config, search=None):
             config.screen_apertures, config.seed + state.iteration + 2000003
         )
         screen = model, state.target[ids]
-    if {"merged": True, "utility": False}[config.replacement]:
-        state, replaced = merge_support(state, config, pool, scores)
-    else:
-        state, replaced = replace_one(state, config, pool, screen)
+    with stage("replace"):
+        if {"merged": True, "utility": False}[config.replacement]:
+            state, replaced = merge_support(state, config, pool, scores)
+        else:
+            state, replaced = replace_one(state, config, pool, screen)
     if search is not None:
         state = replace(state, search_failures=0 if replaced else state.search_failures + 1)
     middle = state.objective
     slides, skip, wait = 0, state.lm_skip, state.lm_wait
     if trainable(state.params, state.parameters) and skip == 0:
         slide = {"joint_cg": joint_slide, "dense": dense_slide}[config.lm_solver]
-        state, slides = slide(state, config, screen)
+        with stage("slide"):
+            state, slides = slide(state, config, screen)
         if config.lm_gain_ratio > 0:
             # The wait doubles while the step keeps paying too little and ends as soon
             # as it pays again, so a late-stage step is never starved.

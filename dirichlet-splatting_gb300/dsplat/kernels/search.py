@@ -27,14 +27,15 @@ def range_gate(points, positions, intervals, spacing, min_fraction):
 
 def peaks(scores, centers, count, separation):
     """Greedy best-first indices at least separation apart."""
-    work = scores.float().clone().contiguous()
+    scores = scores.float().contiguous()
     centers = f32(centers)
     wanted = min(count, len(scores))
     output = torch.empty((wanted,), device=centers.device, dtype=torch.int32)
+    order = torch.sort(scores, descending=True, stable=True).indices.to(torch.int32)
     call(
-        "dsg_peaks", ptr(work) if len(work) else None, ptr(centers) if len(centers) else None,
-        len(work), centers.shape[1], wanted, float(separation), ptr(output),
-        _lib.stream(centers.device),
+        "dsg_peaks", ptr(scores) if len(scores) else None, ptr(order) if len(order) else None,
+        ptr(centers) if len(centers) else None, len(scores), centers.shape[1], wanted,
+        float(separation), ptr(output), _lib.stream(centers.device),
     )  # fmt: skip
     return output[output >= 0].long()
 

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import torch
 
+from .tracing import stage
 from .varpro import accept, fit_coefficients, pcg, screen_bar, solve
 
 
@@ -201,17 +202,21 @@ def joint_slide(state, config, screen=None):
         target = target[ids]
     accepted = 0
     for inner in range(config.lm_steps):
-        matvec, gradient, diagonal, proposal = joint_system(
-            model, state.params, state.coefficients, target, state.parameters, config,
-            config.seed + state.iteration + inner,
-        )  # fmt: skip
-        delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations,
-                    tolerance=config.cg_tolerance)  # fmt: skip
+        with stage("slide.system"):
+            matvec, gradient, diagonal, proposal = joint_system(
+                model, state.params, state.coefficients, target, state.parameters, config,
+                config.seed + state.iteration + inner,
+            )  # fmt: skip
+        with stage("slide.pcg"):
+            delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations,
+                        tolerance=config.cg_tolerance)  # fmt: skip
         if not (torch.isfinite(delta).all() and delta @ gradient < 0):
             break
-        bar = screen_bar(screen, state.params, config)
+        with stage("slide.screen"):
+            bar = screen_bar(screen, state.params, config)
         for fraction in (1.0, 0.5, 0.25, 0.125):
-            trial = accept(state, proposal(delta, fraction), config, bar)
+            with stage("slide.accept"):
+                trial = accept(state, proposal(delta, fraction), config, bar)
             if trial is not None:
                 state, accepted = trial, accepted + 1
                 break

@@ -15,6 +15,7 @@ import torch
 
 from .certificate import certificate
 from .parameters import periodic_delta
+from .tracing import stage
 from .varpro import (
     Fit,
     accept,
@@ -208,24 +209,28 @@ def merge_support(state, config, pool, scores=None):
     if scores is None:
         residual = state.target - state.prediction
         scores = certificate(state.model, candidate, residual, config.coefficients)
-    chosen = _distinct(scores, candidate["centers"], centers, state.parameters["centers"].period,
-                       config.min_separation, config.batch)  # fmt: skip
+    with stage("replace.distinct"):
+        chosen = _distinct(scores, candidate["centers"], centers, state.parameters["centers"].period,
+                           config.min_separation, config.batch)  # fmt: skip
     if not len(chosen):
         return state, 0
     pool = {key: torch.cat((value, candidate[key][chosen])) for key, value in state.params.items()}
-    gram, rhs = pooled_statistics(state, pool, config)
+    with stage("replace.pooled"):
+        gram, rhs = pooled_statistics(state, pool, config)
     real = config.real
     eye = torch.eye(len(gram), dtype=gram.dtype, device=gram.device)
     h = (gram.real if real else gram) + config.ridge * eye
-    inverse = regularized_inverse(h, len(h) * torch.finfo(h.real.dtype).eps)
+    with stage("replace.inverse"):
+        inverse = regularized_inverse(h, len(h) * torch.finfo(h.real.dtype).eps)
     if inverse is None:
         return state, 0
     q = rhs.real if real else rhs
     old = torch.arange(len(q), device=q.device) < count
     limit = None
     while True:
-        removed = backward_elimination(inverse, q, len(chosen), None if limit is None else old,
-                                       limit or 0)  # fmt: skip
+        with stage("replace.elimination"):
+            removed = backward_elimination(inverse, q, len(chosen), None if limit is None else old,
+                                           limit or 0)  # fmt: skip
         gone = torch.zeros(len(q), device=q.device, dtype=torch.bool)
         gone[removed] = True
         owners = gone[:count].nonzero().flatten()
@@ -243,7 +248,8 @@ def merge_support(state, config, pool, scores=None):
                 moved = moved or not torch.equal(fixed, trial[key][owners])
                 trial[key][owners] = fixed
         if moved:
-            fit = varpro(state.model, trial, state.target, config)
+            with stage("replace.refit"):
+                fit = varpro(state.model, trial, state.target, config)
         else:
             trial_gram, trial_rhs = gram[ids[:, None], ids[None, :]], rhs[ids]
             b = fit_coefficients(trial_gram, trial_rhs, config)

@@ -22,6 +22,7 @@ from .certificate import (
     search_certificate,
     select_peaks,
 )
+from .tracing import stage
 
 
 @dataclass(frozen=True)
@@ -115,9 +116,10 @@ def propose(state, config, search):
         normals = state.peak_cache["normals"][:cached]
         candidates["normals"][-cached:] = normal_spec.project(normals, candidates["normals"][-cached:])
 
-    scores = score(candidates)
-    selected = select_peaks(scores, candidates["centers"], peaks, separation)
-    candidates = {key: value[selected] for key, value in candidates.items()}
+    with stage("propose.coarse"):
+        scores = score(candidates)
+        selected = select_peaks(scores, candidates["centers"], peaks, separation)
+        candidates = {key: value[selected] for key, value in candidates.items()}
     for radius, pitch in search.levels:
         offset_lower = [-radius if active else 0 for active in ~frozen]
         offset_upper = [radius if active else 0 for active in ~frozen]
@@ -129,9 +131,10 @@ def propose(state, config, search):
                       for key, value in candidates.items()}  # fmt: skip
         points = (candidates["centers"][:, None] + offsets[None]).reshape(-1, 3)
         candidates = atoms(points, candidates["normals"].repeat_interleave(len(offsets), dim=0))
-        scores = score(candidates)
-        selected = select_peaks(scores, candidates["centers"], peaks, min(separation, radius / 2))
-        candidates = {key: value[selected] for key, value in candidates.items()}
+        with stage("propose.level"):
+            scores = score(candidates)
+            selected = select_peaks(scores, candidates["centers"], peaks, min(separation, radius / 2))
+            candidates = {key: value[selected] for key, value in candidates.items()}
     # FFT-interpolated scores only propose; the refinement rescores exactly.
     initial = scores[selected] if table is None else None
     if search.refine_apertures > search.proposal_apertures:
@@ -139,19 +142,21 @@ def propose(state, config, search):
             search.refine_apertures, config.seed + state.iteration + 1000003
         )
         r, initial = residual[refine_ids], None
-    params, scores = search_certificate(
-        model, r, candidates, spec, replace(search.continuous, peaks=peaks, separation=0), mode,
-        normal_spec=refine_normals, initial_scores=initial,
-        full_model=state.model, full_residual=residual,
-    )  # fmt: skip
+    with stage("propose.refine"):
+        params, scores = search_certificate(
+            model, r, candidates, spec, replace(search.continuous, peaks=peaks, separation=0), mode,
+            normal_spec=refine_normals, initial_scores=initial,
+            full_model=state.model, full_residual=residual,
+        )  # fmt: skip
     if search.full_iterations:
         full = select_peaks(scores, params["centers"], search.full_peaks, min(separation, spec.scale / 2))
-        refined, refined_scores = search_certificate(
-            state.model, residual, {key: value[full] for key, value in params.items()}, spec,
-            replace(search.continuous, peaks=search.full_peaks, iterations=search.full_iterations,
-                    separation=0),
-            mode, normal_spec=refine_normals, initial_scores=scores[full],
-        )  # fmt: skip
+        with stage("propose.full"):
+            refined, refined_scores = search_certificate(
+                state.model, residual, {key: value[full] for key, value in params.items()}, spec,
+                replace(search.continuous, peaks=search.full_peaks, iterations=search.full_iterations,
+                        separation=0),
+                mode, normal_spec=refine_normals, initial_scores=scores[full],
+            )  # fmt: skip
         # The screened finalists stay in the pool beside the fully refined ones.
         scores = torch.cat((refined_scores, scores))
         order = scores.argsort(descending=True, stable=True)

@@ -16,6 +16,7 @@ import torch
 
 from .kernels.cublas import syrk
 from .kernels.reduce import energy
+from .tracing import stage
 
 
 class Fit(NamedTuple):
@@ -166,9 +167,12 @@ def rendered_loss(model, params, coefficients, target, ridge):
 @torch.no_grad()
 def varpro(model, params, target, config):
     """Coefficients, prediction, objective, Gram and right-hand side of one geometry."""
-    gram, rhs = normal_equations(model, params, target, config)
-    b = fit_coefficients(gram, rhs, config)
-    return Fit(b, *rendered_loss(model, params, b, target, config.ridge), gram, rhs)
+    with stage("varpro.normal"):
+        gram, rhs = normal_equations(model, params, target, config)
+    with stage("varpro.solve"):
+        b = fit_coefficients(gram, rhs, config)
+    with stage("varpro.loss"):
+        return Fit(b, *rendered_loss(model, params, b, target, config.ridge), gram, rhs)
 
 
 @torch.no_grad()

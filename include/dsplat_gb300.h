@@ -171,10 +171,12 @@ int dsg_spectral_design(const DsgGrid* grid, const float* taps, const float* cen
 int dsg_range_gate(const float* points, int32_t count, const float* positions,
                    int32_t apertures, const int32_t* intervals, int32_t bins, float spacing,
                    int32_t required, int32_t* output, void* stream);
-/* Greedy separated peaks (reference: dsplat/kernels/search.py:27-39). scores is
- * overwritten (suppressed entries become -inf); output [peaks] int32, -1 past the end. */
-int dsg_peaks(float* scores, const float* centers, int32_t count, int32_t dimension,
-              int32_t peaks, float separation, int32_t* output, void* stream);
+/* Greedy separated peaks (reference: dsplat/kernels/search.py:27-39). order [count]
+ * lists the candidate indices by descending score, ties in index order (a stable
+ * descending sort); non-finite scores are never taken. output [peaks] int32 receives
+ * the chosen indices best first, -1 past the last; peaks <= 4096. */
+int dsg_peaks(const float* scores, const int32_t* order, const float* centers, int32_t count,
+              int32_t dimension, int32_t peaks, float separation, int32_t* output, void* stream);
 /* Quasi-Newton direction per candidate (reference: dsplat/kernels/search.py:42-56). */
 int dsg_direction(const float* inverse, const float* gradient, const float* normals,
                   const float* mask, int32_t count, int32_t width, float radius, float* output,

@@ -50,7 +50,8 @@ def test_invalid_arguments_are_rejected_before_any_launch():
     assert lib.dsg_surfel_render_workspace_bytes(ctypes.byref(chirp), 16384, 2000) == 0
     assert lib.dsg_surfel_correlate_gradient(ctypes.byref(chirp), None, 1, None, None, 1, None, 4,
                                              None, None, None, None, None, 0, None) == 1  # fmt: skip
-    assert lib.dsg_peaks(None, None, 1, 9, 1, 0.0, None, None) == 1
+    assert lib.dsg_peaks(None, None, None, 1, 9, 1, 0.0, None, None) == 1
+    assert lib.dsg_peaks(None, None, None, 1, 3, 5000, 0.0, None, None) == 1
 
 
 def test_cpu_tensors_are_refused():
