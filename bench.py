@@ -1,7 +1,8 @@
 """Benchmark: DSFW steps/s of the 128^2-array, 2000-surfel sphere-cap fit (batch 256).
 
 Our arm (default): the drop-in dsplat package on libdsplat_gb300.so, mixed precision
-(split-BF16x3 tcgen05 Gram; --mode plain uses the FP32 SSYRK drop-in). Workload:
+and batched execution (split-BF16x3 tcgen05 Gram, DSFWConfig(gram="bf16x3",
+batched=True)); --mode plain is the FP32 drop-in with the reference's structure. Workload:
 the 128 x 128 array at 2.5 mm pitch, 2000 surfels on the front hemisphere of a 30 mm
 sphere at 0.35 m, scan synthesized in float64 from the ADC signal chain, fit from
 random surfels in the box plus 5 mm with SpatialSearchConfig() and
@@ -165,7 +166,8 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(device)
     lib = _lib.library()
     model, target, start, parameters, truth = build_problem(device)
-    config = DSFWConfig(iterations=100, batch=256, gram="bf16x3" if args.mode == "mixed" else "fp32")
+    mixed = args.mode == "mixed"
+    config = DSFWConfig(iterations=100, batch=256, gram="bf16x3" if mixed else "fp32", batched=mixed)
     search = SpatialSearchConfig()
     state = initialize(model, target, start, config, parameters=parameters)
     for _ in range(args.warmup):

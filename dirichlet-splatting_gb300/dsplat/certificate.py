@@ -130,13 +130,19 @@ def _controls(reference, center_spec, normal_spec, masks):
 @torch.no_grad()
 def search_certificate(
     model, residual, candidates, center_spec, config, mode, *, normal_spec=None,
-    initial_scores=None, full_model=None, full_residual=None,
+    initial_scores=None, full_model=None, full_residual=None, batched=False,
 ):  # fmt: skip
     """Refine separated peaks in xyz (and unit normals) by batched quasi-Newton ascent.
 
     Every candidate backtracks on its own inside the parameter constraints. The coarse
     peaks stay beside the refined ones, and all are reranked on full_model and
     full_residual when given. Returns parameters and scores, best first.
+
+    batched scores all backtracking fractions of an iteration in one correlation launch
+    and never reads a device value inside the ascent loop: each candidate still takes
+    the largest fraction that raises its score, and an iteration without any accepted
+    step changes nothing, so the result is the sequential search's up to the rounding
+    of the correlation sums.
     """
     reference = candidates["centers"]
     feasible = dict(candidates, centers=center_spec.project(reference, reference))
@@ -168,26 +174,31 @@ def search_certificate(
     count, dim = grad.shape
     eye = torch.eye(dim, device=reference.device).expand(count, dim, dim)
     inverse = eye.clone()
+    fractions = [0.5**backtrack for backtrack in range(config.backtracks)]
     for _ in range(config.iterations):
         direction = search.direction(inverse, grad, params["normals"], controls[1],
                                      config.trust_radius)  # fmt: skip
         old = {key: value.clone() for key, value in params.items()}
-        accepted = torch.zeros(count, dtype=torch.bool, device=reference.device)
-        for backtrack in range(config.backtracks):
-            centers, normals = search.trial(old["centers"], old["normals"], direction, controls,
-                                            0.5**backtrack)  # fmt: skip
-            trial = dict(old, centers=centers, normals=normals)
-            pending = torch.where(~accepted)[0]
-            trial_value = score({key: v[pending] for key, v in trial.items()})
-            keep = torch.zeros_like(accepted)
-            keep[pending] = torch.isfinite(trial_value) & (trial_value > value[pending])
-            for key in specs:
-                params[key][keep] = trial[key][keep]
-            accepted |= keep
-            if accepted.all():
+        if batched:
+            params, accepted = _backtrack_batched(old, direction, controls, fractions, value, specs,
+                                                  score)  # fmt: skip
+        else:
+            accepted = torch.zeros(count, dtype=torch.bool, device=reference.device)
+            for fraction in fractions:
+                centers, normals = search.trial(old["centers"], old["normals"], direction, controls,
+                                                fraction)  # fmt: skip
+                trial = dict(old, centers=centers, normals=normals)
+                pending = torch.where(~accepted)[0]
+                trial_value = score({key: v[pending] for key, v in trial.items()})
+                keep = torch.zeros_like(accepted)
+                keep[pending] = torch.isfinite(trial_value) & (trial_value > value[pending])
+                for key in specs:
+                    params[key][keep] = trial[key][keep]
+                accepted |= keep
+                if accepted.all():
+                    break
+            if not accepted.any():
                 break
-        if not accepted.any():
-            break
         new_value, new_grad = score(params, True)
         new_grad = ascent(params, new_grad)
         # Damped BFGS update of each candidate's inverse Hessian.
@@ -207,3 +218,29 @@ def search_certificate(
         scores = certificate(full_model, combined, full_residual, mode)
     order = scores.argsort(descending=True, stable=True)
     return {key: v[order] for key, v in combined.items()}, scores[order]
+
+
+def _backtrack_batched(old, direction, controls, fractions, value, specs, score):
+    """All backtracking trials of one iteration scored together; no host synchronization.
+
+    Each candidate takes the first (largest) fraction whose finite score exceeds value.
+    """
+    count = len(old["centers"])
+    trials = [search.trial(old["centers"], old["normals"], direction, controls, f) for f in fractions]
+    centers = torch.stack([c for c, _ in trials])  # [B, count, 3]
+    normals = torch.stack([n for _, n in trials])
+    batch = {key: v.repeat(len(fractions), *([1] * (v.ndim - 1))) for key, v in old.items()}
+    batch["centers"] = centers.reshape(-1, 3)
+    batch["normals"] = normals.reshape(-1, 3)
+    values = score(batch).reshape(len(fractions), count)
+    improve = torch.isfinite(values) & (values > value[None])
+    accepted = improve.any(0)
+    first = improve.to(torch.int8).argmax(0)  # first True; 0 where none
+    rows = torch.arange(count, device=first.device)
+    params = dict(old)
+    keep = accepted[:, None]
+    if "centers" in specs:
+        params["centers"] = torch.where(keep, centers[first, rows], old["centers"])
+    if "normals" in specs:
+        params["normals"] = torch.where(keep, normals[first, rows], old["normals"])
+    return params, accepted

@@ -96,6 +96,81 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
   }
 }
 
+// Best-scoring candidates that collide neither with an occupied point nor with a
+// candidate kept before them (reference: dsplat/replacement.py:142-175 _distinct):
+// candidates are visited in descending-score order (ties in index order, non-finite
+// scores skipped); a distance below separation, or exactly zero, is a collision;
+// distances fold periodic axes into [-period/2, period/2]. At most width are kept.
+__device__ __forceinline__ float folded_distance(const float* a, const float* b, int dim,
+                                                 const float* period) {
+  float d2 = 0.0f;
+  for (int j = 0; j < dim; ++j) {
+    float d = a[j] - b[j];
+    if (period != nullptr) d -= period[j] * rintf(d / period[j]);
+    d2 += d * d;
+  }
+  return sqrtf(d2);
+}
+
+__global__ void __launch_bounds__(kPeakThreads) distinct_kernel(
+    const float* __restrict__ scores, const int* __restrict__ order, const float* __restrict__ points,
+    int count, int dimension, const float* __restrict__ occupied, int n_occupied,
+    const float* __restrict__ period, float separation, int width, int* __restrict__ output,
+    int* __restrict__ kept_count) {
+  extern __shared__ float shared_xyz[];  // occupied [n_occupied][dim], then kept [width][dim]
+  float* kept_xyz = shared_xyz + (size_t)n_occupied * dimension;
+  __shared__ int alive[kPeakThreads];
+  __shared__ int n_kept;
+  __shared__ float per[8];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n_occupied * dimension; i += kPeakThreads) shared_xyz[i] = occupied[i];
+  if (tid < dimension) per[tid] = period != nullptr ? period[tid] : 0.0f;
+  if (tid == 0) n_kept = 0;
+  __syncthreads();
+  const float* pp = period != nullptr ? per : nullptr;
+  for (int base = 0; base < count; base += kPeakThreads) {
+    if (n_kept >= width) break;
+    const int pos = base + tid;
+    int index = -1;
+    float c[8];
+    bool ok = false;
+    if (pos < count) {
+      index = order[pos];
+      ok = isfinite(scores[index]);
+      for (int j = 0; j < dimension; ++j) c[j] = points[(size_t)index * dimension + j];
+    }
+    for (int o = 0; ok && o < n_occupied; ++o) {
+      const float d = folded_distance(c, shared_xyz + o * dimension, dimension, pp);
+      if (!(d >= separation) || !(d > 0.0f)) ok = false;
+    }
+    const int kept_now = n_kept;
+    for (int t = 0; ok && t < kept_now; ++t) {
+      const float d = folded_distance(c, kept_xyz + t * dimension, dimension, pp);
+      if (!(d >= separation) || !(d > 0.0f)) ok = false;
+    }
+    alive[tid] = ok ? 1 : 0;
+    __syncthreads();
+    const int limit = min(kPeakThreads, count - base);
+    for (int k = 0; k < limit; ++k) {
+      if (!alive[k]) continue;  // uniform
+      const int slot = n_kept;  // uniform
+      if (slot >= width) break;
+      if (tid == k) {
+        for (int j = 0; j < dimension; ++j) kept_xyz[slot * dimension + j] = c[j];
+        output[slot] = index;
+      }
+      __syncthreads();
+      if (tid > k && tid < limit && alive[tid]) {
+        const float d = folded_distance(c, kept_xyz + slot * dimension, dimension, pp);
+        if (!(d >= separation) || !(d > 0.0f)) alive[tid] = 0;
+      }
+      if (tid == 0) n_kept = slot + 1;
+      __syncthreads();
+    }
+  }
+  if (tid == 0) *kept_count = n_kept;
+}
+
 __global__ void direction_kernel(const float* __restrict__ inverse,
                                  const float* __restrict__ gradient,
                                  const float* __restrict__ normals, const float* __restrict__ mask,
@@ -176,6 +251,28 @@ int dsg_peaks(const float* scores, const int32_t* order, const float* centers, i
     return DSG_ERR_LAUNCH;
   peaks_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(scores, order, centers, count,
                                                                dimension, peaks, separation, output);
+  dsg_count_launches(1);
+  return status();
+}
+
+int dsg_distinct(const float* scores, const int32_t* order, const float* points, int32_t count,
+                 int32_t dimension, const float* occupied, int32_t n_occupied, const float* period,
+                 float separation, int32_t width, int32_t* output, int32_t* kept_count,
+                 void* stream) {
+  if (count < 0 || n_occupied < 0 || width < 0 || dimension < 1 || dimension > 8)
+    return DSG_ERR_ARGUMENT;
+  if (!kept_count || (width > 0 && !output)) return DSG_ERR_ARGUMENT;
+  if ((count > 0 && (!scores || !order || !points)) || (n_occupied > 0 && !occupied))
+    return DSG_ERR_ARGUMENT;
+  const size_t smem = (size_t)(n_occupied + width) * dimension * sizeof(float);
+  if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(distinct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return DSG_ERR_LAUNCH;
+  distinct_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(
+      scores, order, points, count, dimension, occupied, n_occupied, period, separation, width,
+      output, kept_count);
   dsg_count_launches(1);
   return status();
 }

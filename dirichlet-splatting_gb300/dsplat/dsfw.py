@@ -6,7 +6,9 @@ merged replacement pooling up to 1024 candidates per step, and joint Gauss-Newto
 1024 apertures that backs off while it gains less than the replacement. Behaviour
 follows the reference's dsplat/dsfw.py:20-174. DSFWConfig.gram selects the Gram
 arithmetic of the streamed normal equations: "fp32" (cuBLAS SSYRK, the reference's
-choice) or "bf16x3" (split-BF16x3 products on the tcgen05 tensor cores).
+choice) or "bf16x3" (split-BF16x3 products on the tcgen05 tensor cores);
+DSFWConfig.batched selects the batched, synchronization-free execution of the search
+and replacement loops.
 """
 
 from __future__ import annotations
@@ -54,6 +56,10 @@ class DSFWConfig:
     dictionary_elements: int = 32_000_000  # observations x atoms per streamed block
     seed: int = 0
     gram: str = "fp32"  # "fp32" or "bf16x3": arithmetic of the real Gram products
+    # Batched execution: backtracking trials scored in one launch, sync-free loops,
+    # graph-captured elimination, device-side candidate selection. Same results as the
+    # sequential path up to floating-point summation order.
+    batched: bool = False
 
     @property
     def real(self):

@@ -85,6 +85,7 @@ SIGNATURES = {
     "dsg_spectral_design": (ctypes.c_int, [GP, P, P, I32, P, I32, P, P, P]),
     "dsg_range_gate": (ctypes.c_int, [P, I32, P, I32, P, I32, F32, I32, P, P]),
     "dsg_peaks": (ctypes.c_int, [P, P, P, I32, I32, I32, F32, P, P]),
+    "dsg_distinct": (ctypes.c_int, [P, P, P, I32, I32, P, I32, P, F32, I32, P, P, P]),
     "dsg_direction": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P]),
     "dsg_trial": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P, P]),
     "dsg_energy_workspace_bytes": (SZ, [I64]),

@@ -40,6 +40,23 @@ def peaks(scores, centers, count, separation):
     return output[output >= 0].long()
 
 
+def distinct(scores, points, occupied, period, separation, width):
+    """Best-scoring candidates that collide neither with occupied points nor with each other."""
+    scores = scores.float().contiguous()
+    points, occupied = f32(points), f32(occupied)
+    order = torch.sort(scores, descending=True, stable=True).indices.to(torch.int32)
+    output = torch.empty((max(width, 1),), device=points.device, dtype=torch.int32)
+    kept = torch.zeros((1,), device=points.device, dtype=torch.int32)
+    per = None if period is None else torch.as_tensor(period, dtype=torch.float32, device=points.device)
+    call(
+        "dsg_distinct", ptr(scores) if len(scores) else None, ptr(order) if len(order) else None,
+        ptr(points) if len(points) else None, len(scores), points.shape[1],
+        ptr(occupied) if len(occupied) else None, len(occupied), ptr(per), float(separation),
+        int(width), ptr(output), ptr(kept), _lib.stream(points.device),
+    )  # fmt: skip
+    return output[: int(kept.item())].long()
+
+
 def direction(inverse, gradient, normals, mask, radius):
     """Quasi-Newton descent per candidate: tangent to unit normals, inside the trust radius."""
     count, width = gradient.shape

@@ -14,6 +14,7 @@ from dataclasses import replace
 import torch
 
 from .certificate import certificate
+from .kernels import search
 from .parameters import periodic_delta
 from .tracing import stage
 from .varpro import (
@@ -99,15 +100,18 @@ def regularized_inverse(h, floor):
     return None if factor is None else torch.cholesky_inverse(factor)
 
 
-def backward_elimination(inverse, rhs, count, limited=None, limit=0):
+def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, captured=False):
     """Remove count unknowns one at a time from the least squares with this inverse.
 
     With W the inverse of the current system and b = W q, deleting unknown j and
     refitting raises the objective by |b_j|^2 / W_jj; each step deletes the cheapest
     and continues with W - w w^H / W_jj (w = W[:, j]), kept as rank-one corrections.
     At most limit of the unknowns marked in limited are removed. Returns the removed
-    indices in order.
+    indices in order. captured replays the loop from a CUDA graph (one per shape),
+    which removes the per-step launch overhead; the arithmetic is the same.
     """
+    if captured and inverse.is_cuda:
+        return _captured_elimination(inverse, rhs, count, limited, limit)
     size = len(inverse)
     b = inverse @ rhs.to(inverse.dtype)
     diagonal = inverse.diagonal().real.clone()
@@ -133,6 +137,35 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0):
         if limited is not None:
             spent = spent + limited[index]
     return removed
+
+
+_GRAPHS: dict = {}
+
+
+def _captured_elimination(inverse, rhs, count, limited, limit):
+    """backward_elimination replayed from a cached CUDA graph keyed by shape and limit."""
+    key = (tuple(inverse.shape), inverse.dtype, inverse.device, count, limited is not None, int(limit))
+    entry = _GRAPHS.get(key)
+    if entry is None:
+        static = (inverse.clone(), rhs.to(inverse.dtype).clone(),
+                  None if limited is None else limited.clone())  # fmt: skip
+        side = torch.cuda.Stream(inverse.device)
+        side.wait_stream(torch.cuda.current_stream(inverse.device))
+        with torch.cuda.stream(side):  # warm-up outside capture
+            backward_elimination(static[0], static[1], count, static[2], limit)
+        torch.cuda.current_stream(inverse.device).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            removed = backward_elimination(static[0], static[1], count, static[2], limit)
+        entry = (graph, static, removed)
+        _GRAPHS[key] = entry
+    graph, static, removed = entry
+    static[0].copy_(inverse)
+    static[1].copy_(rhs.to(inverse.dtype))
+    if limited is not None:
+        static[2].copy_(limited)
+    graph.replay()
+    return removed.clone()
 
 
 def _distinct(scores, points, occupied, period, separation, width):
@@ -210,8 +243,13 @@ def merge_support(state, config, pool, scores=None):
         residual = state.target - state.prediction
         scores = certificate(state.model, candidate, residual, config.coefficients)
     with stage("replace.distinct"):
-        chosen = _distinct(scores, candidate["centers"], centers, state.parameters["centers"].period,
-                           config.min_separation, config.batch)  # fmt: skip
+        period = state.parameters["centers"].period
+        if getattr(config, "batched", False):
+            chosen = search.distinct(scores, candidate["centers"], centers, period,
+                                     config.min_separation, config.batch)  # fmt: skip
+        else:
+            chosen = _distinct(scores, candidate["centers"], centers, period, config.min_separation,
+                               config.batch)  # fmt: skip
     if not len(chosen):
         return state, 0
     pool = {key: torch.cat((value, candidate[key][chosen])) for key, value in state.params.items()}
@@ -230,7 +268,7 @@ def merge_support(state, config, pool, scores=None):
     while True:
         with stage("replace.elimination"):
             removed = backward_elimination(inverse, q, len(chosen), None if limit is None else old,
-                                           limit or 0)  # fmt: skip
+                                           limit or 0, captured=getattr(config, "batched", False))  # fmt: skip
         gone = torch.zeros(len(q), device=q.device, dtype=torch.bool)
         gone[removed] = True
         owners = gone[:count].nonzero().flatten()

@@ -146,7 +146,7 @@ def propose(state, config, search):
         params, scores = search_certificate(
             model, r, candidates, spec, replace(search.continuous, peaks=peaks, separation=0), mode,
             normal_spec=refine_normals, initial_scores=initial,
-            full_model=state.model, full_residual=residual,
+            full_model=state.model, full_residual=residual, batched=getattr(config, "batched", False),
         )  # fmt: skip
     if search.full_iterations:
         full = select_peaks(scores, params["centers"], search.full_peaks, min(separation, spec.scale / 2))
@@ -156,6 +156,7 @@ def propose(state, config, search):
                 replace(search.continuous, peaks=search.full_peaks, iterations=search.full_iterations,
                         separation=0),
                 mode, normal_spec=refine_normals, initial_scores=scores[full],
+                batched=getattr(config, "batched", False),
             )  # fmt: skip
         # The screened finalists stay in the pool beside the fully refined ones.
         scores = torch.cat((refined_scores, scores))

@@ -177,6 +177,15 @@ int dsg_range_gate(const float* points, int32_t count, const float* positions,
  * the chosen indices best first, -1 past the last; peaks <= 4096. */
 int dsg_peaks(const float* scores, const int32_t* order, const float* centers, int32_t count,
               int32_t dimension, int32_t peaks, float separation, int32_t* output, void* stream);
+/* Candidates (visited in the given descending-score order, non-finite skipped) that
+ * lie at least separation from every occupied point and every earlier kept candidate,
+ * and never at distance zero; periodic axes fold when period [dimension] is non-null.
+ * output [width] receives the kept indices, kept_count (device) their number
+ * (reference: dsplat/replacement.py:142-175 _distinct). */
+int dsg_distinct(const float* scores, const int32_t* order, const float* points, int32_t count,
+                 int32_t dimension, const float* occupied, int32_t n_occupied, const float* period,
+                 float separation, int32_t width, int32_t* output, int32_t* kept_count,
+                 void* stream);
 /* Quasi-Newton direction per candidate (reference: dsplat/kernels/search.py:42-56). */
 int dsg_direction(const float* inverse, const float* gradient, const float* normals,
                   const float* mask, int32_t count, int32_t width, float radius, float* output,

@@ -1,0 +1,80 @@
+"""The batched execution (DSFWConfig.batched) against the sequential reference structure."""
+
+from __future__ import annotations
+
+import itertools
+
+import pytest
+import torch
+from conftest import close, fmcw_specs, surfels
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("separation,period", [(0.0, None), (0.05, None), (1.5, (24.0, 20.0))])
+def test_device_distinct_equals_the_sequential_selection(separation, period):
+    from dsplat.kernels import search
+    from dsplat.replacement import _distinct
+
+    generator = torch.Generator().manual_seed(7)
+    dim = 3 if period is None else 2
+    scale = 1.0 if period is None else 24.0
+    points = (torch.rand(3000, dim, generator=generator) * scale).cuda()
+    points[10] = points[3]  # an exact duplicate must collide even at separation 0
+    occupied = (torch.rand(200, dim, generator=generator) * scale).cuda()
+    occupied[5] = points[20]
+    scores = torch.rand(3000, generator=generator).cuda()
+    scores[::17] = -torch.inf
+    scores[40] = scores[41]
+    for width in (1, 64, 1000):
+        got = search.distinct(scores, points, occupied, period, separation, width)
+        expected = _distinct(scores, points, occupied, period, separation, width)
+        assert got.tolist() == expected.tolist()
+
+
+def test_captured_elimination_equals_the_eager_loop():
+    from dsplat.replacement import backward_elimination
+
+    generator = torch.Generator().manual_seed(5)
+    x = torch.randn(300, 60, generator=generator, dtype=torch.float64)
+    h = x.T @ x
+    q = x.T @ torch.randn(300, generator=generator, dtype=torch.float64)
+    inverse, q = torch.linalg.inv(h).cuda(), q.cuda()
+    limited = torch.arange(60, device="cuda") < 40
+    for lim, l in ((None, 0), (limited, 5)):
+        eager = backward_elimination(inverse, q, 20, lim, l)
+        for _ in range(2):  # the second call replays the cached graph
+            captured = backward_elimination(inverse, q, 20, lim, l, captured=True)
+            assert torch.equal(eager, captured)
+
+
+def test_batched_certificate_search_matches_the_sequential_search(fmcw):
+    from dsplat.certificate import CertificateSearchConfig, search_certificate
+
+    model, params, coefficients = fmcw
+    residual = model.scan.data
+    generator = torch.Generator().manual_seed(2)
+    start = {k: v.repeat(6, *([1] * (v.ndim - 1))) for k, v in params.items()}
+    start["centers"] = start["centers"] + (3e-4 * torch.randn(start["centers"].shape, generator=generator)).cuda()
+    specs = fmcw_specs()
+    config = CertificateSearchConfig(peaks=30, separation=0, iterations=12)
+    seq, seq_scores = search_certificate(model, residual, start, specs["centers"], config, "real",
+                                         normal_spec=specs["normals"])  # fmt: skip
+    bat, bat_scores = search_certificate(model, residual, start, specs["centers"], config, "real",
+                                         normal_spec=specs["normals"], batched=True)  # fmt: skip
+    close(bat_scores, seq_scores, 1e-4)
+    close(bat["centers"], seq["centers"], 1e-4)
+
+
+def test_batched_steps_never_raise_the_objective(fmcw):
+    from dsplat import DSFWConfig, initialize, step
+
+    model, params, _ = fmcw
+    config = DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=16, screen_apertures=16,
+                        batched=True, gram="bf16x3")  # fmt: skip
+    state = initialize(model, model.scan.data, surfels(5, seed=9), config, candidates=params,
+                       parameters=fmcw_specs())  # fmt: skip
+    for _ in range(4):
+        state = step(state, config)
+    objectives = [entry["objective"] for entry in state.history]
+    assert all(b <= a for a, b in itertools.pairwise(objectives)) and objectives[-1] < objectives[0]
