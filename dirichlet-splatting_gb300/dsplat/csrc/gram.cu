@@ -136,8 +136,8 @@ __device__ __forceinline__ void tc_fence_after() {
 __global__ void __launch_bounds__(THREADS, 1)
     gram_bf16x3_kernel(const __grid_constant__ CUtensorMap map_hi,
                        const __grid_constant__ CUtensorMap map_lo, int tiles_per_side,
-                       int stages_total, int k_splits, double* __restrict__ out, int n, int ldo,
-                       int* __restrict__ status) {
+                       int tile_from, int stages_total, int k_splits, double* __restrict__ out,
+                       int n, int ldo, int* __restrict__ status) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -147,14 +147,23 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
-  // Upper-triangle tile (ti <= tj) of this CTA, row-major over the triangle.
-  int rem = blockIdx.x, ti = 0, per_row = tiles_per_side;
-  while (rem >= per_row) {
-    rem -= per_row;
-    ++ti;
-    --per_row;
+  // Tile (ti, tj) of this CTA: every upper-triangle tile (ti <= tj) whose column tile
+  // is at least tile_from; rows above tile_from first, then the remaining triangle.
+  const int band = tiles_per_side - tile_from;
+  int ti, tj;
+  if ((int)blockIdx.x < tile_from * band) {
+    ti = blockIdx.x / band;
+    tj = tile_from + blockIdx.x % band;
+  } else {
+    int rem = blockIdx.x - tile_from * band, per_row = band;
+    ti = tile_from;
+    while (rem >= per_row) {
+      rem -= per_row;
+      ++ti;
+      --per_row;
+    }
+    tj = ti + rem;
   }
-  const int tj = ti + rem;
   const bool diag = ti == tj;
   const int s_begin = (int)((int64_t)blockIdx.y * stages_total / k_splits);
   const int s_end = (int)((int64_t)(blockIdx.y + 1) * stages_total / k_splits);
@@ -334,8 +343,10 @@ int dsg_split_transpose_bf16(const float* rows, int64_t m, int32_t n, int64_t co
 }
 
 int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, int64_t k_pad,
-                    int32_t k_splits, double* out, int32_t ldo, int32_t* status, void* stream) {
-  if (n < 0 || n_pad < n || n_pad % BM != 0 || k_pad < 0 || k_pad % BK != 0 || ldo < n)
+                    int32_t column_from, int32_t k_splits, double* out, int32_t ldo,
+                    int32_t* status, void* stream) {
+  if (n < 0 || n_pad < n || n_pad % BM != 0 || k_pad < 0 || k_pad % BK != 0 || ldo < n ||
+      column_from < 0 || column_from > n)
     return DSG_ERR_ARGUMENT;
   if (n == 0 || k_pad == 0) return DSG_OK;
   if (!hi || !lo || !out || !status || k_splits < 1) return DSG_ERR_ARGUMENT;
@@ -346,7 +357,9 @@ int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, in
   if (!make_map(&map_hi, hi, n_pad, k_pad) || !make_map(&map_lo, lo, n_pad, k_pad))
     return DSG_ERR_ARGUMENT;
   const int tiles = n_pad / BM;
-  const int pairs = tiles * (tiles + 1) / 2;
+  const int tile_from = column_from / BN;
+  const int band = tiles - tile_from;
+  const int pairs = tile_from * band + band * (band + 1) / 2;
   const int stages = (int)(k_pad / BK);
   if (k_splits > stages) k_splits = stages;
   const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
@@ -355,7 +368,7 @@ int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, in
     return DSG_ERR_LAUNCH;
   dim3 grid(pairs, k_splits);
   gram_bf16x3_kernel<<<grid, THREADS, smem, (cudaStream_t)stream>>>(
-      map_hi, map_lo, tiles, stages, k_splits, out, n, ldo, status);
+      map_hi, map_lo, tiles, tile_from, stages, k_splits, out, n, ldo, status);
   dsg_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }

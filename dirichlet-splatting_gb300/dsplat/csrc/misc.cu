@@ -129,6 +129,32 @@ int dsg_range_response(double low, double high, int32_t count, int32_t bins, int
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 
+static cublasHandle_t handle_for_current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_handles[dev] && cublasCreate(&g_handles[dev]) != CUBLAS_STATUS_SUCCESS) g_handles[dev] = nullptr;
+  return g_handles[dev];
+}
+
+int dsg_gemm_f32_bf16x9(int32_t m, int32_t n, int32_t k, const float* a, int32_t lda, const float* b,
+                        int32_t ldb, float beta, float* c, int32_t ldc, void* stream) {
+  if (m < 0 || n < 0 || k < 0 || lda < k || ldb < n || ldc < n) return DSG_ERR_ARGUMENT;
+  if (m == 0 || n == 0) return DSG_OK;
+  if (!a || !b || !c) return DSG_ERR_ARGUMENT;
+  cublasHandle_t h = handle_for_current_device();
+  if (!h) return DSG_ERR_LIBRARY;
+  if (cublasSetStream(h, (cudaStream_t)stream) != CUBLAS_STATUS_SUCCESS) return DSG_ERR_LIBRARY;
+  cublasSetEmulationStrategy(h, CUBLAS_EMULATION_STRATEGY_EAGER);
+  const float one = 1.0f;
+  // Row-major C = A B is column-major C^T = B^T A^T.
+  cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, n, m, k, &one, b, CUDA_R_32F, ldb, a,
+                                   CUDA_R_32F, lda, &beta, c, CUDA_R_32F, ldc,
+                                   CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT);
+  cublasSetEmulationStrategy(h, CUBLAS_EMULATION_STRATEGY_DEFAULT);
+  return st == CUBLAS_STATUS_SUCCESS ? DSG_OK : DSG_ERR_LIBRARY;
+}
+
 int dsg_syrk_f32(const float* rows, int64_t m, int32_t n, float* out, void* stream) {
   if (m < 0 || n < 0 || m > 2147483647LL) return DSG_ERR_ARGUMENT;
   if (m == 0 || n == 0) return DSG_OK;

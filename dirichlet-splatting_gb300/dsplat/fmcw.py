@@ -23,6 +23,7 @@ import torch.nn.functional as F
 
 from . import surfel
 from .kernels import search
+from .kernels.gemm import project
 from .kernels.response import range_response
 
 
@@ -96,7 +97,7 @@ class RowBasis:
         """Real rows ordered bin by bin, (2 k + part) * blocks + block, in one product."""
         tail = rows.shape[1:]
         flat = rows.reshape(self.interleaved.shape[1], -1)
-        return (self.interleaved @ flat).reshape(-1, *tail)
+        return project(self.interleaved, flat).reshape(-1, *tail)
 
 
 def response_basis(config, low, high, device):

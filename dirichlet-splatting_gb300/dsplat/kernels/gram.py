@@ -21,10 +21,16 @@ def _round_up(value, step):
     return -(-value // step) * step
 
 
-def k_splits(n_pad, k_pad):
+def tile_pairs(n_pad, column_from=0):
+    """Number of upper-triangle 128 x 128 tiles whose column tile is at least column_from's."""
+    tiles, first = n_pad // 128, column_from // 128
+    band = tiles - first
+    return first * band + band * (band + 1) // 2
+
+
+def k_splits(n_pad, k_pad, column_from=0):
     """CTAs per output tile: fill the GPU in whole waves, each share at least 16 stages."""
-    tiles = n_pad // 128
-    pairs = tiles * (tiles + 1) // 2
+    pairs = tile_pairs(n_pad, column_from)
     stages = k_pad // 64
     best = 1
     for splits in range(1, max(1, stages // 16) + 1):
@@ -64,8 +70,11 @@ class GramRows:
         )  # fmt: skip
         self.rows += m
 
-    def accumulate(self, total):
-        """total [S, S] float64 += upper tiles of the stored rows' Gram (unused tail is zeroed)."""
+    def accumulate(self, total, column_from=0):
+        """total [S, S] float64 += upper tiles of the stored rows' Gram (unused tail is zeroed).
+
+        column_from > 0 computes only the tiles that hold columns >= column_from.
+        """
         if self.rows < self.k_pad:
             self.hi[:, self.rows :].zero_()
             self.lo[:, self.rows :].zero_()
@@ -78,8 +87,8 @@ class GramRows:
         if k_pad != self.k_pad:  # a narrower view needs contiguous rows for the tensor map
             hi, lo = hi.contiguous(), lo.contiguous()
         call(
-            "dsg_gram_bf16x3", ptr(hi), ptr(lo), self.columns, self.n_pad, k_pad,
-            k_splits(self.n_pad, k_pad), ptr(total), total.shape[1], ptr(status),
+            "dsg_gram_bf16x3", ptr(hi), ptr(lo), self.columns, self.n_pad, k_pad, int(column_from),
+            k_splits(self.n_pad, k_pad, column_from), ptr(total), total.shape[1], ptr(status),
             _lib.stream(total.device),
         )  # fmt: skip
         return status

@@ -120,22 +120,26 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, captured
     removed = torch.zeros(count, device=inverse.device, dtype=torch.long)
     spent = torch.zeros((), device=inverse.device, dtype=torch.long)
     tiny = torch.finfo(diagonal.dtype).tiny
+    # Indexing with device tensors (index_select / index_fill_) keeps every step on the
+    # device: no value is read back, so the loop can also be captured in a CUDA graph.
     for step in range(count):
         cost = b.abs().square() / diagonal.clamp(min=tiny)
         blocked = ~alive if limited is None else ~alive | (limited & (spent >= limit))
-        index = cost.masked_fill(blocked, torch.inf).argmin()
-        column = inverse[:, index] - updates[:, :step] @ updates[index, :step].conj()
-        pivot = column[index].real.clamp(min=tiny)
-        b = b - column * (b[index] / pivot)
+        index = cost.masked_fill(blocked, torch.inf).argmin().view(1)
+        column = inverse.index_select(1, index)[:, 0]
+        if step:
+            column = column - updates[:, :step] @ updates.index_select(0, index)[0, :step].conj()
+        pivot = column.index_select(0, index).real.clamp(min=tiny)
+        b = b - column * (b.index_select(0, index) / pivot)
         scaled = column / pivot.sqrt()
         updates[:, step] = scaled
         diagonal = diagonal - scaled.abs().square()
-        alive[index] = False
-        diagonal[index] = 1.0  # a removed unknown stays masked; this keeps its cost finite
-        b[index] = 0
-        removed[step] = index
+        alive.index_fill_(0, index, False)
+        diagonal.index_fill_(0, index, 1.0)  # a removed unknown stays masked; this keeps its cost finite
+        b.index_fill_(0, index, 0)
+        removed[step : step + 1] = index
         if limited is not None:
-            spent = spent + limited[index]
+            spent = spent + limited.index_select(0, index)[0]
     return removed
 
 
@@ -206,24 +210,53 @@ def _distinct(scores, points, occupied, period, separation, width):
 def pooled_statistics(state, pool, config):
     """Gram and right-hand side over the support followed by the pooled new atoms.
 
-    Only the new columns are streamed; the support block is the state's.
+    Only the new columns are streamed; the support block is the state's. With
+    DSFWConfig.gram == "bf16x3" (real coefficients) the cross products of all pooled
+    rows against the new columns are one tcgen05 launch over the stored split rows.
     """
     model, count = state.model, len(state.coefficients)
     total, added = len(pool["centers"]), len(pool["centers"]) - count
     gram = state.gram.new_empty((total, total))
     rhs = state.rhs.new_empty(total)
     gram[:count, :count], rhs[:count] = state.gram, state.rhs
-    cross = state.gram.new_zeros((total, added))
-    right = state.rhs.new_zeros(added)
-    for a, y in model.blocks(pool, state.target, config.real, row_chunk(model, total, config)):
-        new = a[:, count:]
-        cross.addmm_(a.H, new)
-        right.addmv_(new.H, y)
+    chunk = row_chunk(model, total, config)
+    if config.real and getattr(config, "gram", "fp32") == "bf16x3":
+        cross, right = _pooled_cross_mixed(model, pool, state.target, count, added, chunk, config)
+    else:
+        cross = state.gram.new_zeros((total, added))
+        right = state.rhs.new_zeros(added)
+        for a, y in model.blocks(pool, state.target, config.real, chunk):
+            new = a[:, count:]
+            cross.addmm_(a.H, new)
+            right.addmv_(new.H, y)
     cross /= model.size
     gram[:, count:], gram[count:, :] = cross, cross.H
     gram[count:, count:] = (cross[count:] + cross[count:].H) * 0.5
     rhs[count:] = right / model.size
     return gram, rhs
+
+
+def _pooled_cross_mixed(model, pool, target, count, added, chunk, config):
+    """cross [total, added] = A^T A[:, count:] and right = A[:, count:]^T y on the tensor cores."""
+    from .kernels.gemm import emulated
+    from .kernels.gram import GramRows, check
+    from .varpro import projected_rows
+
+    total = count + added
+    device = target.device
+    store = GramRows(total, projected_rows(model, chunk), device)
+    right = torch.zeros(added, dtype=torch.float64, device=device)
+    with emulated():
+        for a, y in model.blocks(pool, target, True, chunk):
+            store.append(a)
+            right += a[:, count:].T @ y
+    products = torch.zeros((total, total), dtype=torch.float64, device=device)
+    check(store.accumulate(products, column_from=count))
+    cross = torch.empty((total, added), dtype=torch.float64, device=device)
+    cross[:count] = products[:count, count:]
+    block = products[count:, count:]
+    cross[count:] = torch.triu(block) + torch.triu(block, 1).T
+    return cross.to(torch.float32), right.to(torch.float32)
 
 
 @torch.no_grad()

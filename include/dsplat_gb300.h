@@ -215,6 +215,12 @@ int dsg_range_response(double low, double high, int32_t count, int32_t bins, int
  * (cuBLAS SSYRK; reference: dsplat/kernels/cublas.py:31-44 syrk). rows [m, n] row-major. */
 int dsg_syrk_f32(const float* rows, int64_t m, int32_t n, float* out, void* stream);
 
+/* Row-major C[m, n] = A[m, k] B[k, n] + beta C on the tensor cores with FP32-accurate
+ * BF16x9 emulation (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9). The mixed path's row-basis
+ * projection of design blocks (replaces the FP32 GEMM of dsplat/fmcw.py:128-131). */
+int dsg_gemm_f32_bf16x9(int32_t m, int32_t n, int32_t k, const float* a, int32_t lda, const float* b,
+                        int32_t ldb, float beta, float* c, int32_t ldc, void* stream);
+
 /* Mixed precision: split FP32 rows [m, n] into bf16 hi + lo and store them transposed,
  * hi[s * ld + column_offset + r] = bf16(rows[r, s]) and lo the bf16 of the remainder.
  * Feeds dsg_gram_bf16x3 (replaces the FP32 operand of the reference's SYRK,
@@ -226,10 +232,13 @@ int dsg_split_transpose_bf16(const float* rows, int64_t m, int32_t n, int64_t co
  * 128 x 128 tiles of PT PT^T, PT = hi + lo of shape [n_pad, k_pad] bf16 (n_pad a multiple
  * of 128, k_pad of 64, zero padded), on the tcgen05 tensor cores in split-BF16x3 with FP32
  * accumulation; k_splits CTAs share each tile's reduction and add their parts atomically.
+ * Only tiles whose columns reach column_from or beyond are computed (0: the whole upper
+ * triangle; the pooled cross-Gram of dsplat/replacement.py:178-199 needs the new columns).
  * status (one int32, zero before the call) becomes 1 if a bounded wait ran out.
  * Replaces dsplat/kernels/cublas.py:31-44 (cublasSsyrk_v2) on the mixed path. */
 int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, int64_t k_pad,
-                    int32_t k_splits, double* out, int32_t ldo, int32_t* status, void* stream);
+                    int32_t column_from, int32_t k_splits, double* out, int32_t ldo,
+                    int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -47,3 +47,33 @@ def test_bf16x3_is_far_more_accurate_than_one_bf16_pass():
     err1 = float((single - expected)[upper].abs().max())
     # FP32 accumulation in TMEM dominates what remains of the split-BF16x3 error.
     assert err3 < err1 / 10
+
+
+def test_column_range_gram_covers_the_new_columns():
+    from dsplat.kernels.gram import GramRows
+
+    generator = torch.Generator().manual_seed(9)
+    m, n, start = 5000, 700, 450
+    rows = torch.randn(m, n, generator=generator).cuda()
+    total = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    store = GramRows(n, m, "cuda")
+    store.append(rows)
+    assert int(store.accumulate(total, column_from=start).item()) == 0
+    expected = rows.double().T @ rows.double()
+    i, j = torch.meshgrid(torch.arange(n), torch.arange(n), indexing="ij")
+    needed = ((i <= j) & (j >= start)).cuda()
+    error = (total - expected)[needed].abs().max() / expected.abs().max()
+    assert float(error) < 3e-5
+    assert float(total[:, : start - 128].abs().max()) == 0.0  # columns of earlier tiles untouched
+
+
+def test_emulated_projection_is_fp32_accurate():
+    from dsplat.kernels.gemm import emulated, project
+
+    generator = torch.Generator().manual_seed(10)
+    matrix = torch.randn(60, 256, generator=generator).cuda()
+    rows = torch.randn(256, 40000, generator=generator).cuda()
+    with emulated():
+        fast = project(matrix, rows)
+    exact = matrix.double() @ rows.double()
+    assert float((fast.double() - exact).abs().max() / exact.abs().max()) < 1e-5

@@ -390,3 +390,17 @@ def test_spatial_search_proposes_the_true_reflector():
     candidates, scores, _ = propose(state, dsfw_config, search)
     assert float((candidates["centers"][0] - truth["centers"][0]).norm()) < 1e-4
     assert math.isfinite(float(scores[0]))
+
+
+def test_mixed_pooled_statistics_match_the_fp32_stream(fmcw):
+    from dsplat import DSFWConfig, initialize
+    from dsplat.replacement import pooled_statistics
+
+    model, params, _ = fmcw
+    plain, mixed = DSFWConfig(), DSFWConfig(gram="bf16x3", batched=True)
+    state = initialize(model, model.scan.data, surfels(5, seed=2), plain, parameters=fmcw_specs())
+    pool = {k: torch.cat((v, params[k])) for k, v in state.params.items()}
+    gram, rhs = pooled_statistics(state, pool, plain)
+    mixed_gram, mixed_rhs = pooled_statistics(state, pool, mixed)
+    close(mixed_gram, gram, 1e-4)
+    close(mixed_rhs, rhs, 1e-4)
