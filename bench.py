@@ -180,6 +180,7 @@ def run_ours(args, world, rank, local):
 
     tracing.enable()
     _lib.TIMERS = {}
+    _lib.WORK = {}
     launches0 = lib.dsg_launch_count()
     times = []
     with ClockSampler(local) as clocks:
@@ -197,6 +198,7 @@ def run_ours(args, world, rank, local):
         _barrier(world)
     launches = lib.dsg_launch_count() - launches0
     timers, _lib.TIMERS = _lib.TIMERS, None
+    work, _lib.WORK = dict(_lib.WORK), {}
     stages = tracing.report()
     tracing.disable()
     step_ms = [b.elapsed_time(e) for b, e in times]
@@ -228,7 +230,7 @@ def run_ours(args, world, rank, local):
 
     # Roofline of the dominant library kernel over the timed steps.
     totals = {name: sum(b.elapsed_time(e) for b, e in pairs) for name, pairs in timers.items()}
-    roofline = _roofline(totals, timers, args)
+    roofline = _roofline(totals, timers, work, args)
     history = state.history[-1]
     result = {
         "metric": METRIC,
@@ -261,7 +263,7 @@ def run_ours(args, world, rank, local):
     return result
 
 
-def _roofline(totals, timers, args):
+def _roofline(totals, timers, work, args):
     peaks, source = _peaks()
     if not totals:
         return None
@@ -269,10 +271,11 @@ def _roofline(totals, timers, args):
     launches = len(timers[name])
     avg_ms = totals[name] / launches
     if name == "dsg_gram_bf16x3":
-        # Logical FP32 work of the symmetric product, R S (S + 1) per launch, against the
-        # sustained bf16 tensor peak / 3 (three bf16 products per logical multiply-add).
-        flops = GRAM_WORK.get("flops_per_launch")
-        achieved = flops / (avg_ms * 1e-3) / 1e12 if flops else None
+        # Logical FP32 work of the symmetric products (R S (S + 1) for a full Gram) over the
+        # launches' measured time, against the sustained bf16 tensor peak / 3 (three bf16
+        # products per logical multiply-add).
+        flops = work.get(name)
+        achieved = flops / (totals[name] * 1e-3) / 1e12 if flops else None
         peak = peaks["bf16_tflops_sustained"] / 3
         return {"kernel": name, "bound": "tensor", "achieved": achieved and round(achieved, 2),
                 "peak": round(peak, 2), "unit": "TFLOP/s",
@@ -281,22 +284,6 @@ def _roofline(totals, timers, args):
                 "avg_ms": round(avg_ms, 4)}  # fmt: skip
     return {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": None, "traffic": None, "launches": launches, "avg_ms": round(avg_ms, 4)}  # fmt: skip
-
-
-GRAM_WORK: dict = {}
-
-
-def _install_gram_counter():
-    """Record the logical flops of each Gram launch (R S (S + 1)) for the roofline."""
-    from dsplat.kernels import gram as gram_module
-
-    original = gram_module.GramRows.accumulate
-
-    def accumulate(self, total):
-        GRAM_WORK["flops_per_launch"] = float(self.rows) * self.columns * (self.columns + 1)
-        return original(self, total)
-
-    gram_module.GramRows.accumulate = accumulate
 
 
 def cpu_baseline(threads=None, sample_stride=8):
@@ -366,7 +353,6 @@ def main():
     if args.impl == "reference":
         result = run_reference(args, world, rank)
     else:
-        _install_gram_counter()
         result = run_ours(args, world, rank, local)
     if rank == 0 and result is not None:
         print(json.dumps(result), flush=True)

@@ -122,6 +122,14 @@ def library() -> ctypes.CDLL:
 # Optional per-entry-point timing: name -> list of (start, end) CUDA events. Set to a
 # dict to record; None (the default) records nothing.
 TIMERS: dict | None = None
+# Optional algorithmic work per entry point (flops or bytes, as each caller defines),
+# accumulated while TIMERS is recording.
+WORK: dict = {}
+
+
+def add_work(name: str, units: float) -> None:
+    if TIMERS is not None:
+        WORK[name] = WORK.get(name, 0.0) + float(units)
 
 
 def call(name: str, *args) -> None:

@@ -86,6 +86,9 @@ class GramRows:
         hi, lo = self.hi[:, :k_pad], self.lo[:, :k_pad]
         if k_pad != self.k_pad:  # a narrower view needs contiguous rows for the tensor map
             hi, lo = hi.contiguous(), lo.contiguous()
+        # logical FP32 flops of the needed symmetric block (a SYRK count)
+        added = self.columns - int(column_from)
+        _lib.add_work("dsg_gram_bf16x3", float(self.rows) * added * (2 * int(column_from) + added + 1))
         call(
             "dsg_gram_bf16x3", ptr(hi), ptr(lo), self.columns, self.n_pad, k_pad, int(column_from),
             k_splits(self.n_pad, k_pad, column_from), ptr(total), total.shape[1], ptr(status),
