@@ -339,6 +339,109 @@ def run_reference(args, world, rank):
     }  # fmt: skip
 
 
+def _event_time(fn, iterations, warmup, flush):
+    """Average milliseconds of fn() over iterations, CUDA events, L2 flushed before each."""
+    for _ in range(warmup):
+        fn()
+    total = 0.0
+    for _ in range(iterations):
+        flush.zero_()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        fn()
+        end.record()
+        torch.cuda.synchronize()
+        total += start.elapsed_time(end)
+    return total / iterations
+
+
+def run_kernels(args):
+    """Per-kernel roofline table on the sphere-cap geometry (the workload of the DSFW bench).
+
+    full: 128^2 apertures x 2000 surfels (C3 sizes); small: 32^2 apertures x 256 surfels.
+    Work units: pair-bins (aperture x surfel x bin) with the FP32 flop counts per
+    pair-bin 16 (forward), 24 (JVP), 20 (VJP), 18 (correlation); the Gram as logical
+    FP32 flops R S (S + 1).
+    """
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from dsplat import FMCWConfig
+    from dsplat.certificate import fibonacci_sphere
+    from dsplat.kernels import surfel as kernel
+    from dsplat.kernels.gram import GramRows
+    from dsplat.workloads import sphere_cap
+
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    peaks, source = _peaks()
+    small = args.case == "small"
+    config = FMCWConfig()
+    positions, params, reflectivity = sphere_cap(side=32 if small else 128, surfel_count=256 if small else 2000,
+                                                 device=device)  # fmt: skip
+    centers, normals = params["centers"], params["normals"]
+    A, S, K = len(positions), len(centers), config.num_range_bins
+    generator = torch.Generator().manual_seed(0)
+    weights = (reflectivity * params["areas"].sqrt()).to(torch.complex64)
+    upstream = torch.complex(torch.randn(A, K, generator=generator), torch.randn(A, K, generator=generator)).to(device)
+    dc = torch.randn(S, 3, generator=generator).to(device) * 1e-4
+    dn = torch.randn(S, 3, generator=generator).to(device) * 1e-2
+    dw = weights * 0.1
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    fp32_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12  # nominal TFLOP/s
+    rows = []
+
+    def record(name, ms, units, flops_per_unit, unit="pair-bins"):
+        achieved = units * flops_per_unit / (ms * 1e-3) / 1e12
+        rows.append({"kernel": name, "ms": round(ms, 4), "units": units, "unit": unit,
+                     "units_per_s": units / (ms * 1e-3), "achieved_tflops": round(achieved, 3),
+                     "fp32_peak_tflops_nominal": round(fp32_peak, 1),
+                     "frac_fp32": round(achieved / fp32_peak, 4)})  # fmt: skip
+
+    it, wu = args.steps, args.warmup
+    ms = _event_time(lambda: kernel.render(config, positions, centers, normals, weights, 0.0), it, wu, flush)
+    record("dsg_surfel_render", ms, A * S * K, 16)
+    ms = _event_time(lambda: kernel.jvp(config, positions, centers, normals, weights, dc, dn, dw, 0.0), it, wu, flush)
+    record("dsg_surfel_jvp", ms, A * S * K, 24)
+    ms = _event_time(lambda: kernel.vjp(config, positions, centers, normals, weights, upstream, 0.0), it, wu, flush)
+    record("dsg_surfel_vjp", ms, A * S * K, 20)
+    sub = positions[: min(A, 768)].contiguous()
+    cand = centers.repeat(max(1, 8192 // S), 1)[:8192].contiguous()
+    cand_n = normals.repeat(max(1, 8192 // S), 1)[:8192].contiguous()
+    ms = _event_time(lambda: kernel.correlate(config, sub, cand, cand_n, upstream[: len(sub)], 0.0), it, wu, flush)
+    record("dsg_surfel_correlate", ms, len(sub) * len(cand) * K, 18)
+    ms = _event_time(lambda: kernel.correlate_gradient(config, sub, cand[:1024], cand_n[:1024], upstream[: len(sub)],
+                                                       0.0, True), it, wu, flush)  # fmt: skip
+    record("dsg_surfel_correlate_gradient", ms, len(sub) * 1024 * K, 30)
+    bank = fibonacci_sphere(24, device)
+    grid = centers.repeat(max(1, 200000 // S), 1)[:200000].contiguous() if not small else centers
+    grid_n = normals.repeat(max(1, 200000 // S), 1)[: len(grid)].contiguous() if not small else normals
+    prop = positions[: min(A, 384)].contiguous()
+    from dsplat import FMCWModel, Scan
+
+    table = FMCWModel(Scan(upstream[: len(prop)], prop, config)).range_table(upstream[: len(prop)], 8)
+    ms = _event_time(lambda: kernel.correlate_orientations(config, prop, grid, grid_n, bank, upstream[: len(prop)],
+                                                           0.0, table), it, wu, flush)  # fmt: skip
+    record("dsg_surfel_correlate_orientations", ms, len(prop) * len(grid) * 25, 12, "pair-normals")
+    block = positions[: min(A, 125)].contiguous()
+    ms = _event_time(lambda: kernel.design(config, block, centers, normals, params["areas"], 0.0, True), it, wu, flush)
+    record("dsg_surfel_design", ms, len(block) * S * K, 10)
+    rows_r = 100_000 if small else 400_000
+    data = torch.randn(rows_r, S, generator=generator).to(device)
+    store = GramRows(S, rows_r, device)
+    store.append(data)
+    total = torch.zeros((S, S), dtype=torch.float64, device=device)
+    ms = _event_time(lambda: store.accumulate(total), it, wu, flush)
+    logical = rows_r * S * (S + 1)
+    achieved = logical / (ms * 1e-3) / 1e12
+    tensor_peak = peaks["bf16_tflops"] / 3
+    rows.append({"kernel": "dsg_gram_bf16x3", "ms": round(ms, 4), "units": logical, "unit": "logical FP32 flops",
+                 "achieved_tflops": round(achieved, 2), "tensor_peak_tflops": round(tensor_peak, 1),
+                 "frac_tensor": round(achieved / tensor_peak, 4),
+                 "peak_source": f"{source} bf16_tflops (burst) / 3"})  # fmt: skip
+    print(json.dumps({"case": args.case, "apertures": A, "surfels": S, "bins": K, "kernels": rows}), flush=True)
+
+
 def main():
     parser = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     parser.add_argument("--gpus", type=int, default=1)
@@ -348,7 +451,12 @@ def main():
     parser.add_argument("--mode", choices=["mixed", "plain"], default="mixed")
     parser.add_argument("--cpu-threads", type=int, default=None)
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead")
+    parser.add_argument("--case", choices=["small", "full"], default="full")
     args = parser.parse_args()
+    if args.kernels:
+        run_kernels(args)
+        return
     world, rank, local = _distributed()
     if args.impl == "reference":
         result = run_reference(args, world, rank)

@@ -238,7 +238,6 @@ def pooled_statistics(state, pool, config):
 
 def _pooled_cross_mixed(model, pool, target, count, added, chunk, config):
     """cross [total, added] = A^T A[:, count:] and right = A[:, count:]^T y on the tensor cores."""
-    from .kernels.gemm import emulated
     from .kernels.gram import GramRows, check
     from .varpro import projected_rows
 
@@ -246,10 +245,9 @@ def _pooled_cross_mixed(model, pool, target, count, added, chunk, config):
     device = target.device
     store = GramRows(total, projected_rows(model, chunk), device)
     right = torch.zeros(added, dtype=torch.float64, device=device)
-    with emulated():
-        for a, y in model.blocks(pool, target, True, chunk):
-            store.append(a)
-            right += a[:, count:].T @ y
+    for a, y in model.blocks(pool, target, True, chunk):
+        store.append(a)
+        right += a[:, count:].T @ y
     products = torch.zeros((total, total), dtype=torch.float64, device=device)
     check(store.accumulate(products, column_from=count))
     cross = torch.empty((total, added), dtype=torch.float64, device=device)

@@ -127,14 +127,12 @@ def normal_equations(model, params, target, config):
     total = torch.zeros((count, count), dtype=torch.float64, device=device)
     rhs = torch.zeros(count, dtype=torch.float64, device=device)
     if _gram_mode(config) == "bf16x3":
-        from .kernels.gemm import emulated
         from .kernels.gram import GramRows, check
 
         store = GramRows(count, projected_rows(model, chunk), device)
-        with emulated():
-            for a, y in stream:
-                store.append(a)
-                rhs += a.T @ y
+        for a, y in stream:
+            store.append(a)
+            rhs += a.T @ y
         check(store.accumulate(total))
     else:
         part = torch.zeros((count, count), dtype=torch.float32, device=device)
