@@ -175,14 +175,27 @@ def search_certificate(
     eye = torch.eye(dim, device=reference.device).expand(count, dim, dim)
     inverse = eye.clone()
     fractions = [0.5**backtrack for backtrack in range(config.backtracks)]
-    for _ in range(config.iterations):
-        direction = search.direction(inverse, grad, params["normals"], controls[1],
-                                     config.trust_radius)  # fmt: skip
-        old = {key: value.clone() for key, value in params.items()}
-        if batched:
-            params, accepted = _backtrack_batched(old, direction, controls, fractions, value, specs,
-                                                  score)  # fmt: skip
-        else:
+
+    def iterate(params, value, grad, inverse):
+        """One batched ascent iteration; returns the new (params, value, grad, inverse)."""
+        direction = search.direction(inverse, grad, params["normals"], controls[1], config.trust_radius)
+        old = {key: v.clone() for key, v in params.items()}
+        params, accepted = _backtrack_batched(old, direction, controls, fractions, value, specs, score)
+        new_value, new_grad = score(params, True)
+        new_grad = ascent(params, new_grad)
+        inverse = _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye)
+        return params, new_value, new_grad, inverse
+
+    if batched and config.iterations > 1 and reference.is_cuda:
+        params, value, grad, inverse = _graphed_ascent(iterate, config.iterations, params, value, grad, inverse)
+    else:
+        for _ in range(config.iterations):
+            if batched:
+                params, value, grad, inverse = iterate(params, value, grad, inverse)
+                continue
+            direction = search.direction(inverse, grad, params["normals"], controls[1],
+                                         config.trust_radius)  # fmt: skip
+            old = {key: v.clone() for key, v in params.items()}
             accepted = torch.zeros(count, dtype=torch.bool, device=reference.device)
             for fraction in fractions:
                 centers, normals = search.trial(old["centers"], old["normals"], direction, controls,
@@ -199,18 +212,10 @@ def search_certificate(
                     break
             if not accepted.any():
                 break
-        new_value, new_grad = score(params, True)
-        new_grad = ascent(params, new_grad)
-        # Damped BFGS update of each candidate's inverse Hessian.
-        step = torch.cat([(params[k] - old[k]) / spec.scale for k, spec in specs.items()], -1)
-        change = new_grad - grad
-        sy = (step * change).sum(-1)
-        valid = accepted & (sy > 1e-8 * step.norm(dim=-1) * change.norm(dim=-1)) & (sy > 1e-20)
-        rho = torch.where(valid, 1 / sy.clamp(min=1e-30), 0)
-        left = eye - rho[:, None, None] * step[:, :, None] * change[:, None, :]
-        updated = left @ inverse @ left.transpose(-1, -2) + rho[:, None, None] * step[:, :, None] * step[:, None, :]
-        inverse = torch.where(valid[:, None, None], updated, inverse)
-        value, grad = new_value, new_grad
+            new_value, new_grad = score(params, True)
+            new_grad = ascent(params, new_grad)
+            inverse = _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye)
+            value, grad = new_value, new_grad
     combined = {key: torch.cat((coarse[key], params[key])) for key in params}
     if full_model is None:
         scores = torch.cat((coarse_scores[ids], value))
@@ -218,6 +223,56 @@ def search_certificate(
         scores = certificate(full_model, combined, full_residual, mode)
     order = scores.argsort(descending=True, stable=True)
     return {key: v[order] for key, v in combined.items()}, scores[order]
+
+
+def _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye):
+    """Damped BFGS update of each candidate's inverse Hessian (skipped where invalid)."""
+    step = torch.cat([(params[k] - old[k]) / spec.scale for k, spec in specs.items()], -1)
+    change = new_grad - grad
+    sy = (step * change).sum(-1)
+    valid = accepted & (sy > 1e-8 * step.norm(dim=-1) * change.norm(dim=-1)) & (sy > 1e-20)
+    rho = torch.where(valid, 1 / sy.clamp(min=1e-30), 0)
+    left = eye - rho[:, None, None] * step[:, :, None] * change[:, None, :]
+    updated = left @ inverse @ left.transpose(-1, -2) + rho[:, None, None] * step[:, :, None] * step[:, None, :]
+    return torch.where(valid[:, None, None], updated, inverse)
+
+
+def _graphed_ascent(iterate, iterations, params, value, grad, inverse):
+    """Run the batched ascent: one eager iteration, then the rest replayed from a CUDA graph.
+
+    The iteration reads and writes only device tensors of fixed shapes, so the graph
+    captured from the second iteration replays every later one; the eager first
+    iteration doubles as the warm-up that capture needs.
+    """
+    from .kernels import _lib
+
+    device = value.device
+    side = torch.cuda.Stream(device)
+    side.wait_stream(torch.cuda.current_stream(device))
+    timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be timed inside a graph
+    try:
+        with torch.cuda.stream(side):
+            state = iterate(params, value, grad, inverse)
+            static = ({k: v.clone() for k, v in state[0].items()}, state[1].clone(), state[2].clone(),
+                      state[3].clone())  # fmt: skip
+        torch.cuda.current_stream(device).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        before = _lib.library().dsg_launch_count()
+        with torch.cuda.graph(graph):
+            out = iterate(*static)
+            for key, v in out[0].items():
+                static[0][key].copy_(v)
+            static[1].copy_(out[1])
+            static[2].copy_(out[2])
+            static[3].copy_(out[3])
+        per_replay = _lib.library().dsg_launch_count() - before
+        for _ in range(iterations - 1):
+            graph.replay()
+        _lib.REPLAYED_LAUNCHES += per_replay * (iterations - 1)
+    finally:
+        _lib.TIMERS = timers
+    return ({k: v.clone() for k, v in static[0].items()}, static[1].clone(), static[2].clone(),
+            static[3].clone())  # fmt: skip
 
 
 def _backtrack_batched(old, direction, controls, fractions, value, specs, score):

@@ -122,6 +122,9 @@ def library() -> ctypes.CDLL:
 # Optional per-entry-point timing: name -> list of (start, end) CUDA events. Set to a
 # dict to record; None (the default) records nothing.
 TIMERS: dict | None = None
+# Kernel launches replayed from CUDA graphs (the library's own counter sees a captured
+# launch once, at capture time).
+REPLAYED_LAUNCHES = 0
 # Optional algorithmic work per entry point (flops or bytes, as each caller defines),
 # accumulated while TIMERS is recording.
 WORK: dict = {}
