@@ -14,6 +14,9 @@ import torch
 import torch.nn.functional as F
 
 
+_MASKS: dict = {}
+
+
 @dataclass(frozen=True)
 class ParameterConfig:
     trainable: bool | tuple[bool, ...] = True  # one flag, or one per component
@@ -24,10 +27,18 @@ class ParameterConfig:
     normalize: bool = False  # unit vectors (surfel normals)
 
     def mask(self, value):
-        """Boolean mask of the free components of one row of value."""
-        flags = torch.as_tensor(self.trainable, dtype=torch.bool, device=value.device)
+        """Boolean mask of the free components of one row of value.
+
+        Masks are cached per device and width, so that a loop captured in a CUDA graph
+        never copies the flags from the host.
+        """
         width = value.shape[1] if value.ndim == 2 else 1
-        return flags.expand(width)
+        key = (self.trainable, value.device, width)
+        flags = _MASKS.get(key)
+        if flags is None:
+            flags = torch.as_tensor(self.trainable, dtype=torch.bool, device=value.device).expand(width)
+            _MASKS[key] = flags
+        return flags
 
     def project(self, proposed, reference):
         """Closest feasible values to proposed; frozen components are taken from reference."""
