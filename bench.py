@@ -358,7 +358,8 @@ def _event_time(fn, iterations, warmup, flush):
 def run_kernels(args):
     """Per-kernel roofline table on the sphere-cap geometry (the workload of the DSFW bench).
 
-    full: 128^2 apertures x 2000 surfels (C3 sizes); small: 32^2 apertures x 256 surfels.
+    full: 128^2 apertures x 2000 surfels (C3 sizes); medium: 64^2 x 1000 (inputs above
+    L2, a few hundred MB on the device: the size of the ncu captures); small: 32^2 x 256.
     Work units: pair-bins (aperture x surfel x bin) with the FP32 flop counts per
     pair-bin 16 (forward), 24 (JVP), 20 (VJP), 18 (correlation); the Gram as logical
     FP32 flops R S (S + 1).
@@ -366,7 +367,7 @@ def run_kernels(args):
     import __graft_entry__
 
     __graft_entry__.build()
-    from dsplat import FMCWConfig
+    from dsplat import FMCWConfig, FMCWModel, Scan
     from dsplat.certificate import fibonacci_sphere
     from dsplat.kernels import surfel as kernel
     from dsplat.kernels.gram import GramRows
@@ -376,9 +377,9 @@ def run_kernels(args):
     torch.cuda.set_device(device)
     peaks, source = _peaks()
     small = args.case == "small"
+    side, surfel_count = {"small": (32, 256), "medium": (64, 1000), "full": (128, 2000)}[args.case]
     config = FMCWConfig()
-    positions, params, reflectivity = sphere_cap(side=32 if small else 128, surfel_count=256 if small else 2000,
-                                                 device=device)  # fmt: skip
+    positions, params, reflectivity = sphere_cap(side=side, surfel_count=surfel_count, device=device)
     centers, normals = params["centers"], params["normals"]
     A, S, K = len(positions), len(centers), config.num_range_bins
     generator = torch.Generator().manual_seed(0)
@@ -414,11 +415,10 @@ def run_kernels(args):
                                                        0.0, True), it, wu, flush)  # fmt: skip
     record("dsg_surfel_correlate_gradient", ms, len(sub) * 1024 * K, 30)
     bank = fibonacci_sphere(24, device)
-    grid = centers.repeat(max(1, 200000 // S), 1)[:200000].contiguous() if not small else centers
-    grid_n = normals.repeat(max(1, 200000 // S), 1)[: len(grid)].contiguous() if not small else normals
+    ncand = 200000 if args.case == "full" else 50000
+    grid = centers.repeat(ncand // S + 1, 1)[:ncand].contiguous()
+    grid_n = normals.repeat(ncand // S + 1, 1)[:ncand].contiguous()
     prop = positions[: min(A, 384)].contiguous()
-    from dsplat import FMCWModel, Scan
-
     table = FMCWModel(Scan(upstream[: len(prop)], prop, config)).range_table(upstream[: len(prop)], 8)
     ms = _event_time(lambda: kernel.correlate_orientations(config, prop, grid, grid_n, bank, upstream[: len(prop)],
                                                            0.0, table), it, wu, flush)  # fmt: skip
@@ -426,7 +426,18 @@ def run_kernels(args):
     block = positions[: min(A, 125)].contiguous()
     ms = _event_time(lambda: kernel.design(config, block, centers, normals, params["areas"], 0.0, True), it, wu, flush)
     record("dsg_surfel_design", ms, len(block) * S * K, 10)
-    rows_r = 100_000 if small else 400_000
+    from dsplat import DSFWConfig, ParameterConfig
+    from dsplat.varpro import normal_equations
+    from dsplat.workloads import box_of
+
+    low, high = box_of(centers)
+    model = FMCWModel(Scan(upstream, positions, config)).prepare({"centers": ParameterConfig(lower=low, upper=high)})
+    mixed = DSFWConfig(gram="bf16x3")
+    ms = _event_time(lambda: normal_equations(model, params, upstream, mixed), it, wu, flush)
+    rows.append({"kernel": "normal_equations (fused projection + tcgen05 Gram)", "ms": round(ms, 3)})
+    ms = _event_time(lambda: normal_equations(model, params, upstream, DSFWConfig()), it, wu, flush)
+    rows.append({"kernel": "normal_equations (FP32 design + projection + SSYRK)", "ms": round(ms, 3)})
+    rows_r = {"small": 100_000, "medium": 200_000, "full": 400_000}[args.case]
     data = torch.randn(rows_r, S, generator=generator).to(device)
     store = GramRows(S, rows_r, device)
     store.append(data)
@@ -452,7 +463,7 @@ def main():
     parser.add_argument("--cpu-threads", type=int, default=None)
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead")
-    parser.add_argument("--case", choices=["small", "full"], default="full")
+    parser.add_argument("--case", choices=["small", "medium", "full"], default="full")
     args = parser.parse_args()
     if args.kernels:
         run_kernels(args)

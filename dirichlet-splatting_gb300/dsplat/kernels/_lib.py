@@ -93,6 +93,10 @@ SIGNATURES = {
     "dsg_range_response": (ctypes.c_int, [F64, F64, I32, I32, I32, I32, P, P]),
     "dsg_syrk_f32": (ctypes.c_int, [P, I64, I32, P, P]),
     "dsg_gemm_f32_bf16x9": (ctypes.c_int, [I32, I32, I32, P, I32, P, I32, F32, P, I32, P]),
+    "dsg_design_project_bf16x3": (
+        ctypes.c_int,
+        [CP, P, I32, P, P, P, I32, P, P, I32, P, P, I64, I64, P, P],
+    ),
     "dsg_split_transpose_bf16": (ctypes.c_int, [P, I64, I32, I64, P, P, I64, P]),
     "dsg_gram_bf16x3": (ctypes.c_int, [P, P, I32, I32, I64, I32, I32, P, I32, P, P]),
 }

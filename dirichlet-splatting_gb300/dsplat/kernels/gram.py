@@ -97,6 +97,51 @@ class GramRows:
         return status
 
 
+_SPLIT_BASES: dict = {}
+
+
+def split_basis(interleaved):
+    """bf16 hi/lo [128, 2K] of an interleaved row basis [2 rank, 2K] (rows past 2 rank zero)."""
+    key = (interleaved.data_ptr(), tuple(interleaved.shape), interleaved.device)
+    entry = _SPLIT_BASES.get(key)
+    if entry is None:
+        rank2, width = interleaved.shape
+        padded = torch.zeros((128, width), dtype=torch.float32, device=interleaved.device)
+        padded[:rank2] = interleaved
+        hi = padded.to(torch.bfloat16)
+        lo = (padded - hi.float()).to(torch.bfloat16)
+        entry = (hi.contiguous(), lo.contiguous(), interleaved)  # keep the source alive
+        _SPLIT_BASES[key] = entry
+    return entry[0], entry[1]
+
+
+def fused_supported(config, basis):
+    """Whether dsg_design_project_bf16x3 covers this chirp and basis."""
+    return (basis is not None and basis.interleaved.shape[0] <= 128
+            and config.num_range_bins in (32, 64, 128) and config.pad_factor in (1, 2, 4))  # fmt: skip
+
+
+def append_projected(store, config, positions, params, basis, fresnel_n, status):
+    """Store the basis-projected real dictionary rows of apertures `positions` (fused kernel)."""
+    from . import _lib as lib
+
+    hi, lo = split_basis(basis.interleaved)
+    rank2 = basis.interleaved.shape[0]
+    count = len(positions) * rank2
+    if store.rows + count > store.k_pad:
+        raise DsplatKernelError("GramRows capacity exceeded")
+    positions = positions.to(torch.float32).contiguous()
+    centers = params["centers"].to(torch.float32).contiguous()
+    normals = params["normals"].to(torch.float32).contiguous()
+    areas = params["areas"].to(torch.float32).contiguous()
+    call(
+        "dsg_design_project_bf16x3", lib.chirp(config, fresnel_n), ptr(positions), len(positions),
+        ptr(centers), ptr(normals), ptr(areas), len(centers), ptr(hi), ptr(lo), rank2, ptr(store.hi),
+        ptr(store.lo), store.k_pad, store.rows, ptr(status), lib.stream(positions.device),
+    )  # fmt: skip
+    store.rows += count
+
+
 def check(status):
     """Raise if the Gram kernel reported a bounded wait that ran out (reads one int)."""
     if int(status.item()) != 0:

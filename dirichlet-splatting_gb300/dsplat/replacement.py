@@ -239,15 +239,21 @@ def pooled_statistics(state, pool, config):
 def _pooled_cross_mixed(model, pool, target, count, added, chunk, config):
     """cross [total, added] = A^T A[:, count:] and right = A[:, count:]^T y on the tensor cores."""
     from .kernels.gram import GramRows, check
-    from .varpro import projected_rows
+    from .varpro import fused_rows, projected_rows
 
     total = count + added
     device = target.device
     store = GramRows(total, projected_rows(model, chunk), device)
-    right = torch.zeros(added, dtype=torch.float64, device=device)
-    for a, y in model.blocks(pool, target, True, chunk):
-        store.append(a)
-        right += a[:, count:].T @ y
+    fused = fused_rows(model, pool, store, chunk)
+    if fused is not None:
+        new = {key: value[count:] for key, value in pool.items()}
+        right = model.correlate(new, target)[0].real.double()
+        check(fused)
+    else:
+        right = torch.zeros(added, dtype=torch.float64, device=device)
+        for a, y in model.blocks(pool, target, True, chunk):
+            store.append(a)
+            right += a[:, count:].T @ y
     products = torch.zeros((total, total), dtype=torch.float64, device=device)
     check(store.accumulate(products, column_from=count))
     cross = torch.empty((total, added), dtype=torch.float64, device=device)

@@ -106,6 +106,35 @@ def projected_rows(model, chunk):
     return 2 * model.size
 
 
+def fused_rows(model, params, store, chunk):
+    """Store every projected real row block with the fused design-projection kernel.
+
+    Returns the kernel status tensor, or None (nothing stored) when the model or any
+    block's basis is outside what the fused kernel covers; the caller then streams.
+    """
+    from .kernels.gram import append_projected, fused_supported
+
+    if not hasattr(model, "block_basis"):
+        return None
+    config, positions = model.sensor
+    bins = model.shape[1]
+    runs = []  # consecutive blocks sharing one basis: (first aperture, last aperture, basis)
+    for start in range(0, model.size, chunk):
+        rows = slice(start, min(start + chunk, model.size))
+        basis = model.block_basis(rows)
+        if not fused_supported(config, basis):
+            return None
+        first, last = rows.start // bins, rows.stop // bins
+        if runs and runs[-1][2] is basis and runs[-1][1] == first:
+            runs[-1] = (runs[-1][0], last, basis)
+        else:
+            runs.append((first, last, basis))
+    status = torch.zeros(1, dtype=torch.int32, device=positions.device)
+    for first, last, basis in runs:
+        append_projected(store, config, positions[first:last], params, basis, model.fresnel_n, status)
+    return status
+
+
 def normal_equations(model, params, target, config):
     """G = A^H A / M and q = A^H y / M, streamed over projected row blocks.
 
@@ -130,9 +159,14 @@ def normal_equations(model, params, target, config):
         from .kernels.gram import GramRows, check
 
         store = GramRows(count, projected_rows(model, chunk), device)
-        for a, y in stream:
-            store.append(a)
-            rhs += a.T @ y
+        fused = fused_rows(model, params, store, chunk)
+        if fused is not None:
+            rhs += model.correlate(params, target)[0].real.double()
+            check(fused)
+        else:
+            for a, y in stream:
+                store.append(a)
+                rhs += a.T @ y
         check(store.accumulate(total))
     else:
         part = torch.zeros((count, count), dtype=torch.float32, device=device)

@@ -221,6 +221,20 @@ int dsg_syrk_f32(const float* rows, int64_t m, int32_t n, float* out, void* stre
 int dsg_gemm_f32_bf16x9(int32_t m, int32_t n, int32_t k, const float* a, int32_t lda, const float* b,
                         int32_t ldb, float beta, float* c, int32_t ldc, void* stream);
 
+/* Mixed precision, fused: evaluate the real dictionary rows of every (aperture, surfel)
+ * pair of the block (as dsg_surfel_design with real != 0) on chip, project them with the
+ * block's interleaved row basis U [rank2, 2K] given as bf16 hi/lo [128, 2K] (rows >= rank2
+ * zero) on the tcgen05 tensor cores (split-BF16x3), and store the projected rows split
+ * and transposed: pt_hi/pt_lo[s * ld + column_offset + a * rank2 + rho]. pt must have at
+ * least ceil(surfels / 32) * 32 rows. num_bins <= 128, pad in {1, 2, 4}. status as for
+ * dsg_gram_bf16x3. Replaces dsplat/kernels/surfel.py:199-220 (design) followed by
+ * dsplat/fmcw.py:128-131 (RowBasis.reduce_major) on the mixed path. */
+int dsg_design_project_bf16x3(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                              const float* centers, const float* normals, const float* areas,
+                              int32_t surfels, const void* basis_hi, const void* basis_lo,
+                              int32_t rank2, void* pt_hi, void* pt_lo, int64_t ld,
+                              int64_t column_offset, int32_t* status, void* stream);
+
 /* Mixed precision: split FP32 rows [m, n] into bf16 hi + lo and store them transposed,
  * hi[s * ld + column_offset + r] = bf16(rows[r, s]) and lo the bf16 of the remainder.
  * Feeds dsg_gram_bf16x3 (replaces the FP32 operand of the reference's SYRK,

@@ -77,3 +77,24 @@ def test_emulated_projection_is_fp32_accurate():
         fast = project(matrix, rows)
     exact = matrix.double() @ rows.double()
     assert float((fast.double() - exact).abs().max() / exact.abs().max()) < 1e-5
+
+
+@pytest.mark.parametrize("pad", [2, 4])
+def test_fused_design_projection_gram_matches_the_fp32_stream(pad):
+    """Normal equations from on-chip dictionary rows (tcgen05 projection + Gram) vs the FP32 path."""
+    from dsplat import DSFWConfig, FMCWConfig, FMCWModel, ParameterConfig, Scan
+    from dsplat.varpro import normal_equations
+    from dsplat.workloads import box_of, sphere_cap
+
+    config = FMCWConfig(pad_factor=pad) if pad == 2 else FMCWConfig(pad_factor=pad, adc_samples=64)
+    positions, params, reflectivity = sphere_cap(surfel_count=300, side=24, device="cuda")
+    data = FMCWModel(Scan(torch.zeros((len(positions), config.num_range_bins), dtype=torch.complex64,
+                                      device="cuda"), positions, config)).render(params, reflectivity)
+    low, high = box_of(params["centers"])
+    specs = {"centers": ParameterConfig(lower=low, upper=high)}
+    model = FMCWModel(Scan(data, positions, config)).prepare(specs)
+    plain = normal_equations(model, params, data, DSFWConfig(row_chunk=8 * config.num_range_bins))
+    mixed = normal_equations(model, params, data, DSFWConfig(row_chunk=8 * config.num_range_bins, gram="bf16x3"))
+    scale = float(plain[0].abs().max())
+    assert float((mixed[0] - plain[0]).abs().max()) < 1e-4 * scale
+    assert float((mixed[1] - plain[1]).abs().max()) < 1e-4 * float(plain[1].abs().max())
