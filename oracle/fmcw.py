@@ -67,6 +67,7 @@ def render(config, positions, centers, normals, weights, fresnel_n=0.0, chunk=64
     return torch.cat(parts)
 
 
+@torch.enable_grad()
 def vjp(config, positions, centers, normals, weights, upstream, fresnel_n=0.0, chunk=64):
     """Gradients of Re(conj(upstream) . render) for centers, normals and complex weights.
 
@@ -128,6 +129,7 @@ def correlate(config, positions, centers, normals, residual, fresnel_n=0.0, chun
     return corr, norm
 
 
+@torch.enable_grad()
 def correlate_gradient(config, positions, centers, normals, residual, fresnel_n=0.0,
                        include_normals=False, chunk=64):  # fmt: skip
     """corr, norm and their derivatives by centers (and normals), [C, 3 or 6], float64 autograd."""

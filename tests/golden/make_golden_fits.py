@@ -1,0 +1,213 @@
+"""Run the reference's own DSFW solver on small scenes and record its objective histories.
+
+Run here, where the reference checkout exists:
+
+    python tests/golden/make_golden_fits.py [/path/to/Dirichlet-Splatting]
+
+The reference's Python solver (dsplat/dsfw.py, varpro.py, replacement.py,
+refinement.py, certificate.py, parameters.py, fmcw.py, spectral.py) runs unmodified;
+only its kernel-binding modules (dsplat/kernels/*.py, which launch Slang through
+slangtorch and need a GPU) are replaced, before import, by float64 CPU restatements
+from this repository's oracle/. The histories go to tests/golden/reference_fits.json;
+tests/test_fits_gpu.py runs the same scenes through the GB300 package and compares.
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+import types
+from pathlib import Path
+
+import torch
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+DEFAULT_REFERENCE = Path("/root/reference")
+
+
+def _shim_modules():
+    """Kernel-binding modules with the reference's signatures, computed by the oracle."""
+    sys.path.insert(0, str(REPO))
+    from oracle import fmcw as ofmcw
+    from oracle import search as osearch
+    from oracle import spectral as ospectral
+
+    c64, f32 = torch.complex64, torch.float32
+
+    surfel = types.ModuleType("dsplat.kernels.surfel")
+
+    def render(config, positions, centers, normals, weights, fresnel_n):
+        return ofmcw.render(config, positions, centers.detach(), normals.detach(), weights.detach(),
+                            fresnel_n).to(c64)  # fmt: skip
+
+    def jvp(config, positions, centers, normals, weights, dc, dn, dw, fresnel_n):
+        return ofmcw.jvp(config, positions, centers, normals, weights, dc, dn, dw, fresnel_n).to(c64)
+
+    def vjp(config, positions, centers, normals, weights, upstream, fresnel_n):
+        gc, gn, gw = ofmcw.vjp(config, positions, centers, normals, weights, upstream, fresnel_n)
+        return gc.to(f32), gn.to(f32), gw.to(c64)
+
+    def design(config, positions, centers, normals, areas, fresnel_n, real):
+        out = ofmcw.design(config, positions, centers, normals, areas, fresnel_n, real)
+        return out.to(f32) if real else out.to(c64)
+
+    def jacobian(config, positions, centers, normals, fresnel_n):
+        pos, cen, nrm = positions.double(), centers.double(), normals.double()
+        cols = ofmcw.columns(pos, cen, nrm, config, fresnel_n)
+        parts = []
+        for key in ("centers", "normals"):
+            for axis in range(3):
+                tc, tn = torch.zeros_like(cen), torch.zeros_like(nrm)
+                (tc if key == "centers" else tn)[:, axis] = 1.0
+                _, d = torch.func.jvp(lambda c, n: ofmcw.columns(pos, c, n, config, fresnel_n), (cen, nrm),
+                                      (tc, tn))  # fmt: skip
+                parts.append(d)
+        jac = torch.stack(parts, -1).to(c64)
+        return cols.to(c64), jac[..., :3], jac[..., 3:]
+
+    def correlate(config, positions, centers, normals, residual, fresnel_n):
+        corr, norm = ofmcw.correlate(config, positions, centers, normals, residual, fresnel_n)
+        return corr.to(c64), norm.to(f32)
+
+    def correlate_gradient(config, positions, centers, normals, residual, fresnel_n, include_normals):
+        out = ofmcw.correlate_gradient(config, positions, centers, normals, residual, fresnel_n, include_normals)
+        return out[0].to(c64), out[1].to(f32), out[2].to(c64), out[3].to(f32)
+
+    def correlate_orientations(config, positions, centers, normals, bank, residual, fresnel_n, table=None):
+        tab = None if table is None else (table.correlation, table.norm, table.oversample)
+        corr, norm = ofmcw.correlate_orientations(config, positions, centers, normals, bank, residual,
+                                                  fresnel_n, tab)  # fmt: skip
+        return corr.to(c64), norm.to(f32)
+
+    for fn in (render, jvp, vjp, design, jacobian, correlate, correlate_gradient, correlate_orientations):
+        setattr(surfel, fn.__name__, fn)
+
+    spectral = types.ModuleType("dsplat.kernels.spectral")
+    spectral.design = lambda grid, centers, bins, derivatives=False: (
+        tuple(x.to(c64) for x in ospectral.design(grid, centers, bins)) if derivatives
+        else ospectral.design(grid, centers, bins)[0].to(c64))  # fmt: skip
+    spectral.render = lambda grid, centers, coefficients, bins: ospectral.render(grid, centers, coefficients,
+                                                                                 bins).to(c64)  # fmt: skip
+    spectral.jvp = lambda grid, centers, b, dc, db, bins: ospectral.jvp(grid, centers, b, dc, db, bins).to(c64)
+
+    def spectral_vjp(grid, centers, coefficients, upstream, bins):
+        gc, gb = ospectral.vjp(grid, centers, coefficients, upstream, bins)
+        return gc.to(f32), gb.to(c64)
+
+    spectral.vjp = spectral_vjp
+
+    search = types.ModuleType("dsplat.kernels.search")
+    search.range_gate = osearch.range_gate
+    search.peaks = lambda scores, centers, count, separation: osearch.peaks(scores, centers, count, separation)
+    search.direction = lambda inverse, gradient, normals, mask, radius: osearch.direction(
+        inverse, gradient, normals, mask, radius).to(f32)
+    search.trial = lambda centers, normals, direction, controls, fraction: tuple(
+        x.to(f32) for x in osearch.trial(centers, normals, direction, controls, fraction))
+
+    reduce = types.ModuleType("dsplat.kernels.reduce")
+    reduce.energy = lambda value, reference: osearch.energy(value, reference)
+
+    response = types.ModuleType("dsplat.kernels.response")
+    response.range_response = lambda config, low, high, count, device: ofmcw.range_response(config, low, high,
+                                                                                           count)  # fmt: skip
+
+    cublas = types.ModuleType("dsplat.kernels.cublas")
+
+    def syrk(rows, out):
+        out += torch.triu(rows.double().T @ rows.double()).to(out.dtype)
+
+    cublas.syrk = syrk
+    return {"surfel": surfel, "spectral": spectral, "search": search, "reduce": reduce,
+            "response": response, "cublas": cublas}  # fmt: skip
+
+
+def import_reference(root: Path):
+    sys.modules.setdefault("slangtorch", types.ModuleType("slangtorch"))
+    # The shims must be in place before the reference package imports its bindings.
+    for name, module in _shim_modules().items():
+        sys.modules[f"dsplat.kernels.{name}"] = module
+    sys.path.insert(0, str(root))
+    import dsplat  # noqa: E402
+    import dsplat.surfel  # noqa: E402
+    import dsplat.varpro  # noqa: E402
+
+    assert dsplat.__file__.startswith(str(root))
+    assert dsplat.surfel.kernel is sys.modules["dsplat.kernels.surfel"]
+    assert dsplat.varpro.syrk is sys.modules["dsplat.kernels.cublas"].syrk
+
+    return dsplat
+
+
+def aperture_grid(side=8, pitch=0.004):
+    t = (torch.arange(side, dtype=torch.float32) - (side - 1) / 2) * pitch
+    x, y = torch.meshgrid(t, t, indexing="ij")
+    return torch.stack([x.flatten(), y.flatten(), torch.zeros(side * side)], -1)
+
+
+def surfels(count, seed=0, spread=0.01):
+    generator = torch.Generator().manual_seed(seed)
+    centers = torch.tensor([0, 0, 0.3]) + spread * (2 * torch.rand(count, 3, generator=generator) - 1)
+    direction = torch.tensor([0.0, 0, -1]) + 0.3 * torch.randn(count, 3, generator=generator)
+    normals = torch.nn.functional.normalize(direction, dim=1)
+    return dict(centers=centers, normals=normals, areas=torch.full((count,), 1e-4))
+
+
+def fmcw_specs(dsplat):
+    return dict(
+        centers=dsplat.ParameterConfig(scale=0.0005, lower=(-0.02, -0.02, 0.28), upper=(0.02, 0.02, 0.32)),
+        normals=dsplat.ParameterConfig(scale=0.1, normalize=True),
+        areas=dsplat.ParameterConfig(trainable=False),
+    )
+
+
+def main(root: Path) -> None:
+    dsplat = import_reference(root)
+    results = {}
+
+    # FMCW: merged replacement from a displaced start, screened joint Gauss-Newton.
+    config = dsplat.FMCWConfig()
+    positions = aperture_grid()
+    truth = surfels(5)
+    coefficients = torch.linspace(0.5, 1.5, 5)
+    empty = dsplat.Scan(torch.zeros((64, config.num_range_bins), dtype=torch.complex64), positions, config)
+    data = dsplat.FMCWModel(empty).render(truth, coefficients)
+    model = dsplat.FMCWModel(dsplat.Scan(data, positions, config))
+    for name, cfg in {
+        "fmcw_merged_joint": dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=16, screen_apertures=16),
+        "fmcw_merged_dense": dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, lm_solver="dense", lm_rows=2048,
+                                               screen_apertures=0),
+    }.items():  # fmt: skip
+        state = dsplat.initialize(model, data, surfels(5, seed=9), cfg, candidates=truth,
+                                  parameters=fmcw_specs(dsplat))  # fmt: skip
+        for _ in range(4):
+            state = dsplat.step(state, cfg)
+        results[name] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
+                         "centers": state.params["centers"].tolist()}  # fmt: skip
+
+    # Spectral: a misplaced tone recovered by utility replacement and dense LM.
+    grid = dsplat.SpectralGrid((24, 20))
+    smodel = dsplat.SpectralModel(grid)
+    centers = torch.tensor([[3.3, 4.1], [12.0, 15.0], [18.4, 7.9]])
+    b = torch.tensor([1 + 0.5j, -0.7 + 0.2j, 0.4 - 0.9j])
+    target = smodel.render({"centers": centers}, b)
+    wrong = centers.clone()
+    wrong[1] = torch.tensor([20.0, 2.0])
+    cfg = dsplat.DSFWConfig(coefficients="complex", replacement="utility", lm_solver="dense",
+                            lm_rows=grid.size, lm_gain_ratio=0, lm_steps=3)  # fmt: skip
+    specs = {"centers": dsplat.ParameterConfig(period=grid.shape, scale=0.5)}
+    state = dsplat.initialize(smodel, target, {"centers": wrong}, cfg,
+                              candidates={"centers": grid.bins("cpu")}, parameters=specs)  # fmt: skip
+    for _ in range(3):
+        state = dsplat.step(state, cfg)
+    results["spectral_utility_dense"] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
+                                         "centers": state.params["centers"].tolist()}  # fmt: skip
+
+    (HERE / "reference_fits.json").write_text(json.dumps(results, indent=1))
+    print("wrote", HERE / "reference_fits.json")
+    for name, r in results.items():
+        print(name, [round(e["objective"], 12) for e in r["history"]])
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REFERENCE)
