@@ -10,6 +10,8 @@
 // sweeps its pairs' bins reading the geometry by broadcast.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <atomic>
+#include <mutex>
 #include "common.cuh"
 
 namespace dsg {
@@ -1200,3 +1202,72 @@ int dsg_surfel_jacobian(const DsgChirp* chirp, const float* positions, int32_t a
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// VJP without a caller workspace, for callers that cannot allocate device memory: a host
+// whose device memory is owned entirely by another allocator (a framework's caching pool
+// that has reserved the GPU), or a latency-bound pipeline that must not call cudaMalloc
+// because it synchronizes the whole device. The aperture-chunk partials live in one
+// fixed array below, DSG_VJP_SCRATCH_MAX_BYTES long, which every GPU that loads this
+// library holds until the process exits.
+//
+// In host code the array's name is only a stand-in for the symbol; its device address
+// is looked up once per device with cudaGetSymbolAddress, with that device current, on
+// the first call made on that device. That first call may also load this module onto
+// the device, so it should come before any stream capture on that device.
+//
+// Every call on a device shares the one array and leaves its partials there. Nothing in
+// it needs to start at zero: the partial kernel writes every (surfel, chunk) slot that
+// the chunk sum then reads. Calls whose kernels overlap on the GPU (different streams
+// without ordering between them) race on the array and give wrong gradients.
+// ------------------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) float g_vjp_scratch[DSG_VJP_SCRATCH_MAX_BYTES / sizeof(float)];
+
+constexpr int kScratchDevices = 64;
+std::atomic<void*> g_vjp_scratch_address[kScratchDevices];
+std::mutex g_vjp_scratch_mutex;
+
+int vjp_scratch_address(void** out) {
+  int device = -1;
+  if (cudaGetDevice(&device) != cudaSuccess) return DSG_ERR_LAUNCH;
+  if (device < 0 || device >= kScratchDevices) return DSG_ERR_UNSUPPORTED;
+  void* address = g_vjp_scratch_address[device].load(std::memory_order_acquire);
+  if (address == nullptr) {
+    std::lock_guard<std::mutex> lock(g_vjp_scratch_mutex);
+    address = g_vjp_scratch_address[device].load(std::memory_order_acquire);
+    if (address == nullptr) {
+      const cudaError_t e = cudaGetSymbolAddress(&address, g_vjp_scratch);
+      if (e != cudaSuccess || address == nullptr) {
+        cudaGetLastError();
+        return DSG_ERR_LAUNCH;
+      }
+      g_vjp_scratch_address[device].store(address, std::memory_order_release);
+    }
+  }
+  *out = address;
+  return DSG_OK;
+}
+
+}  // namespace
+
+extern "C" int dsg_surfel_vjp_fixed_scratch(const DsgChirp* chirp, const float* positions,
+                                            int32_t apertures, const float* centers,
+                                            const float* normals, const float* weights,
+                                            int32_t surfels, const float* upstream,
+                                            float* grad_centers, float* grad_normals,
+                                            float* grad_weights, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || surfels < 0) return DSG_ERR_ARGUMENT;
+  if (surfels > 0 && (!weights || !grad_weights)) return DSG_ERR_ARGUMENT;
+  const size_t need = dsg_surfel_reduce_workspace_bytes(chirp, apertures, surfels, 8);
+  if (need > DSG_VJP_SCRATCH_MAX_BYTES) return DSG_ERR_WORKSPACE;
+  if (surfels == 0) return DSG_OK;
+  void* scratch = nullptr;
+  const int status = vjp_scratch_address(&scratch);
+  if (status != DSG_OK) return status;
+  return reduce_common(3, chirp, positions, apertures, centers, normals, weights, surfels,
+                       upstream, grad_centers, grad_normals, grad_weights, nullptr, scratch,
+                       DSG_VJP_SCRATCH_MAX_BYTES, stream);
+}

@@ -100,6 +100,27 @@ int dsg_surfel_vjp(const DsgChirp* chirp, const float* positions, int32_t apertu
                    float* grad_normals, float* grad_weights, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* Upper bound of the fixed device scratch of dsg_surfel_vjp_fixed_scratch (4 MiB per GPU). */
+#define DSG_VJP_SCRATCH_MAX_BYTES ((size_t)4 << 20)
+
+/* dsg_surfel_vjp for callers that cannot allocate device memory (their device memory is
+ * owned by another allocator, or cudaMalloc's device-wide synchronization is not
+ * acceptable to them). No counterpart in the reference. Same inputs, outputs and results
+ * as dsg_surfel_vjp, but no workspace argument: the chunk partials go to one fixed
+ * scratch array of DSG_VJP_SCRATCH_MAX_BYTES in the library, held by every GPU that
+ * loads it until the process exits. Returns DSG_ERR_WORKSPACE, without launching, when
+ * dsg_surfel_reduce_workspace_bytes(chirp, apertures, surfels, 8) exceeds that bound
+ * (with the 152-SM grid sizing that is above about 131k surfels). The first call on a
+ * device looks up the scratch address there (and may load the module), so make it
+ * before any stream capture on that device. Calls share the scratch: two calls whose
+ * kernels overlap on the GPU race and give wrong gradients; order them on one stream.
+ * Allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine. */
+int dsg_surfel_vjp_fixed_scratch(const DsgChirp* chirp, const float* positions,
+                                 int32_t apertures, const float* centers, const float* normals,
+                                 const float* weights, int32_t surfels, const float* upstream,
+                                 float* grad_centers, float* grad_normals, float* grad_weights,
+                                 void* stream);
+
 /* conj(column) . residual and |column|^2 per candidate, without area (reference:
  * dsplat/kernels/surfel.py:242-260 correlate). corr [C] complex, norm [C]. */
 int dsg_surfel_correlate(const DsgChirp* chirp, const float* positions, int32_t apertures,
