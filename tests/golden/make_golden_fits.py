@@ -132,6 +132,13 @@ def import_reference(root: Path):
     import dsplat.surfel  # noqa: E402
     import dsplat.varpro  # noqa: E402
 
+    # The reference's grid helpers default to device="cuda"; here the whole solver runs on
+    # the CPU, so only those defaults change (the function bodies stay the reference's).
+    import dsplat.certificate  # noqa: E402
+
+    dsplat.certificate.candidate_grid.__defaults__ = ("cpu",)
+    dsplat.certificate.fibonacci_sphere.__defaults__ = ("cpu",)
+
     assert dsplat.__file__.startswith(str(root))
     assert dsplat.surfel.kernel is sys.modules["dsplat.kernels.surfel"]
     assert dsplat.varpro.syrk is sys.modules["dsplat.kernels.cublas"].syrk
@@ -184,6 +191,35 @@ def main(root: Path) -> None:
             state = dsplat.step(state, cfg)
         results[name] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
                          "centers": state.params["centers"].tolist()}  # fmt: skip
+
+    # FMCW: the pool is the truth displaced by a few tenths of a millimetre, so the fit has
+    # to move every surfel with the joint Gauss-Newton step.
+    generator = torch.Generator().manual_seed(21)
+    nearby = {"centers": truth["centers"] + 3e-4 * torch.randn(5, 3, generator=generator),
+              "normals": torch.nn.functional.normalize(truth["normals"] + 0.05 * torch.randn(5, 3, generator=generator),
+                                                       dim=1),
+              "areas": truth["areas"].clone()}  # fmt: skip
+    cfg = dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0, lm_steps=2)
+    state = dsplat.initialize(model, data, surfels(5, seed=9), cfg, candidates=nearby,
+                              parameters=fmcw_specs(dsplat))  # fmt: skip
+    for _ in range(6):
+        state = dsplat.step(state, cfg)
+    results["fmcw_nearby_joint"] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
+                                    "centers": state.params["centers"].tolist()}  # fmt: skip
+
+    # FMCW: no pool at all; every step proposes candidates by the spatial search (coarse
+    # grid, two finer levels, the normal bank and the continuous certificate ascent).
+    bounds = dict(lower=(-0.012, -0.012, 0.288), upper=(0.012, 0.012, 0.312))
+    specs = fmcw_specs(dsplat)
+    specs["centers"] = dsplat.ParameterConfig(scale=0.0005, **bounds)
+    search = dsplat.SpatialSearchConfig(proposal_apertures=64, refine_apertures=64, normal_candidates=8,
+                                        cache_peaks=32, full_peaks=8)  # fmt: skip
+    cfg = dsplat.DSFWConfig(batch=8, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0)
+    state = dsplat.initialize(model, data, surfels(5, seed=9), cfg, parameters=specs)
+    for _ in range(3):
+        state = dsplat.step(state, cfg, search)
+    results["fmcw_spatial_search"] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
+                                      "centers": state.params["centers"].tolist()}  # fmt: skip
 
     # Spectral: a misplaced tone recovered by utility replacement and dense LM.
     grid = dsplat.SpectralGrid((24, 20))
