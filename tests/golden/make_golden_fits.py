@@ -146,18 +146,19 @@ def import_reference(root: Path):
     return dsplat
 
 
-def aperture_grid(side=8, pitch=0.004):
+def aperture_grid(side=8, pitch=0.004, device="cpu"):
     t = (torch.arange(side, dtype=torch.float32) - (side - 1) / 2) * pitch
     x, y = torch.meshgrid(t, t, indexing="ij")
-    return torch.stack([x.flatten(), y.flatten(), torch.zeros(side * side)], -1)
+    return torch.stack([x.flatten(), y.flatten(), torch.zeros(side * side)], -1).to(device)
 
 
-def surfels(count, seed=0, spread=0.01):
+def surfels(count, seed=0, spread=0.01, device="cpu"):
     generator = torch.Generator().manual_seed(seed)
     centers = torch.tensor([0, 0, 0.3]) + spread * (2 * torch.rand(count, 3, generator=generator) - 1)
     direction = torch.tensor([0.0, 0, -1]) + 0.3 * torch.randn(count, 3, generator=generator)
     normals = torch.nn.functional.normalize(direction, dim=1)
-    return dict(centers=centers, normals=normals, areas=torch.full((count,), 1e-4))
+    out = dict(centers=centers, normals=normals, areas=torch.full((count,), 1e-4))
+    return {k: v.to(device) for k, v in out.items()}
 
 
 def fmcw_specs(dsplat):
@@ -168,16 +169,27 @@ def fmcw_specs(dsplat):
     )
 
 
-def main(root: Path) -> None:
-    dsplat = import_reference(root)
+def _record(state):
+    return {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
+            "centers": state.params["centers"].tolist()}  # fmt: skip
+
+
+def run_scenes(dsplat, device="cpu", names=None):
+    """Every scene through the given `dsplat` package; {name: {"history", "centers"}}.
+
+    The same code runs the reference (on the CPU, through the oracle shims) and the GB300
+    package (on CUDA), so the two records differ only by the implementation.
+    """
     results = {}
+    wanted = (lambda name: True) if names is None else (lambda name: name in names)
 
     # FMCW: merged replacement from a displaced start, screened joint Gauss-Newton.
     config = dsplat.FMCWConfig()
-    positions = aperture_grid()
-    truth = surfels(5)
-    coefficients = torch.linspace(0.5, 1.5, 5)
-    empty = dsplat.Scan(torch.zeros((64, config.num_range_bins), dtype=torch.complex64), positions, config)
+    positions = aperture_grid(device=device)
+    truth = surfels(5, device=device)
+    coefficients = torch.linspace(0.5, 1.5, 5).to(device)
+    empty = dsplat.Scan(torch.zeros((64, config.num_range_bins), dtype=torch.complex64, device=device),
+                        positions, config)  # fmt: skip
     data = dsplat.FMCWModel(empty).render(truth, coefficients)
     model = dsplat.FMCWModel(dsplat.Scan(data, positions, config))
     for name, cfg in {
@@ -185,64 +197,71 @@ def main(root: Path) -> None:
         "fmcw_merged_dense": dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, lm_solver="dense", lm_rows=2048,
                                                screen_apertures=0),
     }.items():  # fmt: skip
-        state = dsplat.initialize(model, data, surfels(5, seed=9), cfg, candidates=truth,
+        if not wanted(name):
+            continue
+        state = dsplat.initialize(model, data, surfels(5, seed=9, device=device), cfg, candidates=truth,
                                   parameters=fmcw_specs(dsplat))  # fmt: skip
         for _ in range(4):
             state = dsplat.step(state, cfg)
-        results[name] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
-                         "centers": state.params["centers"].tolist()}  # fmt: skip
+        results[name] = _record(state)
 
     # FMCW: the pool is the truth displaced by a few tenths of a millimetre, so the fit has
     # to move every surfel with the joint Gauss-Newton step.
-    generator = torch.Generator().manual_seed(21)
-    nearby = {"centers": truth["centers"] + 3e-4 * torch.randn(5, 3, generator=generator),
-              "normals": torch.nn.functional.normalize(truth["normals"] + 0.05 * torch.randn(5, 3, generator=generator),
-                                                       dim=1),
-              "areas": truth["areas"].clone()}  # fmt: skip
-    cfg = dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0, lm_steps=2)
-    state = dsplat.initialize(model, data, surfels(5, seed=9), cfg, candidates=nearby,
-                              parameters=fmcw_specs(dsplat))  # fmt: skip
-    for _ in range(6):
-        state = dsplat.step(state, cfg)
-    results["fmcw_nearby_joint"] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
-                                    "centers": state.params["centers"].tolist()}  # fmt: skip
+    if wanted("fmcw_nearby_joint"):
+        generator = torch.Generator().manual_seed(21)
+        cpu_truth = surfels(5)
+        nearby = {"centers": cpu_truth["centers"] + 3e-4 * torch.randn(5, 3, generator=generator),
+                  "normals": torch.nn.functional.normalize(
+                      cpu_truth["normals"] + 0.05 * torch.randn(5, 3, generator=generator), dim=1),
+                  "areas": cpu_truth["areas"].clone()}  # fmt: skip
+        nearby = {k: v.to(device) for k, v in nearby.items()}
+        cfg = dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0, lm_steps=2)
+        state = dsplat.initialize(model, data, surfels(5, seed=9, device=device), cfg, candidates=nearby,
+                                  parameters=fmcw_specs(dsplat))  # fmt: skip
+        for _ in range(6):
+            state = dsplat.step(state, cfg)
+        results["fmcw_nearby_joint"] = _record(state)
 
     # FMCW: no pool at all; every step proposes candidates by the spatial search (coarse
     # grid, two finer levels, the normal bank and the continuous certificate ascent).
-    bounds = dict(lower=(-0.012, -0.012, 0.288), upper=(0.012, 0.012, 0.312))
-    specs = fmcw_specs(dsplat)
-    specs["centers"] = dsplat.ParameterConfig(scale=0.0005, **bounds)
-    search = dsplat.SpatialSearchConfig(proposal_apertures=64, refine_apertures=64, normal_candidates=8,
-                                        cache_peaks=32, full_peaks=8)  # fmt: skip
-    cfg = dsplat.DSFWConfig(batch=8, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0)
-    state = dsplat.initialize(model, data, surfels(5, seed=9), cfg, parameters=specs)
-    for _ in range(3):
-        state = dsplat.step(state, cfg, search)
-    results["fmcw_spatial_search"] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
-                                      "centers": state.params["centers"].tolist()}  # fmt: skip
+    if wanted("fmcw_spatial_search"):
+        bounds = dict(lower=(-0.012, -0.012, 0.288), upper=(0.012, 0.012, 0.312))
+        specs = fmcw_specs(dsplat)
+        specs["centers"] = dsplat.ParameterConfig(scale=0.0005, **bounds)
+        search = dsplat.SpatialSearchConfig(proposal_apertures=64, refine_apertures=64, normal_candidates=8,
+                                            cache_peaks=32, full_peaks=8)  # fmt: skip
+        cfg = dsplat.DSFWConfig(batch=8, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0)
+        state = dsplat.initialize(model, data, surfels(5, seed=9, device=device), cfg, parameters=specs)
+        for _ in range(3):
+            state = dsplat.step(state, cfg, search)
+        results["fmcw_spatial_search"] = _record(state)
 
     # Spectral: a misplaced tone recovered by utility replacement and dense LM.
-    grid = dsplat.SpectralGrid((24, 20))
-    smodel = dsplat.SpectralModel(grid)
-    centers = torch.tensor([[3.3, 4.1], [12.0, 15.0], [18.4, 7.9]])
-    b = torch.tensor([1 + 0.5j, -0.7 + 0.2j, 0.4 - 0.9j])
-    target = smodel.render({"centers": centers}, b)
-    wrong = centers.clone()
-    wrong[1] = torch.tensor([20.0, 2.0])
-    cfg = dsplat.DSFWConfig(coefficients="complex", replacement="utility", lm_solver="dense",
-                            lm_rows=grid.size, lm_gain_ratio=0, lm_steps=3)  # fmt: skip
-    specs = {"centers": dsplat.ParameterConfig(period=grid.shape, scale=0.5)}
-    state = dsplat.initialize(smodel, target, {"centers": wrong}, cfg,
-                              candidates={"centers": grid.bins("cpu")}, parameters=specs)  # fmt: skip
-    for _ in range(3):
-        state = dsplat.step(state, cfg)
-    results["spectral_utility_dense"] = {"history": [{k: float(v) for k, v in e.items()} for e in state.history],
-                                         "centers": state.params["centers"].tolist()}  # fmt: skip
+    if wanted("spectral_utility_dense"):
+        grid = dsplat.SpectralGrid((24, 20))
+        smodel = dsplat.SpectralModel(grid)
+        centers = torch.tensor([[3.3, 4.1], [12.0, 15.0], [18.4, 7.9]], device=device)
+        b = torch.tensor([1 + 0.5j, -0.7 + 0.2j, 0.4 - 0.9j], device=device)
+        target = smodel.render({"centers": centers}, b)
+        wrong = centers.clone()
+        wrong[1] = torch.tensor([20.0, 2.0], device=device)
+        cfg = dsplat.DSFWConfig(coefficients="complex", replacement="utility", lm_solver="dense",
+                                lm_rows=grid.size, lm_gain_ratio=0, lm_steps=3)  # fmt: skip
+        specs = {"centers": dsplat.ParameterConfig(period=grid.shape, scale=0.5)}
+        state = dsplat.initialize(smodel, target, {"centers": wrong}, cfg,
+                                  candidates={"centers": grid.bins(device)}, parameters=specs)  # fmt: skip
+        for _ in range(3):
+            state = dsplat.step(state, cfg)
+        results["spectral_utility_dense"] = _record(state)
+    return results
 
+
+def main(root: Path) -> None:
+    results = run_scenes(import_reference(root), "cpu")
     (HERE / "reference_fits.json").write_text(json.dumps(results, indent=1))
     print("wrote", HERE / "reference_fits.json")
     for name, r in results.items():
-        print(name, [round(e["objective"], 12) for e in r["history"]])
+        print(name, [e["objective"] for e in r["history"]])
 
 
 if __name__ == "__main__":
