@@ -194,6 +194,7 @@ def run_ours(args, world, rank, local):
             state = step(state, config, search)
             end.record()
             times.append((begin, end))
+        flush[:16].zero_()  # a one-block fill: marks the end of the timed steps in launch lists
         torch.cuda.synchronize(device)
         _barrier(world)
     launches = lib.dsg_launch_count() + _lib.REPLAYED_LAUNCHES - launches0
@@ -263,6 +264,12 @@ def run_ours(args, world, rank, local):
     return result
 
 
+TENSOR_KERNELS = ("dsg_gram_bf16x3", "dsg_design_project_bf16x3")
+# DRAM bytes (read + write) per logical flop, from ncu captures of smaller launches of the
+# same kernels, scaled to each launch by its work (see profiles/).
+TRAFFIC_PER_FLOP: dict = {}
+
+
 def _roofline(totals, timers, work, args):
     peaks, source = _peaks()
     if not totals:
@@ -270,16 +277,20 @@ def _roofline(totals, timers, work, args):
     name = max(totals, key=totals.get)
     launches = len(timers[name])
     avg_ms = totals[name] / launches
-    if name == "dsg_gram_bf16x3":
-        # Logical FP32 work of the symmetric products (R S (S + 1) for a full Gram) over the
-        # launches' measured time, against the sustained bf16 tensor peak / 3 (three bf16
-        # products per logical multiply-add).
+    if name in TENSOR_KERNELS:
+        # Logical FP32 work (the Gram: R S (S + 1) for a full symmetric product; the fused
+        # projection: 4 K rank2 per aperture-surfel pair) over the launches' measured time,
+        # against the sustained bf16 tensor peak / 3 (three bf16 products per logical
+        # multiply-add in split-BF16x3).
         flops = work.get(name)
         achieved = flops / (totals[name] * 1e-3) / 1e12 if flops else None
         peak = peaks["bf16_tflops_sustained"] / 3
+        per_launch = flops / launches if flops else None
+        traffic = TRAFFIC_PER_FLOP.get(name)
         return {"kernel": name, "bound": "tensor", "achieved": achieved and round(achieved, 2),
                 "peak": round(peak, 2), "unit": "TFLOP/s",
-                "frac": achieved and round(achieved / peak, 4), "traffic": None,
+                "frac": achieved and round(achieved / peak, 4),
+                "traffic": traffic and per_launch and round(traffic * per_launch),
                 "peak_source": f"{source} bf16_tflops_sustained / 3", "launches": launches,
                 "avg_ms": round(avg_ms, 4)}  # fmt: skip
     return {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -432,6 +443,30 @@ def run_kernels(args):
 
     low, high = box_of(centers)
     model = FMCWModel(Scan(upstream, positions, config)).prepare({"centers": ParameterConfig(lower=low, upper=high)})
+    # The fused design projection alone, on the first 2048 apertures with their block basis.
+    from dsplat.kernels.gram import GramRows as _Rows
+    from dsplat.kernels.gram import append_projected
+
+    first = positions[: min(A, 2048)].contiguous()
+    basis = model.block_basis(slice(0, len(first) * K))
+    rank2 = basis.interleaved.shape[0]
+    store = _Rows(S, len(first) * rank2, device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def project_once():
+        store.rows = 0
+        append_projected(store, config, first, params, basis, 0.0, status)
+
+    ms = _event_time(project_once, it, wu, flush)
+    values = len(first) * S * K
+    flops = values * 4 * rank2  # logical FP32 multiply-adds of U [rank2, 2K] . v, times 2
+    tensor_peak = peaks["bf16_tflops"] / 3
+    rows.append({"kernel": "dsg_design_project_bf16x3", "ms": round(ms, 4), "units": values,
+                 "unit": "pair-bins (dictionary values)", "rank2": rank2, "units_per_s": values / (ms * 1e-3),
+                 "achieved_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
+                 "tensor_peak_tflops": round(tensor_peak, 1),
+                 "frac_tensor": round(flops / (ms * 1e-3) / 1e12 / tensor_peak, 4),
+                 "out_gbs": round(2 * 2 * len(first) * rank2 * S / (ms * 1e-3) / 1e9, 1)})  # fmt: skip
     mixed = DSFWConfig(gram="bf16x3")
     ms = _event_time(lambda: normal_equations(model, params, upstream, mixed), it, wu, flush)
     rows.append({"kernel": "normal_equations (fused projection + tcgen05 Gram)", "ms": round(ms, 3)})

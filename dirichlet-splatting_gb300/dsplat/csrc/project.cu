@@ -2,19 +2,25 @@
 // tensor cores: the mixed-precision replacement of design_bins + RowBasis.reduce_major
 // (reference: dsplat/kernels/surfel.slang:313-378 and dsplat/fmcw.py:128-131, 276-294).
 //
-// For every aperture a of a block and every tile of 32 surfels, the real dictionary
-// column of each surfel, v[2k + part] = (re, im) of sqrt(area) c D(k - k0), is evaluated
-// in the cotangent form of common.cuh straight into shared memory, split into bf16
-// hi + lo, and multiplied by the block's interleaved basis U [2 rank, 2K] (also split,
-// zero padded to 128 rows) with three tcgen05.mma products per K step (hi.hi, hi.lo,
-// lo.hi). The projected values P[a 2rank + rho, s] = (U v_s)[rho] leave the tensor
-// memory already split and transposed into the Gram operand PT_hi / PT_lo [S_pad, ld],
-// so the design matrix never touches HBM.
+// For one aperture a and a tile of 128 surfels, the real dictionary column of each surfel,
+// v[2k + part] = (re, im) of sqrt(area) c D(k - k0), is evaluated in the cotangent form of
+// common.cuh straight into shared memory, split into bf16 hi + lo, and multiplied by the
+// interleaved basis U [rank2, 2K] (also split, zero padded to N = rank2 rounded up to 32
+// rows) with three tcgen05.mma products per K step (hi.hi, lo.hi, hi.lo): the tile is the
+// M = 128 operand, U the N operand, so the tensor work scales with the basis rank. The
+// projected values P[s, a rank2 + rho] = (U v_s)[rho] leave the tensor memory split and
+// already in the layout of the Gram operand PT_hi / PT_lo [S, ld]: the design matrix never
+// touches HBM.
 //
-// CTA: 8 warps. Warps 0-3 evaluate the dictionary tile (lane = range bin, loop over the
-// tile's 32 surfels, whose geometry warp 0 computed first) into one of two shared
-// buffers; thread 0 then issues the MMAs into one of two TMEM accumulators. Warps 4-7
-// load the accumulator (tcgen05.ld) and store the split rows. All waits are bounded.
+// CTA of 21 warps, persistent over work units of (aperture, 256 surfels):
+//   warps 0-15  geometry of the unit's 256 pairs (one per thread of warps 0-7), then the
+//               dictionary tiles, one K-subtile (32 bins of 128 surfels, 8 surfels per
+//               warp) per pipeline stage;
+//   warps 16-19 epilogue: tcgen05.ld of a finished accumulator, bf16 split, a transpose
+//               through shared memory, and row-contiguous stores of PT;
+//   warp 20     TMEM allocation, the TMA copy of U, and the MMA issue (one thread).
+// Stages and accumulators are rings guarded by mbarriers; every wait is bounded and a
+// wait that runs out raises the status word instead of hanging.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -29,28 +35,77 @@ using namespace tc;
 
 namespace {
 
-constexpr int PM = 128;                 // MMA M: basis rows, zero padded
-constexpr int PN = 32;                  // MMA N: surfels per tile
-constexpr int PTHREADS = 256;
-constexpr int UB_SUB = PM * 64 * 2;     // one [128 x 64] bf16 K-subtile of U: 16 KiB
-constexpr int BB_SUB = PN * 64 * 2;     // one [32 x 64] bf16 K-subtile of a tile: 4 KiB
-constexpr uint32_t PIDESC = idesc_bf16(PM, PN);
+constexpr int TM = 128;                    // MMA M: surfels per tile
+constexpr int UNIT = 256;                  // surfels per work unit (two tiles)
+constexpr int NPROD = 512;                 // producer threads (warps 0-15)
+constexpr int ROWS_PER_WARP = TM / (NPROD / 32);
+constexpr int EPI_WARP = NPROD / 32;       // first of the four epilogue warps
+constexpr int MMA_WARP = EPI_WARP + 4;
+constexpr int PTHREADS = (MMA_WARP + 1) * 32;
+constexpr int A_SUB = TM * 128;            // one [128 x 64] bf16 K-subtile: 16 KiB
+constexpr int STAGE_BYTES = 2 * A_SUB;     // hi + lo
+constexpr int MAX_STAGES = 4;
+constexpr int XPOSE_WORDS = 2 * 32 * 17 + 16;  // per epilogue warp: hi [32][17], lo [32][17]
+constexpr int SMEM_LIMIT = 227 * 1024;
 
-template <int P>
-struct ProjectSmem {
-  static constexpr int REC = 2 + 2 * P;
-};
-
-// Byte offset of element (row n, k) inside a K-major, 128-byte-swizzled operand made of
-// K-subtiles of 64 elements (rows of 128 B, 8-row atoms of 1024 B).
-__device__ __forceinline__ uint32_t sw128_offset(int n, int k, int sub_bytes) {
-  const int sub = k >> 6, within = k & 63;
-  const int chunk = (within >> 3) ^ (n & 7);
-  return (uint32_t)(sub * sub_bytes + (n >> 3) * 1024 + (n & 7) * 128 + chunk * 16 + (within & 7) * 2);
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 lo_half, __nv_bfloat16 hi_half) {
-  return (uint32_t)__bfloat16_as_ushort(lo_half) | ((uint32_t)__bfloat16_as_ushort(hi_half) << 16);
+// Named barrier over `count` threads that also returns the OR of every thread's predicate.
+__device__ __forceinline__ bool bar_or(int id, int count, bool pred) {
+  uint32_t out;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(out)
+      : "r"((uint32_t)pred), "r"(id), "r"(count)
+      : "memory");
+  return out != 0;
+}
+
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) {
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// Shared-memory plan of one CTA; identical on host and device.
+struct Plan {
+  int nsub;        // K-subtiles of 64 elements: 2K / 64
+  int ncols;       // N: rank2 rounded up to 32
+  int stages;      // pipeline depth
+  int u_bytes;     // one of U hi / U lo
+  int table_off, recs_off, xpose_off, bars_off, total;
+};
+
+__host__ __device__ inline Plan make_plan(int K, int N_fft, int P, int rank2, int stages) {
+  Plan p;
+  p.nsub = 2 * K / 64;
+  p.ncols = (rank2 + 31) / 32 * 32;
+  p.stages = stages;
+  p.u_bytes = p.nsub * p.ncols * 128;
+  int off = 2 * p.u_bytes + stages * STAGE_BYTES;  // 1024-aligned blocks first
+  p.table_off = off;
+  off += ((N_fft + K + 3) & ~3) * 4;
+  p.recs_off = off;
+  off += UNIT * (2 + 2 * P) * 4;
+  p.xpose_off = off;
+  off += 4 * XPOSE_WORDS * 4;
+  p.bars_off = (off + 7) & ~7;
+  off = p.bars_off + (1 + 2 * MAX_STAGES + 4 + 1) * 8 + 8;
+  p.total = off + 1024;  // slack for the 1024-byte alignment of the base
+  return p;
 }
 
 template <int P>
@@ -58,81 +113,83 @@ __global__ void __launch_bounds__(PTHREADS, 1)
     design_project_kernel(Consts c, const __grid_constant__ CUtensorMap u_hi_map,
                           const __grid_constant__ CUtensorMap u_lo_map, const float* __restrict__ pos,
                           int A, const float* __restrict__ cen, const float* __restrict__ nrm,
-                          const float* __restrict__ areas, int S, int rank2,
+                          const float* __restrict__ areas, int S, int rank2, int stages,
                           __nv_bfloat16* __restrict__ pt_hi, __nv_bfloat16* __restrict__ pt_lo,
                           int64_t ld, int64_t col0, int* __restrict__ status) {
-  constexpr int REC = ProjectSmem<P>::REC;
+  constexpr int REC = 2 + 2 * P;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  const int K2 = 2 * c.K;           // reduction length: (re, im) of every bin
-  const int nsub = K2 / 64;         // K-subtiles of 64 elements
+  const Plan plan = make_plan(c.K, c.N, P, rank2, stages);
+  const int nsub = plan.nsub, N = plan.ncols;
   uint8_t* u_hi = smem;
-  uint8_t* u_lo = u_hi + nsub * UB_SUB;
-  uint8_t* tiles = u_lo + nsub * UB_SUB;  // [2 buffers][hi, lo][nsub][PN x 64]
-  const int tile_bytes = 2 * nsub * BB_SUB;
-  float* table = reinterpret_cast<float*>(tiles + 2 * tile_bytes);
-  const int tbl_n = c.N + c.K;
-  float* recs = table + ((tbl_n + 3) & ~3);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(recs + ((PN * REC + 1) & ~1));
-  uint64_t* u_full = bars;          // U landed
-  uint64_t* mma_done = bars + 1;    // [2] MMA of a buffer finished (tile smem and TMEM ready)
-  uint64_t* tmem_free = bars + 3;   // [2] epilogue finished reading a TMEM buffer
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 5);
+  uint8_t* u_lo = smem + plan.u_bytes;
+  uint8_t* stage_base = smem + 2 * plan.u_bytes;
+  float* table = reinterpret_cast<float*>(smem + plan.table_off);
+  float* recs = reinterpret_cast<float*>(smem + plan.recs_off);
+  uint32_t* xpose = reinterpret_cast<uint32_t*>(smem + plan.xpose_off);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + plan.bars_off);
+  uint64_t* u_full = bars;                    // U landed
+  uint64_t* full = bars + 1;                  // [stages] a stage holds a finished K-subtile
+  uint64_t* empty = full + MAX_STAGES;        // [stages] the MMAs reading a stage finished
+  uint64_t* done = empty + MAX_STAGES;        // [2] an accumulator holds a finished tile
+  uint64_t* tfree = done + 2;                 // [2] the epilogue has read an accumulator
+  uint64_t* drain = tfree + 2;                // every issued MMA finished
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int groups = (S + PN - 1) / PN;
-  const int tiles_total = A * groups;
+  const int groups = (S + UNIT - 1) / UNIT;
+  const int units = A * groups;
+  uint32_t tmem_cols = 32;
+  while ((int)tmem_cols < 2 * N) tmem_cols <<= 1;
 
-  for (int i = threadIdx.x; i < tbl_n; i += PTHREADS) table[i] = tan_entry(i, c.N, false);
+  for (int i = threadIdx.x; i < c.N + c.K; i += PTHREADS) table[i] = tan_entry(i, c.N, false);
   if (threadIdx.x == 0) {
     mbar_init(u_full, 1);
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&mma_done[b], 1);
-      mbar_init(&tmem_free[b], 4);
+    for (int b = 0; b < stages; ++b) {
+      mbar_init(&full[b], NPROD / 32);
+      mbar_init(&empty[b], 1);
     }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&done[b], 1);
+      mbar_init(&tfree[b], 4);
+    }
+    mbar_init(drain, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(64));
+                 "r"(tmem_cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = idesc_bf16(TM, N);
 
-  if (threadIdx.x == 0) {  // the basis, once per CTA
-    mbar_expect_tx(u_full, 2 * nsub * UB_SUB);
-    for (int t = 0; t < nsub; ++t) {
-      tma_load_2d(u_hi + t * UB_SUB, &u_hi_map, 64 * t, 0, u_full);
-      tma_load_2d(u_lo + t * UB_SUB, &u_lo_map, 64 * t, 0, u_full);
-    }
-  }
-
-  if (warp < 4) {
-    // ---------------- producers: dictionary tiles and MMA issue ----------------
-    bool u_ready = false;
-    int local = 0;
-    for (int t = blockIdx.x; t < tiles_total; t += gridDim.x, ++local) {
-      const int a = t / groups, g = t % groups;
-      const int buf = local & 1, use = local >> 1;
-      // geometry of the tile's 32 pairs (warp 0, one pair per lane)
-      if (warp == 0) {
-        const int s = g * PN + lane;
-        float* r = recs + lane * REC;
+  if (warp < EPI_WARP) {
+    // ---------------- producers: pair geometry and dictionary K-subtiles ----------------
+    int stage = 0;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+      const int a = unit / groups, g = unit % groups;
+      // Everyone is done with the last records; the OR over the barrier makes the abort
+      // decision the same in every producer thread.
+      if (bar_or(1, NPROD, *abort != 0)) break;
+      if (threadIdx.x < UNIT) {
+        const int s = g * UNIT + threadIdx.x;
+        float* r = recs + threadIdx.x * REC;
         Pair q;
         const int sc = s < S ? s : 0;
         pair_setup(c, __ldg(pos + 3 * a), __ldg(pos + 3 * a + 1), __ldg(pos + 3 * a + 2),
                    __ldg(cen + 3 * sc), __ldg(cen + 3 * sc + 1), __ldg(cen + 3 * sc + 2),
                    __ldg(nrm + 3 * sc), __ldg(nrm + 3 * sc + 1), __ldg(nrm + 3 * sc + 2), q);
         if (s < S && q.amp > 0.0f) {
-          float2 cw = cscale(q.rot, q.amp * sqrtf(__ldg(areas + s)) * c.inv_S);
+          const float2 cw = cscale(q.rot, q.amp * sqrtf(__ldg(areas + s)) * c.inv_S);
           float2 nu[P];
           numerators<P>(q.off, nu);
           r[0] = q.tl;
@@ -145,93 +202,154 @@ __global__ void __launch_bounds__(PTHREADS, 1)
 #pragma unroll
           for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 + 2 * k) = make_float2(0.f, 0.f);
         }
-        // the buffer is free once the MMA that read it two tiles ago has finished
-        if (lane == 0 && use > 0 && !mbar_wait(&mma_done[buf], (use - 1) & 1, abort)) *abort = 1;
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");
-      if (*abort) break;  // uniform: read after the barrier
-      uint8_t* hi = tiles + buf * tile_bytes;
-      uint8_t* lo = hi + nsub * BB_SUB;
-      const int k = warp * 32 + lane;  // range bin of this thread
-      if (k < c.K) {
-#pragma unroll 4
-        for (int n = 0; n < PN; ++n) {
-          const float* r = recs + n * REC;
-          const float tl = r[0];
-          const int lobe = __float_as_int(r[1]);
-          const float2 gg = *reinterpret_cast<const float2*>(r + 2 + 2 * ((k - lobe) & (P - 1)));
-          const float cot = cot_from(table[k - lobe + c.N - 1], tl);
-          const float re = gg.x * cot - gg.y, im = gg.y * cot + gg.x;
-          const __nv_bfloat16 re_h = __float2bfloat16_rn(re), im_h = __float2bfloat16_rn(im);
-          const __nv_bfloat16 re_l = __float2bfloat16_rn(re - __bfloat162float(re_h));
-          const __nv_bfloat16 im_l = __float2bfloat16_rn(im - __bfloat162float(im_h));
-          const uint32_t off = sw128_offset(n, 2 * k, BB_SUB);
-          *reinterpret_cast<uint32_t*>(hi + off) = pack_bf16x2(re_h, im_h);
-          *reinterpret_cast<uint32_t*>(lo + off) = pack_bf16x2(re_l, im_l);
-        }
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("bar.sync 1, 128;" ::: "memory");
-      if (threadIdx.x == 0) {
-        bool ok = true;
-        if (!u_ready) ok = u_ready = mbar_wait(u_full, 0, abort);
-        if (ok && use > 0) ok = mbar_wait(&tmem_free[buf], (use - 1) & 1, abort);
-        if (!ok) {
-          *abort = 1;
-        } else {
-          tc_fence_after();
-          const uint32_t d = tmem + (uint32_t)(buf * PN);
-          for (int kk = 0; kk < K2 / 16; ++kk) {
-            const uint32_t uoff = (uint32_t)((kk >> 2) * UB_SUB + (kk & 3) * 32);
-            const uint32_t boff = (uint32_t)((kk >> 2) * BB_SUB + (kk & 3) * 32);
-            const uint64_t ah = sw128_desc(smem_u32(u_hi) + uoff), al = sw128_desc(smem_u32(u_lo) + uoff);
-            const uint64_t bh = sw128_desc(smem_u32(hi) + boff), bl = sw128_desc(smem_u32(lo) + boff);
-            umma_bf16(d, ah, bh, PIDESC, kk != 0);
-            umma_bf16(d, ah, bl, PIDESC, 1u);
-            umma_bf16(d, al, bh, PIDESC, 1u);
+      asm volatile("bar.sync 1, %0;" ::"r"(NPROD) : "memory");
+      const int tiles = min(2, (S - g * UNIT + TM - 1) / TM);
+      for (int u = 0; u < tiles; ++u) {
+        for (int j = 0; j < nsub; ++j, ++stage) {
+          const int slot = stage % stages;
+          const int round = stage / stages;
+          bool ok = true;
+          if (lane == 0 && round > 0 && !mbar_wait(&empty[slot], (round - 1) & 1, abort)) {
+            *abort = 1;
+            ok = false;
           }
-          umma_commit(&mma_done[buf]);
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+          if (ok) {
+            uint8_t* hi = stage_base + slot * STAGE_BYTES;
+            uint8_t* lo = hi + A_SUB;
+            const int k = j * 32 + lane;  // this lane's range bin
+            const uint32_t lane_bytes = (uint32_t)(lane & 3) << 2;
+#pragma unroll
+            for (int i = 0; i < ROWS_PER_WARP; ++i) {
+              const int row = warp * ROWS_PER_WARP + i;  // surfel within the tile
+              const float* r = recs + (u * TM + row) * REC;
+              const float tl = r[0];
+              const int lobe = __float_as_int(r[1]);
+              const float2 gg = *reinterpret_cast<const float2*>(r + 2 + 2 * ((k - lobe) & (P - 1)));
+              const float cot = cot_from(table[k - lobe + c.N - 1], tl);
+              const float re = gg.x * cot - gg.y, im = gg.y * cot + gg.x;
+              const __nv_bfloat162 h = __floats2bfloat162_rn(re, im);
+              const __nv_bfloat162 l = __floats2bfloat162_rn(re - __low2float(h), im - __high2float(h));
+              // K-major, 128-byte swizzle: row, then the 16-byte chunk XOR (row mod 8)
+              const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128) +
+                                   ((uint32_t)((lane >> 2) ^ (row & 7)) << 4) + lane_bytes;
+              *reinterpret_cast<uint32_t*>(hi + off) = bf16x2_bits(h);
+              *reinterpret_cast<uint32_t*>(lo + off) = bf16x2_bits(l);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&full[slot]);
         }
+      }
+    }
+  } else if (warp < MMA_WARP) {
+    // ---------------- epilogue: TMEM -> split PT rows ----------------
+    const int quarter = warp & 3;  // TMEM lanes 32 quarter .. 32 quarter + 31
+    uint32_t* xh = xpose + quarter * XPOSE_WORDS;
+    uint32_t* xl = xh + 32 * 17 + 16;
+    int tile = 0;
+    bool ok = true;
+    for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
+      const int a = unit / groups, g = unit % groups;
+      const int tiles = min(2, (S - g * UNIT + TM - 1) / TM);
+      const int64_t base_col = col0 + (int64_t)a * rank2;
+      for (int u = 0; u < tiles; ++u, ++tile) {
+        const int acc = tile & 1, use = tile >> 1;
+        if (!mbar_wait(&done[acc], use & 1, abort)) {
+          *abort = 1;
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const int row0 = g * UNIT + u * TM + quarter * 32;  // surfel of lane 0
+        for (int c0 = 0; c0 < N; c0 += 32) {
+          uint32_t v[32];
+          tmem_ld32_nowait(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * N + c0), v);
+#pragma unroll
+          for (int w = 0; w < 16; ++w) {
+            const float x0 = __uint_as_float(v[2 * w]), x1 = __uint_as_float(v[2 * w + 1]);
+            const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+            const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h));
+            xh[lane * 17 + w] = bf16x2_bits(h);
+            xl[lane * 17 + w] = bf16x2_bits(l);
+          }
+          __syncwarp();
+          // one row per step: lanes 0-15 store its hi words, lanes 16-31 its lo words
+          const int word = lane & 15;
+          const bool col_ok = c0 + 2 * word < rank2;
+          __nv_bfloat16* dst_base = lane < 16 ? pt_hi : pt_lo;
+          const uint32_t* src = lane < 16 ? xh : xl;
+          for (int r = 0; r < 32; ++r) {
+            const int s = row0 + r;
+            if (s < S && col_ok)
+              *reinterpret_cast<uint32_t*>(dst_base + (int64_t)s * ld + base_col + c0 + 2 * word) =
+                  src[r * 17 + word];
+          }
+          __syncwarp();
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tfree[acc]);
       }
     }
   } else {
-    // ---------------- consumers: TMEM -> split, transposed rows ----------------
-    const int quarter = warp & 3;
-    const int rho = 32 * quarter + lane;
-    int local = 0;
-    for (int t = blockIdx.x; t < tiles_total; t += gridDim.x, ++local) {
-      const int a = t / groups, g = t % groups;
-      const int buf = local & 1, use = local >> 1;
-      if (!mbar_wait(&mma_done[buf], use & 1, abort)) {
-        *abort = 1;
-        break;
-      }
-      tc_fence_after();
-      uint32_t v[32];
-      const bool rows_here = 32 * quarter < rank2;
-      if (rows_here) tmem_ld32(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(buf * PN), v);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tmem_free[buf]);
-      if (rows_here && rho < rank2) {
-        const int64_t col = col0 + (int64_t)a * rank2 + rho;
-#pragma unroll
-        for (int n = 0; n < PN; ++n) {
-          const int s = g * PN + n;
-          const float x = __uint_as_float(v[n]);
-          const __nv_bfloat16 h = __float2bfloat16_rn(x);
-          const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-          pt_hi[(int64_t)s * ld + col] = h;
-          pt_lo[(int64_t)s * ld + col] = l;
+    // ---------------- MMA issue (one thread) ----------------
+    if (lane == 0) {
+    mbar_expect_tx(u_full, 2 * plan.u_bytes);
+    for (int t = 0; t < nsub; ++t) {
+      tma_load_2d(u_hi + t * (N * 128), &u_hi_map, 64 * t, 0, u_full);
+      tma_load_2d(u_lo + t * (N * 128), &u_lo_map, 64 * t, 0, u_full);
+    }
+    bool ok = mbar_wait(u_full, 0, abort);
+    int stage = 0, tile = 0;
+    for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
+      const int g = unit % groups;
+      const int tiles = min(2, (S - g * UNIT + TM - 1) / TM);
+      for (int u = 0; u < tiles && ok; ++u, ++tile) {
+        const int acc = tile & 1, use = tile >> 1;
+        if (use > 0 && !mbar_wait(&tfree[acc], (use - 1) & 1, abort)) {
+          ok = false;
+          break;
         }
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(acc * N);
+        for (int j = 0; j < nsub; ++j, ++stage) {
+          const int slot = stage % stages;
+          if (!mbar_wait(&full[slot], (stage / stages) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a_hi = smem_u32(stage_base + slot * STAGE_BYTES);
+          const uint32_t a_lo = a_hi + A_SUB;
+          const uint32_t b_hi = smem_u32(u_hi + j * (N * 128));
+          const uint32_t b_lo = smem_u32(u_lo + j * (N * 128));
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint32_t step = (uint32_t)kk * 32;
+            umma_bf16(d, sw128_desc(a_hi + step), sw128_desc(b_hi + step), idesc, (j | kk) != 0);
+            umma_bf16(d, sw128_desc(a_lo + step), sw128_desc(b_hi + step), idesc, 1u);
+            umma_bf16(d, sw128_desc(a_hi + step), sw128_desc(b_lo + step), idesc, 1u);
+          }
+          umma_commit(&empty[slot]);
+        }
+        if (ok) umma_commit(&done[acc]);
       }
     }
+    if (!ok) *abort = 1;
+    // Every MMA issued so far completes before the accumulators are released.
+    umma_commit(drain);
+    mbar_wait_plain(drain, 0);
+    }
+    __syncwarp();
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == MMA_WARP) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols));
   }
   if (threadIdx.x == 0 && *abort) atomicExch(status, 1);
 }
@@ -252,38 +370,40 @@ bool encode_ready() {
   return true;
 }
 
-bool basis_map(CUtensorMap* map, const void* base, int cols) {
-  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)PM};
+// Rows [0, box_rows) of the [128, cols] bf16 basis, 64 columns per copy, 128-byte swizzle.
+bool basis_map(CUtensorMap* map, const void* base, int cols, int box_rows) {
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, 128};
   const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-  const cuuint32_t box[2] = {64, PM};
+  const cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   return g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-size_t project_smem(int K, int N, int P) {
-  const int nsub = 2 * K / 64;
-  const size_t tbl = (size_t)((N + K + 3) & ~3) * 4;
-  const size_t recs = (size_t)((PN * (2 + 2 * P) + 1) & ~1) * 4;
-  return 1024 + 2 * (size_t)nsub * UB_SUB + 2 * 2 * (size_t)nsub * BB_SUB + tbl + recs + 64;
+// Deepest stage ring (at most MAX_STAGES) that fits the shared-memory limit; 0 if fewer than 2.
+int plan_stages(int K, int N_fft, int P, int rank2) {
+  for (int stages = MAX_STAGES; stages >= 2; --stages)
+    if (make_plan(K, N_fft, P, rank2, stages).total <= SMEM_LIMIT) return stages;
+  return 0;
 }
 
 template <int P>
 int launch_project(const Consts& c, const CUtensorMap& mh, const CUtensorMap& ml, const float* pos,
                    int A, const float* cen, const float* nrm, const float* areas, int S, int rank2,
                    void* hi, void* lo, int64_t ld, int64_t col0, int* status, cudaStream_t st) {
-  const size_t smem = project_smem(c.K, c.N, P);
+  const int stages = plan_stages(c.K, c.N, P, rank2);
+  if (stages == 0) return DSG_ERR_UNSUPPORTED;
+  const size_t smem = (size_t)make_plan(c.K, c.N, P, rank2, stages).total;
   auto kern = design_project_kernel<P>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return DSG_ERR_LAUNCH;
-  const int groups = (S + PN - 1) / PN;
-  const long long tiles = (long long)A * groups;
+  const long long units = (long long)A * ((S + UNIT - 1) / UNIT);
   int sms = 152;
   int dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = (int)(tiles < sms ? tiles : sms);
-  kern<<<grid, PTHREADS, smem, st>>>(c, mh, ml, pos, A, cen, nrm, areas, S, rank2,
+  const int grid = (int)(units < sms ? units : sms);
+  kern<<<grid, PTHREADS, smem, st>>>(c, mh, ml, pos, A, cen, nrm, areas, S, rank2, stages,
                                      reinterpret_cast<__nv_bfloat16*>(hi),
                                      reinterpret_cast<__nv_bfloat16*>(lo), ld, col0, status);
   dsg_count_launches(1);
@@ -305,16 +425,21 @@ int dsg_design_project_bf16x3(const DsgChirp* chirp, const float* positions, int
   const int K = chirp->num_bins;
   if (!(K == 32 || K == 64 || K == 128) || !(chirp->pad == 1 || chirp->pad == 2 || chirp->pad == 4))
     return DSG_ERR_UNSUPPORTED;
-  if (apertures < 0 || surfels < 0 || rank2 < 1 || rank2 > PM || column_offset < 0) return DSG_ERR_ARGUMENT;
+  if (apertures < 0 || surfels < 0 || rank2 < 2 || rank2 > 128 || (rank2 & 1) || column_offset < 0 ||
+      (column_offset & 1) || (ld & 1))
+    return DSG_ERR_ARGUMENT;
   if (apertures == 0 || surfels == 0) return DSG_OK;
   if (!positions || !centers || !normals || !areas || !basis_hi || !basis_lo || !pt_hi || !pt_lo || !status)
     return DSG_ERR_ARGUMENT;
   if (ld < column_offset + (int64_t)apertures * rank2) return DSG_ERR_ARGUMENT;
   if ((reinterpret_cast<uintptr_t>(basis_hi) | reinterpret_cast<uintptr_t>(basis_lo)) & 15u)
     return DSG_ERR_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(pt_hi) | reinterpret_cast<uintptr_t>(pt_lo)) & 3u) return DSG_ERR_ARGUMENT;
   if (!encode_ready()) return DSG_ERR_LIBRARY;
+  const int ncols = (rank2 + 31) / 32 * 32;
   CUtensorMap mh, ml;
-  if (!basis_map(&mh, basis_hi, 2 * K) || !basis_map(&ml, basis_lo, 2 * K)) return DSG_ERR_ARGUMENT;
+  if (!basis_map(&mh, basis_hi, 2 * K, ncols) || !basis_map(&ml, basis_lo, 2 * K, ncols))
+    return DSG_ERR_ARGUMENT;
   const Consts c = make_consts(*chirp);
   cudaStream_t st = (cudaStream_t)stream;
   switch (chirp->pad) {

@@ -713,112 +713,140 @@ __global__ void __launch_bounds__(128) jacobian_kernel(Consts c, const float* __
 }
 
 // ------------------------------------------------------------------------------------
-// Normal-bank scores (reference: dsplat/kernels/correlate.slang:110-169). Thread =
-// candidate; the aperture loop is sequential, so every sum has a fixed order. The
-// per-aperture correlation comes either from the exact bin sum or from Catmull-Rom
-// interpolation of an oversampled FFT range table.
+// Normal-bank scores (reference: dsplat/kernels/correlate.slang:110-169). A warp owns
+// one candidate. Its lanes first evaluate 32 apertures' pair geometry and per-aperture
+// correlation in parallel (from the exact bin sum, or by Catmull-Rom interpolation of an
+// oversampled FFT range table) into a per-warp record; then each lane takes one normal
+// of the bank (lane 0 of the first chunk: the candidate's own normal) and adds the 32
+// apertures in order. Every sum runs over apertures in ascending order, so the result
+// is fixed; a lane holds three accumulators, not three per normal, which keeps the
+// kernel at full occupancy.
 // ------------------------------------------------------------------------------------
-constexpr int kBankChunk = 32;
+constexpr int kOrientWarps = 8;
+constexpr int kOrientRec = 8;  // ux, uy, uz, path = amp_scale / r, corr.re, corr.im, norm, pad
 
-template <int P>
-__global__ void __launch_bounds__(128) orientations_kernel(
+// amp of scattering() for one normal: cos^2 F(cos) lambda / (8 pi r) with the same rounding
+// ((path cos) cos) F; without a Fresnel factor F = 1 and the last product is exact.
+template <bool FRESNEL>
+__device__ __forceinline__ float bank_amplitude(const Consts& c, float cosv, float path) {
+  if (!(cosv > 0.0f)) return 0.0f;
+  float amp = path * cosv * cosv;
+  if (FRESNEL) {
+    float f, df;
+    fresnel_factor(cosv, c.fresnel_n, f, df);
+    amp *= f;
+  }
+  return amp;
+}
+
+template <int P, bool FRESNEL>
+__global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
     Consts c, const float* __restrict__ pos, int A, const float* __restrict__ cen,
     const float* __restrict__ nrm, int C, const float* __restrict__ bank, int bank_size,
-    int j_begin, const float2* __restrict__ res, const float2* __restrict__ table,
+    const float2* __restrict__ res, const float2* __restrict__ table,
     const float* __restrict__ norm_table, int oversample, float* __restrict__ out) {
   extern __shared__ float smem[];
   const int tbl_n = c.N + c.K;
   float* tbl = smem;
-  float* bk = smem + ((tbl_n + 3) & ~3);
-  const int nj = min(kBankChunk, bank_size + 1 - j_begin);
   if (table == nullptr)
     for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) tbl[i] = tan_entry(i, c.N, true);
-  for (int i = threadIdx.x; i < 3 * nj; i += blockDim.x) {
-    const int j = j_begin + i / 3;
-    bk[i] = j == 0 ? 0.0f : __ldg(bank + 3 * (j - 1) + i % 3);
-  }
   __syncthreads();
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= C) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* rec = smem + ((tbl_n + 3) & ~3) + warp * 32 * kOrientRec;
+  const int s = blockIdx.x * kOrientWarps + warp;
+  if (s >= C) return;  // warp-uniform; no block barrier follows
   const float cx = __ldg(cen + 3 * s), cy = __ldg(cen + 3 * s + 1), cz = __ldg(cen + 3 * s + 2);
   const float own[3] = {__ldg(nrm + 3 * s), __ldg(nrm + 3 * s + 1), __ldg(nrm + 3 * s + 2)};
-  float acc[kBankChunk][3];
-#pragma unroll
-  for (int j = 0; j < kBankChunk; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0f;
   const int size = c.N * oversample;
-  for (int a = 0; a < A; ++a) {
-    Pair q;
-    pair_setup(c, __ldg(pos + 3 * a), __ldg(pos + 3 * a + 1), __ldg(pos + 3 * a + 2), cx, cy, cz,
-               own[0], own[1], own[2], q);
-    float2 corr;
-    float norm;
-    if (table != nullptr) {
-      // x = k0 * oversample with k0 = lobe - off
-      const float x = ((float)q.lobe - q.off) * (float)oversample;
-      const float fb = floorf(x);
-      const float t = x - fb;
-      const int base = (int)fb;
-      const float t2 = t * t, t3 = t2 * t;
-      const float wts[4] = {-0.5f * t + t2 - 0.5f * t3, 1.0f - 2.5f * t2 + 1.5f * t3,
-                            0.5f * t + 2.0f * t2 - 1.5f * t3, -0.5f * t2 + 0.5f * t3};
-      float2 v = make_float2(0.f, 0.f);
-      float nn = 0.0f;
+  const int normals = bank_size + 1;
+  float* o = out + (size_t)s * normals * 3;
+  for (int j0 = 0; j0 < normals; j0 += 32) {
+    const int j = j0 + lane;
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    if (j == 0) {
+      ex = own[0];
+      ey = own[1];
+      ez = own[2];
+    } else if (j < normals) {
+      ex = __ldg(bank + 3 * (j - 1));
+      ey = __ldg(bank + 3 * (j - 1) + 1);
+      ez = __ldg(bank + 3 * (j - 1) + 2);
+    }
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f;
+    for (int a0 = 0; a0 < A; a0 += 32) {
+      const int a = a0 + lane;
+      if (a < A) {
+        Pair q;
+        pair_setup(c, __ldg(pos + 3 * a), __ldg(pos + 3 * a + 1), __ldg(pos + 3 * a + 2), cx, cy, cz,
+                   own[0], own[1], own[2], q);
+        float2 corr;
+        float norm;
+        if (table != nullptr) {
+          // x = k0 * oversample with k0 = lobe - off
+          const float x = ((float)q.lobe - q.off) * (float)oversample;
+          const float fb = floorf(x);
+          const float t = x - fb;
+          const int base = (int)fb;
+          const float t2 = t * t, t3 = t2 * t;
+          const float wts[4] = {-0.5f * t + t2 - 0.5f * t3, 1.0f - 2.5f * t2 + 1.5f * t3,
+                                0.5f * t + 2.0f * t2 - 1.5f * t3, -0.5f * t2 + 0.5f * t3};
+          float2 v = make_float2(0.f, 0.f);
+          float nn = 0.0f;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        int k = (base + j - 1) % size;
-        if (k < 0) k += size;
-        const float2 tv = ldg2(table + (size_t)a * size + k);
-        v.x += wts[j] * tv.x;
-        v.y += wts[j] * tv.y;
-        nn += wts[j] * __ldg(norm_table + k);
-      }
-      corr = cmulc(q.rot, v);  // value * conj(rot)... conj(rot) * v
-      norm = fmaxf(nn, 0.0f);
-    } else {
-      float2 nu[P];
-      numerators<P>(q.off, nu);
-      float2 z = make_float2(0.f, 0.f);
-      float n0 = 0.0f;
-      const float* tb = tbl + (c.N - 1 - q.lobe);
-      const float2* row = res + (size_t)a * c.K;
-      for (int k = 0; k < c.K; ++k) {
-        float2 D;
-        if (k == q.lobe) {
-          float2 d1;
-          dirichlet_near(q.off, c.S, c.N, D, d1);
+          for (int i = 0; i < 4; ++i) {
+            int k = (base + i - 1) % size;
+            if (k < 0) k += size;
+            const float2 tv = ldg2(table + (size_t)a * size + k);
+            v.x += wts[i] * tv.x;
+            v.y += wts[i] * tv.y;
+            nn += wts[i] * __ldg(norm_table + k);
+          }
+          corr = cmulc(q.rot, v);  // conj(rot) * v
+          norm = fmaxf(nn, 0.0f);
         } else {
-          const float cot = cot_from(tb[k], q.tl);
-          D = cscale(cmul(nu[(k - q.lobe) & (P - 1)], make_float2(cot, 1.0f)), c.inv_S);
+          float2 nu[P];
+          numerators<P>(q.off, nu);
+          float2 z = make_float2(0.f, 0.f);
+          float n0 = 0.0f;
+          const float* tb = tbl + (c.N - 1 - q.lobe);
+          const float2* row = res + (size_t)a * c.K;
+          for (int k = 0; k < c.K; ++k) {
+            float2 D;
+            if (k == q.lobe) {
+              float2 d1;
+              dirichlet_near(q.off, c.S, c.N, D, d1);
+            } else {
+              const float cot = cot_from(tb[k], q.tl);
+              D = cscale(cmul(nu[(k - q.lobe) & (P - 1)], make_float2(cot, 1.0f)), c.inv_S);
+            }
+            z = cadd(z, cmulc(D, ldg2(row + k)));
+            n0 += D.x * D.x + D.y * D.y;
+          }
+          corr = cmulc(q.rot, z);
+          norm = n0;
         }
-        z = cadd(z, cmulc(D, ldg2(row + k)));
-        n0 += D.x * D.x + D.y * D.y;
+        *reinterpret_cast<float4*>(rec + lane * kOrientRec) =
+            make_float4(q.ux, q.uy, q.uz, c.amp_scale * q.inv_r);
+        *reinterpret_cast<float4*>(rec + lane * kOrientRec + 4) = make_float4(corr.x, corr.y, norm, 0.0f);
       }
-      corr = cmulc(q.rot, z);
-      norm = n0;
-    }
-#pragma unroll
-    for (int j = 0; j < kBankChunk; ++j) {
-      if (j < nj) {
-        const bool self = (j_begin + j) == 0;
-        const float ex = self ? own[0] : bk[3 * j];
-        const float ey = self ? own[1] : bk[3 * j + 1];
-        const float ez = self ? own[2] : bk[3 * j + 2];
-        const float cosv = q.ux * ex + q.uy * ey + q.uz * ez;
-        float amp, amp_cos;
-        scattering(c, cosv, q.inv_r, amp, amp_cos);
-        acc[j][0] += amp * corr.x;
-        acc[j][1] += amp * corr.y;
-        acc[j][2] += amp * amp * norm;
+      __syncwarp();
+      const int count = min(32, A - a0);
+#pragma unroll 4
+      for (int i = 0; i < count; ++i) {
+        const float4 g = *reinterpret_cast<const float4*>(rec + i * kOrientRec);
+        const float4 v = *reinterpret_cast<const float4*>(rec + i * kOrientRec + 4);
+        const float cosv = g.x * ex + g.y * ey + g.z * ez;
+        const float amp = bank_amplitude<FRESNEL>(c, cosv, g.w);
+        acc0 += amp * v.x;
+        acc1 += amp * v.y;
+        acc2 += amp * amp * v.z;
       }
+      __syncwarp();
     }
-  }
-  float* o = out + (size_t)s * (bank_size + 1) * 3;
-#pragma unroll
-  for (int j = 0; j < kBankChunk; ++j) {
-    if (j < nj) {
-      o[3 * (j_begin + j)] = acc[j][0];
-      o[3 * (j_begin + j) + 1] = acc[j][1];
-      o[3 * (j_begin + j) + 2] = acc[j][2];
+    if (j < normals) {
+      o[3 * j] = acc0;
+      o[3 * j + 1] = acc1;
+      o[3 * j + 2] = acc2;
     }
   }
 }
@@ -1003,12 +1031,15 @@ struct OrientLaunch {
   cudaStream_t st;
   template <int P>
   int run() {
-    const size_t smem = (table_floats(c.N, c.K) + 3 * kBankChunk) * sizeof(float);
-    for (int j0 = 0; j0 < nb + 1; j0 += kBankChunk) {
-      orientations_kernel<P><<<(C + 127) / 128, 128, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
-                                                                 j0, res, table, ntab, ov, out);
-      dsg_count_launches(1);
-    }
+    const size_t smem = (((c.N + c.K + 3) & ~3) + kOrientWarps * 32 * kOrientRec) * sizeof(float);
+    const dim3 grid((C + kOrientWarps - 1) / kOrientWarps);
+    if (c.fresnel_n > 1.0f)
+      orientations_kernel<P, true><<<grid, kOrientWarps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
+                                                                          res, table, ntab, ov, out);
+    else
+      orientations_kernel<P, false><<<grid, kOrientWarps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
+                                                                           res, table, ntab, ov, out);
+    dsg_count_launches(1);
     return launch_status();
   }
 };

@@ -134,6 +134,9 @@ def append_projected(store, config, positions, params, basis, fresnel_n, status)
     centers = params["centers"].to(torch.float32).contiguous()
     normals = params["normals"].to(torch.float32).contiguous()
     areas = params["areas"].to(torch.float32).contiguous()
+    # logical FP32 flops of the projection U [rank2, 2K] . v over every aperture-surfel pair
+    lib.add_work("dsg_design_project_bf16x3",
+                 float(len(positions)) * len(centers) * 2 * (2 * config.num_range_bins) * rank2)  # fmt: skip
     call(
         "dsg_design_project_bf16x3", lib.chirp(config, fresnel_n), ptr(positions), len(positions),
         ptr(centers), ptr(normals), ptr(areas), len(centers), ptr(hi), ptr(lo), rank2, ptr(store.hi),

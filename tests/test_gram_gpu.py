@@ -98,3 +98,52 @@ def test_fused_design_projection_gram_matches_the_fp32_stream(pad):
     scale = float(plain[0].abs().max())
     assert float((mixed[0] - plain[0]).abs().max()) < 1e-4 * scale
     assert float((mixed[1] - plain[1]).abs().max()) < 1e-4 * float(plain[1].abs().max())
+
+
+@pytest.mark.parametrize("pad,rank2,surfels", [(2, 56, 300), (2, 2, 1), (4, 100, 129), (1, 128, 257), (2, 34, 128)])
+def test_design_projection_matches_float64(pad, rank2, surfels):
+    """dsg_design_project_bf16x3 straight through the C ABI against the float64 oracle:
+    PT[s, offset + a rank2 + rho] = sum_j U[rho, j] v_{a,s}[j], v the real dictionary row
+    (re, im interleaved per bin) including sqrt(area). Partial tiles, ranks that are not a
+    multiple of 32 and a nonzero column offset all appear."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+    from conftest import aperture_grid, surfels as make_surfels
+    from dsplat import FMCWConfig
+    from dsplat.kernels import _lib
+    from dsplat.kernels.gram import split_basis
+
+    from oracle import fmcw as ofmcw
+
+    config = FMCWConfig(pad_factor=pad, adc_samples=256 // pad)  # 128 range bins
+    K = config.num_range_bins
+    positions = aperture_grid(6)
+    params = make_surfels(surfels, seed=rank2)
+    A = len(positions)
+    generator = torch.Generator().manual_seed(rank2 + surfels)
+    basis = (torch.randn(rank2, 2 * K, generator=generator) / (2 * K) ** 0.5).cuda()
+    hi_u, lo_u = split_basis(basis)
+    offset = 6
+    ld = offset + A * rank2 + 4
+    pt_hi = torch.zeros((surfels, ld), dtype=torch.bfloat16, device="cuda")
+    pt_lo = torch.zeros_like(pt_hi)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("dsg_design_project_bf16x3", _lib.chirp(config, 0.0), _lib.ptr(positions), A,
+              _lib.ptr(params["centers"]), _lib.ptr(params["normals"]), _lib.ptr(params["areas"]), surfels,
+              _lib.ptr(hi_u), _lib.ptr(lo_u), rank2, _lib.ptr(pt_hi), _lib.ptr(pt_lo), ld, offset,
+              _lib.ptr(status), _lib.stream(positions.device))  # fmt: skip
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    got = (pt_hi.double() + pt_lo.double()).cpu()
+    rows = ofmcw.design(config, positions.cpu(), params["centers"].cpu(), params["normals"].cpu(),
+                        params["areas"].cpu(), real=True)  # [2K A, S], row j A + a
+    v = rows.reshape(2 * K, A, surfels)
+    expected = torch.einsum("rj,jas->sar", basis.cpu().double(), v).reshape(surfels, A * rank2)
+    block = got[:, offset : offset + A * rank2]
+    scale = float(expected.abs().max())
+    assert float((block - expected).abs().max()) < 5e-5 * scale
+    assert float((block - expected).norm() / expected.norm()) < 2e-5
+    # Columns outside the block are never written.
+    assert float(got[:, :offset].abs().max()) == 0.0 and float(got[:, offset + A * rank2 :].abs().max()) == 0.0

@@ -253,3 +253,37 @@ def test_normal_bank_scores_match_the_oracle(fmcw):
     close(tn, on, 1e-4)
     close(tc, ec, 3e-2)  # the FFT table approximates the exact scores (reference bound)
     close(tn, en, 3e-2)
+
+
+def test_normal_bank_scores_ragged_sizes_and_fresnel():
+    """49 apertures (a partial aperture chunk), 41 bank normals (two normal chunks), 37
+    candidates (a partial block) and a Fresnel factor, exact and table paths."""
+    from dsplat import FMCWConfig, FMCWModel, Scan
+    from dsplat.certificate import fibonacci_sphere
+    from dsplat.kernels import surfel as kernel
+
+    config = FMCWConfig()
+    positions = aperture_grid(7)
+    truth = surfels(4, seed=21)
+    weights = torch.tensor([1.0, -0.5, 0.7, 0.3], device="cuda").to(torch.complex64)
+    empty = Scan(torch.zeros((len(positions), config.num_range_bins), dtype=torch.complex64, device="cuda"),
+                 positions, config)  # fmt: skip
+    residual = FMCWModel(empty, fresnel_n=1.5).render(truth, weights)
+    model = FMCWModel(Scan(residual, positions, config), fresnel_n=1.5)
+    candidates = surfels(37, seed=22)
+    bank = fibonacci_sphere(40, "cuda")
+    corr, norm = kernel.correlate_orientations(config, positions, candidates["centers"], candidates["normals"],
+                                               bank, residual, 1.5)  # fmt: skip
+    ec, en = ofmcw.correlate_orientations(config, positions.cpu(), candidates["centers"].cpu(),
+                                          candidates["normals"].cpu(), bank.cpu(), residual.cpu(), 1.5)  # fmt: skip
+    assert corr.shape == (37, 41) and norm.shape == (37, 41)
+    close(corr, ec, 1e-5)
+    close(norm, en, 1e-5)
+    table = model.range_table(residual, 8)
+    tc, tn = kernel.correlate_orientations(config, positions, candidates["centers"], candidates["normals"],
+                                           bank, residual, 1.5, table)  # fmt: skip
+    oc, on = ofmcw.correlate_orientations(
+        config, positions.cpu(), candidates["centers"].cpu(), candidates["normals"].cpu(), bank.cpu(),
+        residual.cpu(), 1.5, table=(table.correlation.cpu(), table.norm.cpu(), 8))  # fmt: skip
+    close(tc, oc, 1e-4)
+    close(tn, on, 1e-4)
