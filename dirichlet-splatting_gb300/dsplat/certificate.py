@@ -17,14 +17,18 @@ import torch
 from .kernels import search
 
 
-def certificate(model, params, residual, mode, *, gradient=False, normals=False):
+def certificate(model, params, residual, mode, *, gradient=False, normals=False, active=None):
     """Squared normalized certificate per atom, optionally with its explicit gradient.
 
     The gradient is by centers, and by normals too when normals is set. The small
     per-candidate algebra runs in double so the 1e-60 norm floor is representable.
+    active (count tensor, period) lets the model skip atoms whose index mod period is not
+    below count; their values are then meaningless and must be masked by the caller.
     """
     if gradient:
         c, n, dc, dn = model.correlate_gradient(params, residual, include_normals=normals)
+    elif active is not None:
+        c, n = model.correlate(params, residual, active=active)
     else:
         c, n = model.correlate(params, residual)
     c, n = c.to(torch.complex128), n.double().clamp(min=1e-60)
@@ -161,9 +165,9 @@ def search_certificate(
         ]
         return -torch.cat(parts, -1)
 
-    def score(params, gradient=False):
+    def score(params, gradient=False, active=None):
         return certificate(model, params, residual, mode, gradient=gradient,
-                           normals="normals" in specs)  # fmt: skip
+                           normals="normals" in specs, active=active)  # fmt: skip
 
     coarse_scores = score(feasible) if initial_scores is None else initial_scores
     ids = select_peaks(coarse_scores, feasible["centers"], config.peaks, config.separation)
@@ -276,22 +280,40 @@ def _graphed_ascent(iterate, iterations, params, value, grad, inverse):
 
 
 def _backtrack_batched(old, direction, controls, fractions, value, specs, score):
-    """All backtracking trials of one iteration scored together; no host synchronization.
+    """All backtracking trials of one iteration scored without host synchronization.
 
     Each candidate takes the first (largest) fraction whose finite score exceeds value.
+    The full step is scored for every candidate; the smaller fractions only for those the
+    full step did not improve, compacted to the front of each fraction's block, with the
+    pending count kept on the device (score(batch, active=(count, period)) skips the rest).
     """
     count = len(old["centers"])
     trials = [search.trial(old["centers"], old["normals"], direction, controls, f) for f in fractions]
     centers = torch.stack([c for c, _ in trials])  # [B, count, 3]
     normals = torch.stack([n for _, n in trials])
-    batch = {key: v.repeat(len(fractions), *([1] * (v.ndim - 1))) for key, v in old.items()}
-    batch["centers"] = centers.reshape(-1, 3)
-    batch["normals"] = normals.reshape(-1, 3)
-    values = score(batch).reshape(len(fractions), count)
-    improve = torch.isfinite(values) & (values > value[None])
-    accepted = improve.any(0)
-    first = improve.to(torch.int8).argmax(0)  # first True; 0 where none
-    rows = torch.arange(count, device=first.device)
+    first_values = score(dict(old, centers=centers[0], normals=normals[0]))
+    improve_first = torch.isfinite(first_values) & (first_values > value)
+    rows = torch.arange(count, device=value.device)
+    if len(fractions) > 1:
+        # Pending candidates first (stable), the improved ones after them.
+        order = torch.argsort(improve_first.to(torch.int8), stable=True)
+        pending = (~improve_first).sum().to(torch.int32).reshape(1)
+        rest = len(fractions) - 1
+        batch = {key: v[order].repeat(rest, *([1] * (v.ndim - 1))) for key, v in old.items()}
+        batch["centers"] = centers[1:, order].reshape(-1, 3)
+        batch["normals"] = normals[1:, order].reshape(-1, 3)
+        values = score(batch, active=(pending, count)).reshape(rest, count)
+        live = rows[None] < pending  # compacted position holds a pending candidate
+        improve = torch.isfinite(values) & (values > value[order][None]) & live
+        later = improve.any(0)
+        step = improve.to(torch.int8).argmax(0) + 1  # fraction index, compacted order
+        accepted_later = torch.zeros_like(improve_first).scatter(0, order, later)
+        fraction_later = torch.zeros_like(rows).scatter(0, order, step)
+    else:
+        accepted_later = torch.zeros_like(improve_first)
+        fraction_later = torch.zeros_like(rows)
+    accepted = improve_first | accepted_later
+    first = torch.where(improve_first, 0, fraction_later)
     params = dict(old)
     keep = accepted[:, None]
     if "centers" in specs:

@@ -319,8 +319,24 @@ __global__ void __launch_bounds__(128) reduce_kernel(Consts c, const float* __re
                                                      const float2* __restrict__ w, int S,
                                                      const float2* __restrict__ res,
                                                      int chunk_len, int chunks,
-                                                     float* __restrict__ partial) {
+                                                     float* __restrict__ partial,
+                                                     const int* __restrict__ active, int period) {
   constexpr int NV = ModeInfo<MODE>::NV;
+  // Optional active set: surfel s counts only when s mod period < *active. A CTA without
+  // any active surfel writes zero partials and leaves (the same decision in every thread).
+  if (active != nullptr) {
+    const int limit = __ldg(active);
+    const int s0 = blockIdx.x * kWarps * 4;
+    bool any = false;
+    for (int j = 0; j < kWarps * 4 && !any; ++j) any = s0 + j < S && (s0 + j) % period < limit;
+    if (!any) {
+      for (int i = threadIdx.x; i < kWarps * 4 * NV; i += blockDim.x) {
+        const int t = s0 + i / NV;
+        if (t < S) partial[((size_t)t * chunks + blockIdx.y) * NV + i % NV] = 0.0f;
+      }
+      return;
+    }
+  }
   constexpr bool kGrad = MODE == 1 || MODE == 2;
   constexpr bool kNorm = MODE != 3;
   constexpr bool kDeriv = MODE != 0;
@@ -545,9 +561,11 @@ __global__ void __launch_bounds__(128) reduce_kernel(Consts c, const float* __re
     __syncwarp();
   }
   if (lp == 0 && s_ok) {
+    // an inactive candidate of a CTA that had active ones still reports zeros
+    const bool live = active == nullptr || s % period < __ldg(active);
     float* p = partial + ((size_t)s * chunks + blockIdx.y) * NV;
 #pragma unroll
-    for (int v = 0; v < NV; ++v) p[v] = accv[v];
+    for (int v = 0; v < NV; ++v) p[v] = live ? accv[v] : 0.0f;
   }
 }
 
@@ -982,6 +1000,7 @@ template <int MODE>
 struct ReduceLaunch {
   Consts c; const float* pos; int A; const float* cen; const float* nrm; const float2* w; int S;
   const float2* res; float* partial; float* o0; float* o1; float* o2; float* o3; cudaStream_t st;
+  const int* active = nullptr; int period = 1;
   template <int BPL, int P>
   int run() {
     constexpr int REC = reduce_record<P>();
@@ -992,7 +1011,7 @@ struct ReduceLaunch {
     const int chunk_len = ((A + chunks - 1) / chunks + 7) / 8 * 8;
     const int nch = (A + chunk_len - 1) / chunk_len;
     dim3 grid((S + 15) / 16, nch);
-    kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, res, chunk_len, nch, partial);
+    kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, res, chunk_len, nch, partial, active, period);
     chunk_sum_kernel<MODE><<<(S + 127) / 128, 128, 0, st>>>(partial, S, nch, o0, o1, o2, o3);
     dsg_count_launches(2);
     return launch_status();
@@ -1165,6 +1184,29 @@ int dsg_surfel_correlate(const DsgChirp* chirp, const float* positions, int32_t 
                          size_t workspace_bytes, void* stream) {
   return reduce_common(0, chirp, positions, apertures, centers, normals, nullptr, candidates,
                        residual, corr, norm, nullptr, nullptr, workspace, workspace_bytes, stream);
+}
+
+int dsg_surfel_correlate_active(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                                const float* centers, const float* normals, int32_t candidates,
+                                const float* residual, const int32_t* active, int32_t period,
+                                float* corr, float* norm, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || candidates < 0 || period < 1 || !active) return DSG_ERR_ARGUMENT;
+  if (candidates == 0) return DSG_OK;
+  if (apertures == 0)
+    return reduce_common(0, chirp, positions, apertures, centers, normals, nullptr, candidates,
+                         residual, corr, norm, nullptr, nullptr, workspace, workspace_bytes, stream);
+  if (!positions || !residual || !centers || !normals || !corr || !norm) return DSG_ERR_ARGUMENT;
+  const size_t need = dsg_surfel_reduce_workspace_bytes(chirp, apertures, candidates, 3);
+  if (workspace == nullptr || workspace_bytes < need) return DSG_ERR_WORKSPACE;
+  const Consts c = make_consts(*chirp);
+  ReduceLaunch<0> L{c, positions, apertures, centers, normals, nullptr, candidates,
+                    reinterpret_cast<const float2*>(residual), reinterpret_cast<float*>(workspace),
+                    corr, norm, nullptr, nullptr, (cudaStream_t)stream};
+  L.active = active;
+  L.period = period;
+  return dispatch_kp(c.K, c.P, L);
 }
 
 int dsg_surfel_correlate_gradient(const DsgChirp* chirp, const float* positions,

@@ -292,8 +292,8 @@ class FMCWModel:
     def vjp(self, params, coefficients, upstream):
         return surfel.vjp(*self.sensor, params, coefficients, upstream, self.fresnel_n)
 
-    def correlate(self, params, residual):
-        return surfel.correlate(*self.sensor, params, residual.reshape(self.shape), self.fresnel_n)
+    def correlate(self, params, residual, active=None):
+        return surfel.correlate(*self.sensor, params, residual.reshape(self.shape), self.fresnel_n, active)
 
     def correlate_gradient(self, params, residual, include_normals=False):
         return surfel.correlate_gradient(

@@ -69,6 +69,7 @@ SIGNATURES = {
     "dsg_surfel_vjp": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, P, P, P, SZ, P]),
     "dsg_surfel_vjp_fixed_scratch": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, P, P, P]),
     "dsg_surfel_correlate": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, P, P, SZ, P]),
+    "dsg_surfel_correlate_active": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, I32, P, P, P, SZ, P]),
     "dsg_surfel_correlate_gradient": (
         ctypes.c_int,
         [CP, P, I32, P, P, I32, P, I32, P, P, P, P, P, SZ, P],
@@ -87,6 +88,8 @@ SIGNATURES = {
     "dsg_range_gate": (ctypes.c_int, [P, I32, P, I32, P, I32, F32, I32, P, P]),
     "dsg_peaks": (ctypes.c_int, [P, P, P, I32, I32, I32, F32, P, P]),
     "dsg_distinct": (ctypes.c_int, [P, P, P, I32, I32, P, I32, P, F32, I32, P, P, P]),
+    "dsg_elimination_workspace_bytes": (SZ, [I32, I32, I32]),
+    "dsg_backward_elimination": (ctypes.c_int, [P, P, I32, I32, P, I64, I32, P, SZ, P, P]),
     "dsg_direction": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P]),
     "dsg_trial": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P, P]),
     "dsg_energy_workspace_bytes": (SZ, [I64]),

@@ -82,3 +82,24 @@ def trial(centers, normals, direction, controls, fraction):
         width, float(fraction), ptr(out_centers), ptr(out_normals), _lib.stream(centers.device),
     )  # fmt: skip
     return out_centers, out_normals
+
+
+def backward_elimination(inverse, rhs, count, limited=None, limit=0):
+    """Removal order of backward elimination from the float64 inverse (dsg_backward_elimination)."""
+    n = len(inverse)
+    device = inverse.device
+    removed = torch.empty((count,), dtype=torch.long, device=device)
+    if count == 0:
+        return removed
+    complex_mode = inverse.is_complex()
+    dtype = torch.complex128 if complex_mode else torch.float64
+    w = inverse.to(dtype).contiguous()
+    q = rhs.to(dtype).contiguous()
+    lim = None if limited is None else limited.to(torch.uint8).contiguous()
+    nbytes = _lib.query("dsg_elimination_workspace_bytes", n, count, int(complex_mode))
+    work, nbytes = _lib.workspace(nbytes, device)
+    call(
+        "dsg_backward_elimination", ptr(w), ptr(q), n, count, None if lim is None else ptr(lim),
+        int(limit), int(complex_mode), ptr(work), nbytes, ptr(removed), _lib.stream(device),
+    )  # fmt: skip
+    return removed

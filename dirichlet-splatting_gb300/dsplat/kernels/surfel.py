@@ -134,8 +134,12 @@ def jacobian(config, positions, centers, normals, fresnel_n):
     return torch.view_as_complex(cols), jac[..., :3], jac[..., 3:]
 
 
-def correlate(config, positions, centers, normals, residual, fresnel_n):
-    """conj(column) . residual and |column|^2 per candidate, without area."""
+def correlate(config, positions, centers, normals, residual, fresnel_n, active=None):
+    """conj(column) . residual and |column|^2 per candidate, without area.
+
+    active = (count, period), count an int32 device tensor of one element: only candidates
+    whose index mod period is below count are computed; the others get zeros.
+    """
     positions, centers, normals = f32(positions), f32(centers), f32(normals)
     r = real_view(residual)
     chirp = _lib.chirp(config, fresnel_n)
@@ -143,10 +147,18 @@ def correlate(config, positions, centers, normals, residual, fresnel_n):
     corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
     nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3)
     work, nbytes = _lib.workspace(nbytes, centers.device)
-    call(
-        "dsg_surfel_correlate", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
-        count, ptr(r), ptr(corr), ptr(norm), ptr(work), nbytes, _lib.stream(centers.device),
-    )  # fmt: skip
+    if active is None:
+        call(
+            "dsg_surfel_correlate", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
+            count, ptr(r), ptr(corr), ptr(norm), ptr(work), nbytes, _lib.stream(centers.device),
+        )  # fmt: skip
+    else:
+        limit, period = active
+        call(
+            "dsg_surfel_correlate_active", chirp, ptr(positions), apertures, ptr(centers),
+            ptr(normals), count, ptr(r), ptr(limit), int(period), ptr(corr), ptr(norm), ptr(work),
+            nbytes, _lib.stream(centers.device),
+        )  # fmt: skip
     return torch.view_as_complex(corr), norm
 
 

@@ -100,18 +100,19 @@ def regularized_inverse(h, floor):
     return None if factor is None else torch.cholesky_inverse(factor)
 
 
-def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, captured=False):
+def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, on_device=False):
     """Remove count unknowns one at a time from the least squares with this inverse.
 
     With W the inverse of the current system and b = W q, deleting unknown j and
     refitting raises the objective by |b_j|^2 / W_jj; each step deletes the cheapest
     and continues with W - w w^H / W_jj (w = W[:, j]), kept as rank-one corrections.
     At most limit of the unknowns marked in limited are removed. Returns the removed
-    indices in order. captured replays the loop from a CUDA graph (one per shape),
-    which removes the per-step launch overhead; the arithmetic is the same.
+    indices in order. on_device runs the loop as two small CUDA kernels per step
+    (dsg_backward_elimination) instead of about ten PyTorch launches; the arithmetic is
+    the same up to the order of the float64 sums.
     """
-    if captured and inverse.is_cuda:
-        return _captured_elimination(inverse, rhs, count, limited, limit)
+    if on_device and inverse.is_cuda:
+        return search.backward_elimination(inverse, rhs, count, limited, limit)
     size = len(inverse)
     b = inverse @ rhs.to(inverse.dtype)
     diagonal = inverse.diagonal().real.clone()
@@ -141,35 +142,6 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, captured
         if limited is not None:
             spent = spent + limited.index_select(0, index)[0]
     return removed
-
-
-_GRAPHS: dict = {}
-
-
-def _captured_elimination(inverse, rhs, count, limited, limit):
-    """backward_elimination replayed from a cached CUDA graph keyed by shape and limit."""
-    key = (tuple(inverse.shape), inverse.dtype, inverse.device, count, limited is not None, int(limit))
-    entry = _GRAPHS.get(key)
-    if entry is None:
-        static = (inverse.clone(), rhs.to(inverse.dtype).clone(),
-                  None if limited is None else limited.clone())  # fmt: skip
-        side = torch.cuda.Stream(inverse.device)
-        side.wait_stream(torch.cuda.current_stream(inverse.device))
-        with torch.cuda.stream(side):  # warm-up outside capture
-            backward_elimination(static[0], static[1], count, static[2], limit)
-        torch.cuda.current_stream(inverse.device).wait_stream(side)
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph):
-            removed = backward_elimination(static[0], static[1], count, static[2], limit)
-        entry = (graph, static, removed)
-        _GRAPHS[key] = entry
-    graph, static, removed = entry
-    static[0].copy_(inverse)
-    static[1].copy_(rhs.to(inverse.dtype))
-    if limited is not None:
-        static[2].copy_(limited)
-    graph.replay()
-    return removed.clone()
 
 
 def _distinct(scores, points, occupied, period, separation, width):
@@ -305,7 +277,7 @@ def merge_support(state, config, pool, scores=None):
     while True:
         with stage("replace.elimination"):
             removed = backward_elimination(inverse, q, len(chosen), None if limit is None else old,
-                                           limit or 0, captured=getattr(config, "batched", False))  # fmt: skip
+                                           limit or 0, on_device=getattr(config, "batched", False))  # fmt: skip
         gone = torch.zeros(len(q), device=q.device, dtype=torch.bool)
         gone[removed] = True
         owners = gone[:count].nonzero().flatten()

@@ -85,8 +85,11 @@ class SpectralModel:
         )
         return {"centers": gc}, gb
 
-    def correlate(self, params, residual):
-        """a^H r and |a|^2 of every atom; an FFT when the atoms are exactly the grid bins."""
+    def correlate(self, params, residual, active=None):
+        """a^H r and |a|^2 of every atom; an FFT when the atoms are exactly the grid bins.
+
+        active is accepted for the FMCW model's interface and ignored: every atom is scored.
+        """
         centers = params["centers"]
         bins = self.grid.bins(centers.device)
         if centers.shape == bins.shape and torch.equal(centers, bins):

@@ -68,10 +68,14 @@ def jacobian(config, positions, params, fresnel_n=0.0):
     }
 
 
-def correlate(config, positions, params, residual, fresnel_n=0.0):
-    """a^H r and |a|^2 of every surfel's column a against the residual profiles [A, K]."""
+def correlate(config, positions, params, residual, fresnel_n=0.0, active=None):
+    """a^H r and |a|^2 of every surfel's column a against the residual profiles [A, K].
+
+    active (count tensor, period) restricts the work to surfels whose index mod period is
+    below count (the others return zeros).
+    """
     corr, norm = kernel.correlate(
-        config, positions, params["centers"], params["normals"], residual, fresnel_n
+        config, positions, params["centers"], params["normals"], residual, fresnel_n, active
     )
     return corr * params["areas"].sqrt(), norm * params["areas"]
 

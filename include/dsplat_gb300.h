@@ -128,6 +128,18 @@ int dsg_surfel_correlate(const DsgChirp* chirp, const float* positions, int32_t 
                          const float* residual, float* corr, float* norm, void* workspace,
                          size_t workspace_bytes, void* stream);
 
+/* dsg_surfel_correlate restricted to an active set held on the device: candidate s is
+ * computed when s mod period < *active, and the others get corr = norm = 0. No counterpart
+ * in the reference: its batched certificate search (dsplat/certificate.py, the backtracking
+ * of search_certificate) scores every trial step; here the later backtracking fractions are
+ * scored only for the candidates the first fraction did not improve, compacted to the
+ * front of each period, without reading the count back to the host. */
+int dsg_surfel_correlate_active(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                                const float* centers, const float* normals, int32_t candidates,
+                                const float* residual, const int32_t* active, int32_t period,
+                                float* corr, float* norm, void* workspace, size_t workspace_bytes,
+                                void* stream);
+
 /* correlate plus derivatives by centers (and normals) (reference:
  * dsplat/kernels/surfel.py:293-315 correlate_gradient). width = 3 or 6.
  * corr [C] complex, norm [C], dcorr [C,width] complex, dnorm [C,width]. */
@@ -274,6 +286,20 @@ int dsg_split_transpose_bf16(const float* rows, int64_t m, int32_t n, int64_t co
 int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, int64_t k_pad,
                     int32_t column_from, int32_t k_splits, double* out, int32_t ldo,
                     int32_t* status, void* stream);
+
+/* Workspace of dsg_backward_elimination, in bytes. */
+size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_complex);
+
+/* Backward elimination of the merged replacement (reference: dsplat/replacement.py:104-140,
+ * backward_elimination): with the float64 inverse W [n,n] (complex128 when is_complex,
+ * row-major) of the pooled system and its right-hand side q [n], remove count unknowns one
+ * at a time, each the cheapest |b_j|^2 / W_jj (b = W q) of those still allowed, continuing
+ * with the rank-one-updated inverse; at most limit of the unknowns with limited[j] != 0
+ * (uint8 [n], or NULL for no limit) are removed. removed [count] (int64) receives the
+ * indices in order. Launches 1 + 2 count kernels; ties go to the lowest index. */
+int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, int32_t count,
+                             const uint8_t* limited, int64_t limit, int32_t is_complex, void* workspace,
+                             size_t workspace_bytes, int64_t* removed, void* stream);
 
 #ifdef __cplusplus
 }

@@ -8,8 +8,13 @@ The reference's Python solver (dsplat/dsfw.py, varpro.py, replacement.py,
 refinement.py, certificate.py, parameters.py, fmcw.py, spectral.py) runs unmodified;
 only its kernel-binding modules (dsplat/kernels/*.py, which launch Slang through
 slangtorch and need a GPU) are replaced, before import, by float64 CPU restatements
-from this repository's oracle/. The histories go to tests/golden/reference_fits.json;
-tests/test_fits_gpu.py runs the same scenes through the GB300 package and compares.
+from this repository's oracle/, and the products it would compute on the GPU keep
+their GPU arithmetic: the cuBLAS SSYRK of the normal equations accumulates in float32,
+and the Gauss-Newton probe signs are the draws of a CUDA generator (recorded by
+record_cuda_signs.py into cuda_rademacher.npz), not of the CPU generator. Two more runs
+perturb every model-kernel output by relative noise of 1e-6 and 1e-5 and record how far
+the trajectory moves ("spread"). The records go to tests/golden/reference_fits.json;
+tests/test_fits_gpu.py runs the same scenes through the GB300 package on CUDA.
 """
 
 from __future__ import annotations
@@ -19,11 +24,38 @@ import sys
 import types
 from pathlib import Path
 
+import numpy as np
 import torch
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 DEFAULT_REFERENCE = Path("/root/reference")
+
+
+# Relative perturbation of every model-kernel output (0: exact oracle values). Runs with
+# a small perturbation show how far the reference's own trajectory moves under the
+# rounding noise that float32 kernels bring; the tests allow that spread.
+NOISE = {"scale": 0.0, "generator": torch.Generator().manual_seed(0)}
+
+
+def _perturb(value):
+    if isinstance(value, tuple):
+        return tuple(_perturb(v) for v in value)
+    if not isinstance(value, torch.Tensor) or NOISE["scale"] == 0.0 or not value.is_floating_point() and not value.is_complex():
+        return value
+    g = NOISE["generator"]
+    noise = torch.randn(value.shape, generator=g, dtype=torch.float64)
+    if value.is_complex():
+        noise = torch.complex(noise, torch.randn(value.shape, generator=g, dtype=torch.float64))
+    return (value.to(noise.dtype) * (1 + NOISE["scale"] * noise)).to(value.dtype)
+
+
+def _perturbed(fn):
+    def wrapper(*args, **kwargs):
+        return _perturb(fn(*args, **kwargs))
+
+    wrapper.__name__ = fn.__name__
+    return wrapper
 
 
 def _shim_modules():
@@ -97,6 +129,11 @@ def _shim_modules():
 
     spectral.vjp = spectral_vjp
 
+    for module in (surfel, spectral):
+        for name in [n for n in vars(module) if not n.startswith("_")]:
+            if callable(getattr(module, name)):
+                setattr(module, name, _perturbed(getattr(module, name)))
+
     search = types.ModuleType("dsplat.kernels.search")
     search.range_gate = osearch.range_gate
     search.peaks = lambda scores, centers, count, separation: osearch.peaks(scores, centers, count, separation)
@@ -115,11 +152,46 @@ def _shim_modules():
     cublas = types.ModuleType("dsplat.kernels.cublas")
 
     def syrk(rows, out):
-        out += torch.triu(rows.double().T @ rows.double()).to(out.dtype)
+        # cublasSsyrk_v2 accumulates in float32; so does this product (float32 CPU GEMM).
+        out += torch.triu(rows.float().T @ rows.float()).to(out.dtype)
 
     cublas.syrk = syrk
     return {"surfel": surfel, "spectral": spectral, "search": search, "reduce": reduce,
             "response": response, "cublas": cublas}  # fmt: skip
+
+
+class _RecordedGenerator:
+    """A CUDA generator stand-in whose randint draws come from cuda_rademacher.npz."""
+
+    def __init__(self, device=None):
+        self.seed, self.calls = None, 0
+
+    def manual_seed(self, seed):
+        self.seed, self.calls = int(seed), 0
+        return self
+
+
+class _TorchWithCudaDraws(types.ModuleType):
+    """torch for the reference's refinement module, except Generator and randint."""
+
+    def __init__(self, draws):
+        super().__init__("torch")
+        self._draws = draws
+        self.Generator = _RecordedGenerator
+
+    def __getattr__(self, name):
+        return getattr(torch, name)
+
+    def randint(self, low, high, size, *, device=None, generator=None, **kwargs):
+        if not isinstance(generator, _RecordedGenerator):
+            return torch.randint(low, high, size, device=device, generator=generator, **kwargs)
+        assert (low, high) == (0, 2) and size[-1] == 2, (low, high, size)
+        count = int(np.prod(size))
+        bits = np.unpackbits(self._draws[f"s{generator.seed}_{size[0]}x{size[1]}"])
+        draw = bits[generator.calls * count : (generator.calls + 1) * count]
+        assert len(draw) == count, "more recorded draws needed"
+        generator.calls += 1
+        return torch.as_tensor(draw.reshape(size), dtype=torch.int64, device=device)
 
 
 def import_reference(root: Path):
@@ -138,6 +210,10 @@ def import_reference(root: Path):
 
     dsplat.certificate.candidate_grid.__defaults__ = ("cpu",)
     dsplat.certificate.fibonacci_sphere.__defaults__ = ("cpu",)
+    # The Gauss-Newton probe signs are the ones a CUDA generator draws (record_cuda_signs.py).
+    import dsplat.refinement  # noqa: E402
+
+    dsplat.refinement.torch = _TorchWithCudaDraws(np.load(HERE / "cuda_rademacher.npz"))
 
     assert dsplat.__file__.startswith(str(root))
     assert dsplat.surfel.kernel is sys.modules["dsplat.kernels.surfel"]
@@ -256,8 +332,31 @@ def run_scenes(dsplat, device="cpu", names=None):
     return results
 
 
+def _spread(runs):
+    """Per step: NMSE range and replacement counts over the runs; final-center scatter."""
+    first = runs[0]
+    steps = []
+    for i in range(len(first["history"])):
+        entries = [r["history"][i] for r in runs if i < len(r["history"])]
+        steps.append({"nmse_min": min(e["nmse"] for e in entries), "nmse_max": max(e["nmse"] for e in entries),
+                      "replaced": sorted({e.get("replaced", -1.0) for e in entries})})  # fmt: skip
+    base = torch.tensor(first["centers"], dtype=torch.float64)
+    scatter = max(float(torch.cdist(torch.tensor(r["centers"], dtype=torch.float64), base).min(1).values.max())
+                  for r in runs)  # fmt: skip
+    return {"steps": steps, "center_scatter_m": scatter}
+
+
 def main(root: Path) -> None:
-    results = run_scenes(import_reference(root), "cpu")
+    dsplat = import_reference(root)
+    results = run_scenes(dsplat, "cpu")
+    perturbed = []
+    for seed, scale in ((1, 1e-6), (2, 1e-5)):
+        NOISE["scale"], NOISE["generator"] = scale, torch.Generator().manual_seed(seed)
+        perturbed.append(run_scenes(dsplat, "cpu"))
+    NOISE["scale"] = 0.0
+    for name, record in results.items():
+        record["spread"] = _spread([record] + [run[name] for run in perturbed])
+        record["spread"]["noise"] = [1e-6, 1e-5]
     (HERE / "reference_fits.json").write_text(json.dumps(results, indent=1))
     print("wrote", HERE / "reference_fits.json")
     for name, r in results.items():

@@ -32,20 +32,24 @@ def test_device_distinct_equals_the_sequential_selection(separation, period):
         assert got.tolist() == expected.tolist()
 
 
-def test_captured_elimination_equals_the_eager_loop():
+@pytest.mark.parametrize("complex_mode", [False, True])
+def test_device_elimination_equals_the_eager_loop(complex_mode):
+    """dsg_backward_elimination against the PyTorch loop: the same removal order, with and
+    without a limit on the marked unknowns, for a real and a Hermitian inverse."""
     from dsplat.replacement import backward_elimination
 
     generator = torch.Generator().manual_seed(5)
-    x = torch.randn(300, 60, generator=generator, dtype=torch.float64)
-    h = x.T @ x
-    q = x.T @ torch.randn(300, generator=generator, dtype=torch.float64)
+    dtype = torch.complex128 if complex_mode else torch.float64
+    x = torch.randn(300, 60, generator=generator, dtype=dtype)
+    h = x.mH @ x
+    q = x.mH @ torch.randn(300, generator=generator, dtype=dtype)
     inverse, q = torch.linalg.inv(h).cuda(), q.cuda()
     limited = torch.arange(60, device="cuda") < 40
     for lim, l in ((None, 0), (limited, 5)):
         eager = backward_elimination(inverse, q, 20, lim, l)
-        for _ in range(2):  # the second call replays the cached graph
-            captured = backward_elimination(inverse, q, 20, lim, l, captured=True)
-            assert torch.equal(eager, captured)
+        for _ in range(2):
+            device = backward_elimination(inverse, q, 20, lim, l, on_device=True)
+            assert torch.equal(eager, device)
 
 
 def test_batched_certificate_search_matches_the_sequential_search(fmcw):

@@ -7,9 +7,12 @@ oracle (tests/golden/make_golden_fits.py). The same scene code runs here through
 package on CUDA, so the records differ only by the implementation: float32 kernels in a
 different summation order against float64 ones.
 
-Bars: the replacement counts agree step by step; every step's NMSE agrees within 5 % of
-the reference's (or both sit below 1e-9, float32 round-off of an exact fit); and every
-final reference center has one of ours within 50 um (0.05 of a trust-region step).
+The reference itself is re-run with every model-kernel output perturbed by relative noise
+of 1e-6 and 1e-5 (the rounding of float32 kernels); "spread" records how far those runs
+move. Bars, step by step: the replacement count is one the reference runs produced; the
+NMSE lies within the reference runs' range widened by 5 % (or below 1e-9, float32
+round-off of an exact fit). Every final reference center has one of ours within 50 um or
+within twice the reference runs' own center scatter, whichever is larger.
 """
 
 from __future__ import annotations
@@ -43,15 +46,17 @@ def test_fit_follows_the_reference_solver(name):
     ours = _scenes()(dsplat, "cuda", names={name})[name]
     theirs = REFERENCE[name]
     assert len(ours["history"]) == len(theirs["history"])
-    for mine, ref in zip(ours["history"], theirs["history"], strict=True):
-        assert mine.get("replaced") == ref.get("replaced"), (name, mine, ref)
-        bar = NMSE_RELATIVE * ref["nmse"] + NMSE_FLOOR
-        assert abs(mine["nmse"] - ref["nmse"]) <= bar, (name, mine, ref)
+    spread = theirs["spread"]
+    for mine, ref, band in zip(ours["history"], theirs["history"], spread["steps"], strict=True):
+        assert mine.get("replaced", -1.0) in band["replaced"], (name, mine, ref, band)
+        low = band["nmse_min"] * (1 - NMSE_RELATIVE) - NMSE_FLOOR
+        high = band["nmse_max"] * (1 + NMSE_RELATIVE) + NMSE_FLOOR
+        assert low <= mine["nmse"] <= high, (name, mine, ref, band)
     mine_c = torch.tensor(ours["centers"], dtype=torch.float64)
     ref_c = torch.tensor(theirs["centers"], dtype=torch.float64)
     assert mine_c.shape == ref_c.shape
     nearest = torch.cdist(ref_c, mine_c).min(dim=1).values
-    assert float(nearest.max()) < CENTER_TOL_M, (name, nearest.tolist())
+    assert float(nearest.max()) < max(CENTER_TOL_M, 2 * spread["center_scatter_m"]), (name, nearest.tolist())
 
 
 def test_reference_records_are_complete():
@@ -61,3 +66,4 @@ def test_reference_records_are_complete():
     for record in REFERENCE.values():
         assert record["history"][0]["iteration"] == 0
         assert all("nmse" in e and "objective" in e for e in record["history"])
+        assert len(record["spread"]["steps"]) == len(record["history"])

@@ -287,3 +287,21 @@ def test_normal_bank_scores_ragged_sizes_and_fresnel():
         residual.cpu(), 1.5, table=(table.correlation.cpu(), table.norm.cpu(), 8))  # fmt: skip
     close(tc, oc, 1e-4)
     close(tn, on, 1e-4)
+
+
+def test_correlate_active_set_matches_the_full_launch(fmcw):
+    """dsg_surfel_correlate_active: candidates s with s mod period < count equal the full
+    correlate; the rest are zero. Three blocks of 70 candidates, 23 active per block."""
+    from dsplat.kernels import surfel as kernel
+
+    model, _, _ = fmcw
+    config, positions = model.sensor
+    residual = model.scan.data
+    cand = surfels(210, seed=31)
+    corr, norm = kernel.correlate(config, positions, cand["centers"], cand["normals"], residual, 0.0)
+    count = torch.tensor([23], dtype=torch.int32, device="cuda")
+    ac, an = kernel.correlate(config, positions, cand["centers"], cand["normals"], residual, 0.0,
+                              active=(count, 70))  # fmt: skip
+    live = torch.arange(210, device="cuda") % 70 < 23
+    assert torch.equal(ac[live], corr[live]) and torch.equal(an[live], norm[live])
+    assert float(ac[~live].abs().max()) == 0.0 and float(an[~live].abs().max()) == 0.0
