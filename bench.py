@@ -269,7 +269,10 @@ def run_ours(args, world, rank, local):
 TENSOR_KERNELS = ("dsg_gram_bf16x3", "dsg_design_project_bf16x3")
 # DRAM bytes (read + write) per logical flop, from ncu captures of smaller launches of the
 # same kernels, scaled to each launch by its work (see profiles/).
-TRAFFIC_PER_FLOP: dict = {}
+TRAFFIC_PER_FLOP = {
+    # profiles/design_project_bf16x3_2048ap_1000s.md: 327.3 MB of DRAM traffic for 48.2 GFLOP
+    "dsg_design_project_bf16x3": 327.3e6 / 48.2e9,
+}
 
 
 def _roofline(totals, timers, work, args):
