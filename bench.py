@@ -256,6 +256,7 @@ def run_ours(args, world, rank, local):
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "roofline": roofline,
+        "tensor_roofline": None if roofline and roofline["bound"] == "tensor" else _tensor_roofline(totals, timers, work),
         "kernel_ms": {k: round(v, 3) for k, v in sorted(totals.items(), key=lambda kv: -kv[1])},
         "stage_ms": stages,
         "fit": {"iteration": history["iteration"], "nmse": history["nmse"],
@@ -298,8 +299,30 @@ def _roofline(totals, timers, work, args):
                 "traffic": traffic and per_launch and round(traffic * per_launch),
                 "peak_source": f"{source} bf16_tflops_sustained / 3", "launches": launches,
                 "avg_ms": round(avg_ms, 4)}  # fmt: skip
+    flops = work.get(name)
+    if flops:
+        # FP32-issue-bound kernels (splat forward / JVP / VJP, certificate correlations, the
+        # normal bank): SURVEY-convention FP32 flops per pair-bin or pair-normal over the
+        # launches' time, against the nominal FP32 rate at the measured maximum SM clock
+        # (152 SMs x 128 lanes x 2 flops); the measured-peaks file has no FP32 figure.
+        mhz = peaks.get("sm_max_mhz", 2070.0)
+        peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+        achieved = flops / (totals[name] * 1e-3) / 1e12
+        return {"kernel": name, "bound": "fp32", "achieved": round(achieved, 2), "peak": round(peak, 1),
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "peak_source": f"nominal FP32 at {source} sm_max_mhz", "launches": launches,
+                "avg_ms": round(avg_ms, 4)}  # fmt: skip
     return {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": None, "traffic": None, "launches": launches, "avg_ms": round(avg_ms, 4)}  # fmt: skip
+
+
+def _tensor_roofline(totals, timers, work):
+    """The same figures for the tensor-core kernel with the largest time, when it is not the top."""
+    tensor = [k for k in TENSOR_KERNELS if k in totals]
+    if not tensor:
+        return None
+    name = max(tensor, key=totals.get)
+    return _roofline({name: totals[name]}, {name: timers[name]}, work, None)
 
 
 def cpu_baseline(threads=None, sample_stride=8):

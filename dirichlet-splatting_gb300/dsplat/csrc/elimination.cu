@@ -5,13 +5,14 @@
 // continues with W - w w^H / W_jj, w the current column j, kept as rank-one factors
 // U[t] = w_t / sqrt(pivot_t) so a step costs O(n * step).
 //
-// Two kernels per step on the caller's stream, in float64 (real or complex):
-//   pick_kernel   (one CTA) cost, masked argmin (first minimum; NaN counts as minimal, as
-//                 torch.argmin), the pivot W_jj - sum_t |U[t][j]|^2 and the bookkeeping;
-//   update_kernel (n / 32 CTAs) the column w_i = W_ij - sum_t U[t][i] conj(U[t][j]) with
-//                 the sum split over 8 warps, then b, U[step] and the diagonal.
-// The arithmetic is that of the reference's loop; only the order of the float64 sums in
-// the column differs.
+// One kernel per step on the caller's stream, in float64 (real or complex), after an
+// initial pick of the first unknown:
+//   step_kernel (n / 32 CTAs) the column w_i = W_ij - sum_t U[t][i] conj(U[t][j]) with the
+//   sum split over 8 warps, then b, U[step] and the diagonal, and each CTA's masked argmin
+//   of the next costs; the last CTA to finish (an atomic count, no waiting) reduces those,
+//   computes the next pivot W_jj - sum_t |U[t][j]|^2 and writes the next pick.
+// The argmin takes the first minimum and counts NaN as minimal, as torch.argmin. The
+// arithmetic is that of the reference's loop; only the order of the float64 sums differs.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -47,6 +48,10 @@ __device__ __forceinline__ double mul(double a, double b) { return a * b; }
 __device__ __forceinline__ Cplx mul(Cplx a, Cplx b) {
   return Cplx{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
 }
+// Loads that bypass L1 (values written by another CTA of the same launch).
+__device__ __forceinline__ double load_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ Cplx load_cg(const Cplx* p) { return Cplx{__ldcg(&p->x), __ldcg(&p->y)}; }
+
 template <typename T>
 __device__ __forceinline__ T zero();
 template <>
@@ -62,6 +67,24 @@ struct Pick {
   double pad;
 };
 
+struct Candidate {
+  double cost;  // NaN allowed
+  int index;    // 0x7fffffff: none
+  int pad;
+};
+
+constexpr int kNone = 0x7fffffff;
+
+// Whether (cost b, index ib) precedes (cost a, index ia) in torch.argmin order.
+__device__ __forceinline__ bool precedes(double b, int ib, double a, int ia) {
+  if (ib == kNone) return false;
+  if (ia == kNone) return true;
+  const bool nb = b != b, na = a != a;
+  if (nb != na) return nb;
+  if (nb) return ib < ia;
+  return b < a || (b == a && ib < ia);
+}
+
 constexpr int kPickThreads = 1024;
 constexpr int kRows = 32;  // rows per update CTA
 constexpr int kSplit = 8;  // warps sharing one row's sum over the earlier steps
@@ -70,7 +93,7 @@ constexpr int kSplit = 8;  // warps sharing one row's sum over the earlier steps
 template <typename T>
 __global__ void init_kernel(const T* __restrict__ W, const T* __restrict__ q, int n, T* __restrict__ b,
                             double* __restrict__ diag, uint8_t* __restrict__ alive,
-                            Pick* __restrict__ pick) {
+                            Pick* __restrict__ pick, unsigned* __restrict__ counter) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + warp;  // one row per warp
   if (i < n) {
@@ -83,7 +106,10 @@ __global__ void init_kernel(const T* __restrict__ W, const T* __restrict__ q, in
       alive[i] = 1;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) pick->spent = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    pick->spent = 0;
+    *counter = 0;
+  }
 }
 
 template <typename T>
@@ -169,15 +195,23 @@ __global__ void __launch_bounds__(kPickThreads) pick_kernel(
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRows * kSplit) update_kernel(
-    const T* __restrict__ W, int n, int step, T* __restrict__ b_in, T* __restrict__ b_out,
+__global__ void __launch_bounds__(kRows * kSplit) step_kernel(
+    const T* __restrict__ W, int n, int step, int count, const T* __restrict__ b_in, T* __restrict__ b_out,
     double* __restrict__ diag, uint8_t* __restrict__ alive, T* __restrict__ U,
-    const Pick* __restrict__ pick) {
+    const uint8_t* __restrict__ limited, long long limit, const Pick* __restrict__ pick_in,
+    Pick* __restrict__ pick_out, Candidate* __restrict__ partials, unsigned* __restrict__ counter,
+    int64_t* __restrict__ removed) {
   __shared__ T s_part[kSplit][kRows];
   __shared__ T s_uj[256];
+  __shared__ double s_red[kRows * kSplit / 32];
+  __shared__ Candidate s_best[kRows * kSplit / 32];
+  __shared__ bool s_last;
+  const double tiny = 2.2250738585072014e-308;  // smallest normal double (torch.finfo.tiny)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int j = (int)pick->index;
-  const double pivot = pick->pivot;
+  const int j = (int)pick_in->index;
+  const double pivot = pick_in->pivot;
+  const long long spent = pick_in->spent;  // marked removals including j
+  const bool spent_out = limited != nullptr && spent >= limit;
   const int i = blockIdx.x * kRows + lane;
   T acc = zero<T>();
   for (int t0 = 0; t0 < step; t0 += 256) {
@@ -190,47 +224,131 @@ __global__ void __launch_bounds__(kRows * kSplit) update_kernel(
   }
   s_part[warp][lane] = acc;
   __syncthreads();
-  if (warp == 0 && i < n) {
-    T sum = s_part[0][lane];
-    for (int w = 1; w < kSplit; ++w) sum = add(sum, s_part[w][lane]);
-    const T column = step ? sub(W[(size_t)i * n + j], sum) : W[(size_t)i * n + j];
-    const T bj = b_in[j];
-    const T scaled = divide(column, sqrt(pivot));
-    // b_i - w_i (b_j / pivot); the removed unknown keeps b = 0 and diag = 1 so that its
-    // masked cost stays finite (as the reference's loop).
-    T bi = sub(b_in[i], mul(column, divide(bj, pivot)));
-    double di = diag[i] - abs2(scaled);
-    if (i == j) {
-      alive[i] = 0;
-      di = 1.0;
-      bi = zero<T>();
+  if (warp == 0) {
+    double cost = INFINITY;
+    int index = kNone;
+    if (i < n) {
+      T sum = s_part[0][lane];
+      for (int w = 1; w < kSplit; ++w) sum = add(sum, s_part[w][lane]);
+      const T column = step ? sub(W[(size_t)i * n + j], sum) : W[(size_t)i * n + j];
+      const T bj = b_in[j];
+      const T scaled = divide(column, sqrt(pivot));
+      // b_i - w_i (b_j / pivot); the removed unknown keeps b = 0 and diag = 1 so that its
+      // masked cost stays finite (as the reference's loop).
+      T bi = sub(b_in[i], mul(column, divide(bj, pivot)));
+      double di = diag[i] - abs2(scaled);
+      bool live = alive[i] != 0;
+      if (i == j) {
+        alive[i] = 0;
+        live = false;
+        di = 1.0;
+        bi = zero<T>();
+      }
+      U[(size_t)step * n + i] = scaled;
+      b_out[i] = bi;
+      diag[i] = di;
+      const bool blocked = !live || (spent_out && limited[i]);
+      cost = blocked ? INFINITY : abs2(bi) / fmax(di, tiny);
+      index = i;
     }
-    U[(size_t)step * n + i] = scaled;
-    b_out[i] = bi;
-    diag[i] = di;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double oc = __shfl_xor_sync(0xffffffffu, cost, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, index, o);
+      if (precedes(oc, oi, cost, index)) {
+        cost = oc;
+        index = oi;
+      }
+    }
+    if (lane == 0) partials[blockIdx.x] = Candidate{cost, index, 0};
+    __threadfence();  // this lane's writes reach L2 before the CTA is counted
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  // The last CTA: every other CTA's writes are visible (they fenced before counting).
+  __threadfence();
+  if (threadIdx.x == 0) *counter = 0;
+  if (step + 1 >= count) return;
+  double cost = INFINITY;
+  int index = kNone;
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) {
+    const double oc = __ldcg(&partials[c].cost);
+    const int oi = __ldcg(&partials[c].index);
+    if (precedes(oc, oi, cost, index)) {
+      cost = oc;
+      index = oi;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double oc = __shfl_xor_sync(0xffffffffu, cost, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, index, o);
+    if (precedes(oc, oi, cost, index)) {
+      cost = oc;
+      index = oi;
+    }
+  }
+  if (lane == 0) s_best[warp] = Candidate{cost, index, 0};
+  __syncthreads();
+  __shared__ int s_next;
+  if (threadIdx.x == 0) {
+    cost = INFINITY;
+    index = kNone;
+    for (int w = 0; w < kRows * kSplit / 32; ++w)
+      if (precedes(s_best[w].cost, s_best[w].index, cost, index)) {
+        cost = s_best[w].cost;
+        index = s_best[w].index;
+      }
+    // Every cost infinite: torch.argmin of an all-inf vector returns 0.
+    if (index == kNone || (cost == INFINITY)) index = 0;
+    s_next = index;
+  }
+  __syncthreads();
+  const int jn = s_next;
+  double part = 0.0;
+  for (int t = threadIdx.x; t <= step; t += blockDim.x) {
+    const T u = t == step ? load_cg(&U[(size_t)t * n + jn]) : U[(size_t)t * n + jn];
+    part += abs2(u);
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if (lane == 0) s_red[warp] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double total = 0.0;
+    for (int w = 0; w < kRows * kSplit / 32; ++w) total += s_red[w];
+    const double pv = real_part(W[(size_t)jn * n + jn]) - total;
+    pick_out->index = jn;
+    pick_out->pivot = fmax(pv, tiny);
+    pick_out->spent = spent + (limited != nullptr && limited[jn] ? 1 : 0);
+    removed[step + 1] = jn;
   }
 }
 
 template <typename T>
 int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* limited, long long limit,
         void* workspace, int64_t* removed, cudaStream_t st) {
+  const int blocks = (n + kRows - 1) / kRows;
   uint8_t* w = reinterpret_cast<uint8_t*>(workspace);
   T* b0 = reinterpret_cast<T*>(w);
   T* b1 = b0 + n;
   double* diag = reinterpret_cast<double*>(b1 + n);
   T* U = reinterpret_cast<T*>(diag + n);
-  Pick* pick = reinterpret_cast<Pick*>(U + (size_t)count * n);
-  uint8_t* alive = reinterpret_cast<uint8_t*>(pick + 1);
+  Pick* picks = reinterpret_cast<Pick*>(U + (size_t)count * n);  // [2]
+  Candidate* partials = reinterpret_cast<Candidate*>(picks + 2);
+  unsigned* counter = reinterpret_cast<unsigned*>(partials + blocks);
+  uint8_t* alive = reinterpret_cast<uint8_t*>(counter + 4);
   const T* W = reinterpret_cast<const T*>(inverse);
-  init_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, reinterpret_cast<const T*>(rhs), n, b0, diag, alive, pick);
-  const int blocks = (n + kRows - 1) / kRows;
+  init_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, reinterpret_cast<const T*>(rhs), n, b0, diag, alive, picks,
+                                             counter);
+  pick_kernel<T><<<1, kPickThreads, 0, st>>>(W, n, 0, b0, diag, alive, limited, limit, U, picks, removed);
   for (int step = 0; step < count; ++step) {
-    T* bi = (step & 1) ? b1 : b0;
+    const T* bi = (step & 1) ? b1 : b0;
     T* bo = (step & 1) ? b0 : b1;
-    pick_kernel<T><<<1, kPickThreads, 0, st>>>(W, n, step, bi, diag, alive, limited, limit, U, pick, removed);
-    update_kernel<T><<<blocks, kRows * kSplit, 0, st>>>(W, n, step, bi, bo, diag, alive, U, pick);
+    step_kernel<T><<<blocks, kRows * kSplit, 0, st>>>(W, n, step, count, bi, bo, diag, alive, U, limited, limit,
+                                                      picks + (step & 1), picks + ((step + 1) & 1), partials,
+                                                      counter, removed);
   }
-  dsg_count_launches(1 + 2 * count);
+  dsg_count_launches(2 + count);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 
@@ -241,7 +359,9 @@ extern "C" {
 size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_complex) {
   if (n <= 0 || count < 0) return 0;
   const size_t elem = is_complex ? 16 : 8;
-  return elem * 2 * (size_t)n + 8 * (size_t)n + elem * (size_t)count * n + sizeof(Pick) + (size_t)n + 64;
+  const size_t blocks = ((size_t)n + kRows - 1) / kRows;
+  return elem * 2 * (size_t)n + 8 * (size_t)n + elem * (size_t)count * n + 2 * sizeof(Pick) +
+         blocks * sizeof(Candidate) + 16 + (size_t)n + 64;
 }
 
 int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, int32_t count,

@@ -97,9 +97,9 @@ __host__ __device__ inline Plan make_plan(int K, int N_fft, int P, int rank2, in
   p.u_bytes = p.nsub * p.ncols * 128;
   int off = 2 * p.u_bytes + stages * STAGE_BYTES;  // 1024-aligned blocks first
   p.table_off = off;
-  off += ((N_fft + K + 3) & ~3) * 4;
+  off += (N_fft + K) * 8;  // tan pairs (t_i, t_{i+1})
   p.recs_off = off;
-  off += UNIT * (2 + 2 * P) * 4;
+  off += UNIT * ((2 * P + 2 + 3) & ~3) * 4;
   p.xpose_off = off;
   off += 4 * XPOSE_WORDS * 4;
   p.bars_off = (off + 7) & ~7;
@@ -116,7 +116,8 @@ __global__ void __launch_bounds__(PTHREADS, 1)
                           const float* __restrict__ areas, int S, int rank2, int stages,
                           __nv_bfloat16* __restrict__ pt_hi, __nv_bfloat16* __restrict__ pt_lo,
                           int64_t ld, int64_t col0, int* __restrict__ status) {
-  constexpr int REC = 2 + 2 * P;
+  // record of a pair: numerators gg[0..P) at 0, tl at 2P, lobe at 2P + 1; 16-byte multiple
+  constexpr int REC = (2 * P + 2 + 3) & ~3;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(PTHREADS, 1)
   uint8_t* u_hi = smem;
   uint8_t* u_lo = smem + plan.u_bytes;
   uint8_t* stage_base = smem + 2 * plan.u_bytes;
-  float* table = reinterpret_cast<float*>(smem + plan.table_off);
+  float2* table = reinterpret_cast<float2*>(smem + plan.table_off);
   float* recs = reinterpret_cast<float*>(smem + plan.recs_off);
   uint32_t* xpose = reinterpret_cast<uint32_t*>(smem + plan.xpose_off);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + plan.bars_off);
@@ -144,7 +145,8 @@ __global__ void __launch_bounds__(PTHREADS, 1)
   uint32_t tmem_cols = 32;
   while ((int)tmem_cols < 2 * N) tmem_cols <<= 1;
 
-  for (int i = threadIdx.x; i < c.N + c.K; i += PTHREADS) table[i] = tan_entry(i, c.N, false);
+  for (int i = threadIdx.x; i < c.N + c.K; i += PTHREADS)
+    table[i] = make_float2(tan_entry(i, c.N, false), i + 1 < c.N + c.K ? tan_entry(i + 1, c.N, false) : 0.0f);
   if (threadIdx.x == 0) {
     mbar_init(u_full, 1);
     for (int b = 0; b < stages; ++b) {
@@ -192,15 +194,15 @@ __global__ void __launch_bounds__(PTHREADS, 1)
           const float2 cw = cscale(q.rot, q.amp * sqrtf(__ldg(areas + s)) * c.inv_S);
           float2 nu[P];
           numerators<P>(q.off, nu);
-          r[0] = q.tl;
-          r[1] = __int_as_float(q.lobe);
+          r[2 * P] = q.tl;
+          r[2 * P + 1] = __int_as_float(q.lobe);
 #pragma unroll
-          for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 + 2 * k) = cmul(cw, nu[k]);
+          for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 * k) = cmul(cw, nu[k]);
         } else {
-          r[0] = 1.0f;
-          r[1] = __int_as_float(c.N - 1);
+          r[2 * P] = 1.0f;
+          r[2 * P + 1] = __int_as_float(c.N - 1);
 #pragma unroll
-          for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 + 2 * k) = make_float2(0.f, 0.f);
+          for (int k = 0; k < P; ++k) *reinterpret_cast<float2*>(r + 2 * k) = make_float2(0.f, 0.f);
         }
       }
       asm volatile("bar.sync 1, %0;" ::"r"(NPROD) : "memory");
@@ -218,24 +220,44 @@ __global__ void __launch_bounds__(PTHREADS, 1)
           if (ok) {
             uint8_t* hi = stage_base + slot * STAGE_BYTES;
             uint8_t* lo = hi + A_SUB;
-            const int k = j * 32 + lane;  // this lane's range bin
-            const uint32_t lane_bytes = (uint32_t)(lane & 3) << 2;
+            // A lane evaluates bins k, k + 1 of one row; the two half-warps take
+            // neighbouring rows, so a store instruction fills two whole 128-byte rows.
+            const int half = lane >> 4, pair = lane & 15;
+            const int k = j * 32 + 2 * pair;
+            const uint32_t pair_bytes = (uint32_t)(pair & 1) << 3;
+            const int chunk = pair >> 1;
 #pragma unroll
-            for (int i = 0; i < ROWS_PER_WARP; ++i) {
-              const int row = warp * ROWS_PER_WARP + i;  // surfel within the tile
+            for (int i = 0; i < ROWS_PER_WARP / 2; ++i) {
+              const int row = warp * ROWS_PER_WARP + 2 * i + half;  // surfel within the tile
               const float* r = recs + (u * TM + row) * REC;
-              const float tl = r[0];
-              const int lobe = __float_as_int(r[1]);
-              const float2 gg = *reinterpret_cast<const float2*>(r + 2 + 2 * ((k - lobe) & (P - 1)));
-              const float cot = cot_from(table[k - lobe + c.N - 1], tl);
-              const float re = gg.x * cot - gg.y, im = gg.y * cot + gg.x;
-              const __nv_bfloat162 h = __floats2bfloat162_rn(re, im);
-              const __nv_bfloat162 l = __floats2bfloat162_rn(re - __low2float(h), im - __high2float(h));
+              const float2 tl_lobe = *reinterpret_cast<const float2*>(r + 2 * P);
+              const float tl = tl_lobe.x;
+              const int m = k - __float_as_int(tl_lobe.y);  // bin offset from the lobe
+              float2 g0, g1;  // numerators of bins k and k + 1
+              if (P == 1) {
+                g0 = g1 = *reinterpret_cast<const float2*>(r);
+              } else if (P == 2) {
+                const float4 both = *reinterpret_cast<const float4*>(r);
+                const bool odd = (m & 1) != 0;
+                g0 = odd ? make_float2(both.z, both.w) : make_float2(both.x, both.y);
+                g1 = odd ? make_float2(both.x, both.y) : make_float2(both.z, both.w);
+              } else {
+                g0 = *reinterpret_cast<const float2*>(r + 2 * (m & (P - 1)));
+                g1 = *reinterpret_cast<const float2*>(r + 2 * ((m + 1) & (P - 1)));
+              }
+              const float2 t = table[m + c.N - 1];
+              const float c0 = cot_from(t.x, tl), c1 = cot_from(t.y, tl);
+              const float re0 = g0.x * c0 - g0.y, im0 = g0.y * c0 + g0.x;
+              const float re1 = g1.x * c1 - g1.y, im1 = g1.y * c1 + g1.x;
+              const __nv_bfloat162 h0 = __floats2bfloat162_rn(re0, im0);
+              const __nv_bfloat162 h1 = __floats2bfloat162_rn(re1, im1);
+              const __nv_bfloat162 l0 = __floats2bfloat162_rn(re0 - __low2float(h0), im0 - __high2float(h0));
+              const __nv_bfloat162 l1 = __floats2bfloat162_rn(re1 - __low2float(h1), im1 - __high2float(h1));
               // K-major, 128-byte swizzle: row, then the 16-byte chunk XOR (row mod 8)
               const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128) +
-                                   ((uint32_t)((lane >> 2) ^ (row & 7)) << 4) + lane_bytes;
-              *reinterpret_cast<uint32_t*>(hi + off) = bf16x2_bits(h);
-              *reinterpret_cast<uint32_t*>(lo + off) = bf16x2_bits(l);
+                                   ((uint32_t)(chunk ^ (row & 7)) << 4) + pair_bytes;
+              *reinterpret_cast<uint2*>(hi + off) = make_uint2(bf16x2_bits(h0), bf16x2_bits(h1));
+              *reinterpret_cast<uint2*>(lo + off) = make_uint2(bf16x2_bits(l0), bf16x2_bits(l1));
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           }

@@ -16,6 +16,19 @@ from . import _lib
 from ._lib import call, f32, ptr, real_view
 
 
+# FP32 flops per counting unit (pair-bin; pair-normal for the normal bank) used for the
+# roofline accounting of the FP32-issue-bound kernels.
+FLOPS_PER_UNIT = {
+    "dsg_surfel_render": 16, "dsg_surfel_jvp": 24, "dsg_surfel_vjp": 20, "dsg_surfel_correlate": 18,
+    "dsg_surfel_correlate_active": 18, "dsg_surfel_correlate_gradient": 30,
+    "dsg_surfel_correlate_orientations": 12,
+}  # fmt: skip
+
+
+def _work(name, units):
+    _lib.add_work(name, float(units) * FLOPS_PER_UNIT[name])
+
+
 def _outputs(centers, *shape, dtype=torch.float32):
     return torch.empty(shape, dtype=dtype, device=centers.device)
 
@@ -29,6 +42,7 @@ def _profiles(config, positions, centers, normals, weights, fresnel_n):
     out = _outputs(centers, apertures, config.num_range_bins, 2)
     nbytes = _lib.query("dsg_surfel_render_workspace_bytes", chirp, apertures, count)
     work, nbytes = _lib.workspace(nbytes, centers.device)
+    _work("dsg_surfel_render", len(positions) * len(centers) * config.num_range_bins)
     call(
         "dsg_surfel_render", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
         ptr(weights), count, ptr(out), ptr(work), nbytes, _lib.stream(centers.device),
@@ -46,6 +60,7 @@ def vjp(config, positions, centers, normals, weights, upstream, fresnel_n):
                   _outputs(centers, count, 2))  # fmt: skip
     nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 8)
     work, nbytes = _lib.workspace(nbytes, centers.device)
+    _work("dsg_surfel_vjp", apertures * count * config.num_range_bins)
     call(
         "dsg_surfel_vjp", chirp, ptr(positions), apertures, ptr(centers), ptr(normals), ptr(w),
         count, ptr(u), ptr(gc), ptr(gn), ptr(gw), ptr(work), nbytes,
@@ -65,6 +80,7 @@ def jvp(config, positions, centers, normals, weights, delta_centers, delta_norma
     out = _outputs(centers, apertures, config.num_range_bins, 2)
     nbytes = _lib.query("dsg_surfel_render_workspace_bytes", chirp, apertures, count)
     work, nbytes = _lib.workspace(nbytes, centers.device)
+    _work("dsg_surfel_jvp", apertures * count * config.num_range_bins)
     call(
         "dsg_surfel_jvp", chirp, ptr(positions), apertures, ptr(centers), ptr(normals), ptr(w),
         ptr(dc), ptr(dn), ptr(dw), count, ptr(out), ptr(work), nbytes,
@@ -148,12 +164,14 @@ def correlate(config, positions, centers, normals, residual, fresnel_n, active=N
     nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3)
     work, nbytes = _lib.workspace(nbytes, centers.device)
     if active is None:
+        _work("dsg_surfel_correlate", apertures * count * config.num_range_bins)
         call(
             "dsg_surfel_correlate", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
             count, ptr(r), ptr(corr), ptr(norm), ptr(work), nbytes, _lib.stream(centers.device),
         )  # fmt: skip
     else:
         limit, period = active
+        _work("dsg_surfel_correlate_active", apertures * count * config.num_range_bins)
         call(
             "dsg_surfel_correlate_active", chirp, ptr(positions), apertures, ptr(centers),
             ptr(normals), count, ptr(r), ptr(limit), int(period), ptr(corr), ptr(norm), ptr(work),
@@ -178,6 +196,7 @@ def correlate_orientations(config, positions, centers, normals, bank, residual, 
     else:
         r, rt, nt = None, f32(table.correlation), f32(table.norm)
         oversample = table.oversample
+    _work("dsg_surfel_correlate_orientations", len(positions) * count * (len(bank) + 1))
     call(
         "dsg_surfel_correlate_orientations", chirp, ptr(positions), len(positions), ptr(centers),
         ptr(normals), count, ptr(bank) if len(bank) else None, len(bank), ptr(r), ptr(rt),
@@ -199,6 +218,7 @@ def correlate_gradient(config, positions, centers, normals, residual, fresnel_n,
         "dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3 + 3 * width
     )
     work, nbytes = _lib.workspace(nbytes, centers.device)
+    _work("dsg_surfel_correlate_gradient", apertures * count * config.num_range_bins)
     call(
         "dsg_surfel_correlate_gradient", chirp, ptr(positions), apertures, ptr(centers),
         ptr(normals), count, ptr(r), width, ptr(corr), ptr(norm), ptr(dcorr), ptr(dnorm),
