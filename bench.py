@@ -166,6 +166,7 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(device)
     lib = _lib.library()
     model, target, start, parameters, truth = build_problem(device)
+    pristine = {key: value.clone() for key, value in start.items()}  # the plain run's start
     mixed = args.mode == "mixed"
     config = DSFWConfig(iterations=100, batch=256, gram="bf16x3" if mixed else "fp32", batched=mixed)
     search = SpatialSearchConfig()
@@ -207,6 +208,7 @@ def run_ours(args, world, rank, local):
     step_ms = [b.elapsed_time(e) for b, e in times]
     total_s = _max_over_ranks(sum(step_ms) / 1e3, world, device)
     value = world * args.steps / total_s
+    timed_fit = {"nmse": state.history[-1]["nmse"], "median_center_to_surface_m": median_distance(state.params, truth)}
 
     # End to end: every step copies its inputs in from pinned host memory and its result out.
     host_target = target.cpu().pin_memory()
@@ -262,6 +264,31 @@ def run_ours(args, world, rank, local):
         "fit": {"iteration": history["iteration"], "nmse": history["nmse"],
                 "median_center_to_surface_m": median_distance(state.params, truth)},
     }
+    result["fit_after_timed_steps"] = timed_fit
+    if mixed and not args.no_plain:
+        # The metric compares mixed+batched with the plain FP32 run: the same start, the
+        # same warm-up and timed steps, the NMSE after them side by side.
+        plain = DSFWConfig(iterations=100, batch=256)
+        other = initialize(model, target, pristine, plain, parameters=parameters)
+        for _ in range(args.warmup):
+            other = step(other, plain, search)
+        torch.cuda.synchronize(device)
+        pairs = []
+        for _ in range(args.steps):
+            flush.view(torch.float32).fill_(1.0)
+            begin, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            begin.record()
+            other = step(other, plain, search)
+            end.record()
+            pairs.append((begin, end))
+        torch.cuda.synchronize(device)
+        plain_s = _max_over_ranks(sum(b.elapsed_time(e) for b, e in pairs) / 1e3, world, device)
+        plain_value = world * args.steps / plain_s
+        result["plain_fp32"] = {"value": round(plain_value, 4), "ms_per_step": round(plain_s * 1e3 / args.steps, 3),
+                                "fit_after_timed_steps": {"nmse": other.history[-1]["nmse"],
+                                                          "median_center_to_surface_m":
+                                                              median_distance(other.params, truth)}}  # fmt: skip
+        result["speedup_vs_plain_fp32"] = round(value / plain_value, 3)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.cpu_threads)
     return result
@@ -462,6 +489,13 @@ def run_kernels(args):
     ms = _event_time(lambda: kernel.correlate_orientations(config, prop, grid, grid_n, bank, upstream[: len(prop)],
                                                            0.0, table), it, wu, flush)  # fmt: skip
     record("dsg_surfel_correlate_orientations", ms, len(prop) * len(grid) * 25, 12, "pair-normals")
+    from dsplat.groundtruth import synthesize
+
+    amplitudes = (reflectivity * params["areas"].sqrt()).to(torch.complex64)
+    ms = _event_time(lambda: synthesize(positions, centers, normals, amplitudes, config), it, wu, flush)
+    rows.append({"kernel": "synthesize (dsg_synthesize_adc float64 + range FFT)", "ms": round(ms, 3),
+                 "units": A * S * config.adc_samples, "unit": "echo samples (float64)",
+                 "units_per_s": A * S * config.adc_samples / (ms * 1e-3)})  # fmt: skip
     block = positions[: min(A, 125)].contiguous()
     ms = _event_time(lambda: kernel.design(config, block, centers, normals, params["areas"], 0.0, True), it, wu, flush)
     record("dsg_surfel_design", ms, len(block) * S * K, 10)
@@ -525,6 +559,7 @@ def main():
     parser.add_argument("--mode", choices=["mixed", "plain"], default="mixed")
     parser.add_argument("--cpu-threads", type=int, default=None)
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison run")
     parser.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead")
     parser.add_argument("--case", choices=["small", "medium", "full"], default="full")
     args = parser.parse_args()

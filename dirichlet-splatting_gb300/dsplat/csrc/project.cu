@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(PTHREADS, 1)
           const int slot = stage % stages;
           const int round = stage / stages;
           bool ok = true;
-          if (lane == 0 && round > 0 && !mbar_wait(&empty[slot], (round - 1) & 1, abort)) {
+          if (lane == 0 && round > 0 && !mbar_wait_sleep(&empty[slot], (round - 1) & 1, abort)) {
             *abort = 1;
             ok = false;
           }
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(PTHREADS, 1)
       const int64_t base_col = col0 + (int64_t)a * rank2;
       for (int u = 0; u < tiles; ++u, ++tile) {
         const int acc = tile & 1, use = tile >> 1;
-        if (!mbar_wait(&done[acc], use & 1, abort)) {
+        if (!mbar_wait_sleep(&done[acc], use & 1, abort)) {
           *abort = 1;
           ok = false;
           break;
@@ -324,14 +324,14 @@ __global__ void __launch_bounds__(PTHREADS, 1)
       tma_load_2d(u_hi + t * (N * 128), &u_hi_map, 64 * t, 0, u_full);
       tma_load_2d(u_lo + t * (N * 128), &u_lo_map, 64 * t, 0, u_full);
     }
-    bool ok = mbar_wait(u_full, 0, abort);
+    bool ok = mbar_wait_sleep(u_full, 0, abort);
     int stage = 0, tile = 0;
     for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
       const int g = unit % groups;
       const int tiles = min(2, (S - g * UNIT + TM - 1) / TM);
       for (int u = 0; u < tiles && ok; ++u, ++tile) {
         const int acc = tile & 1, use = tile >> 1;
-        if (use > 0 && !mbar_wait(&tfree[acc], (use - 1) & 1, abort)) {
+        if (use > 0 && !mbar_wait_sleep(&tfree[acc], (use - 1) & 1, abort)) {
           ok = false;
           break;
         }
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(PTHREADS, 1)
         const uint32_t d = tmem + (uint32_t)(acc * N);
         for (int j = 0; j < nsub; ++j, ++stage) {
           const int slot = stage % stages;
-          if (!mbar_wait(&full[slot], (stage / stages) & 1, abort)) {
+          if (!mbar_wait_sleep(&full[slot], (stage / stages) & 1, abort)) {
             ok = false;
             break;
           }

@@ -741,20 +741,21 @@ __global__ void __launch_bounds__(128) jacobian_kernel(Consts c, const float* __
 // kernel at full occupancy.
 // ------------------------------------------------------------------------------------
 constexpr int kOrientWarps = 8;
-constexpr int kOrientRec = 8;  // ux, uy, uz, path = amp_scale / r, corr.re, corr.im, norm, pad
+// per aperture: ux, uy, uz, pad, path corr.re, path corr.im, path^2 norm, pad, with
+// path = lambda / (8 pi r); the amplitude of a normal is then path cos^2 F(cos).
+constexpr int kOrientRec = 8;
 
-// amp of scattering() for one normal: cos^2 F(cos) lambda / (8 pi r) with the same rounding
-// ((path cos) cos) F; without a Fresnel factor F = 1 and the last product is exact.
+// cos^2 F(cos) for cos > 0, else 0 (the angular part of the scattering amplitude).
 template <bool FRESNEL>
-__device__ __forceinline__ float bank_amplitude(const Consts& c, float cosv, float path) {
+__device__ __forceinline__ float bank_angular(const Consts& c, float cosv) {
   if (!(cosv > 0.0f)) return 0.0f;
-  float amp = path * cosv * cosv;
+  float a = cosv * cosv;
   if (FRESNEL) {
     float f, df;
     fresnel_factor(cosv, c.fresnel_n, f, df);
-    amp *= f;
+    a *= f;
   }
-  return amp;
+  return a;
 }
 
 template <int P, bool FRESNEL>
@@ -843,9 +844,10 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
           corr = cmulc(q.rot, z);
           norm = n0;
         }
-        *reinterpret_cast<float4*>(rec + lane * kOrientRec) =
-            make_float4(q.ux, q.uy, q.uz, c.amp_scale * q.inv_r);
-        *reinterpret_cast<float4*>(rec + lane * kOrientRec + 4) = make_float4(corr.x, corr.y, norm, 0.0f);
+        const float path = c.amp_scale * q.inv_r;
+        *reinterpret_cast<float4*>(rec + lane * kOrientRec) = make_float4(q.ux, q.uy, q.uz, 0.0f);
+        *reinterpret_cast<float4*>(rec + lane * kOrientRec + 4) =
+            make_float4(path * corr.x, path * corr.y, path * path * norm, 0.0f);
       }
       __syncwarp();
       const int count = min(32, A - a0);
@@ -854,10 +856,10 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
         const float4 g = *reinterpret_cast<const float4*>(rec + i * kOrientRec);
         const float4 v = *reinterpret_cast<const float4*>(rec + i * kOrientRec + 4);
         const float cosv = g.x * ex + g.y * ey + g.z * ez;
-        const float amp = bank_amplitude<FRESNEL>(c, cosv, g.w);
-        acc0 += amp * v.x;
-        acc1 += amp * v.y;
-        acc2 += amp * amp * v.z;
+        const float a = bank_angular<FRESNEL>(c, cosv);
+        acc0 += a * v.x;
+        acc1 += a * v.y;
+        acc2 += a * a * v.z;
       }
       __syncwarp();
     }

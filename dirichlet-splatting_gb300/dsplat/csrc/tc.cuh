@@ -61,6 +61,33 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   return false;
 }
 
+// try_wait with a suspend-time hint: a waiting thread sleeps in hardware until the phase
+// completes or the hint runs out, instead of spinning on the issue slots its warp shares
+// with producer warps. SLEEP_LIMIT x SLEEP_NS bounds the whole wait (about 2.6 s).
+constexpr uint32_t SLEEP_NS = 10000;
+constexpr uint32_t SLEEP_LIMIT = 1u << 18;
+
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(SLEEP_NS)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded, sleeping wait; false when the bound ran out or another role gave up.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  for (uint32_t i = 0; i < SLEEP_LIMIT; ++i) {
+    if (mbar_try_wait_sleep(bar, parity)) return true;
+    if ((i & 15u) == 15u && *abort) return false;
+  }
+  return false;
+}
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
                                             uint64_t* bar) {
   asm volatile(

@@ -58,22 +58,21 @@ def synthesize(aperture_positions, surfel_centers, surfel_normals, surfel_amplit
                fresnel_n=0.0):  # fmt: skip
     """Scan [apertures, range bins] of surfels with amplitudes reflectivity * sqrt(area).
 
-    Blocks of 256 apertures and 512 surfels bound the double-precision workspace.
+    The ADC samples are summed in float64 by dsg_synthesize_adc on the surfels' device;
+    the range FFT is torch.fft. Inputs must be CUDA tensors.
     """
+    from .kernels import _lib
+
     device = surfel_centers.device
-    time = torch.arange(config.adc_samples, device=device, dtype=torch.float64) / config.sample_rate_hz
-    centers, normals = surfel_centers.double(), surfel_normals.double()
-    amplitudes = surfel_amplitudes.to(torch.complex128)
-    profiles = []
-    for start in range(0, len(aperture_positions), 256):
-        block = aperture_positions[start : start + 256].double()
-        adc = torch.zeros((len(block), config.adc_samples), device=device, dtype=torch.complex128)
-        for s in range(0, len(centers), 512):
-            part = slice(s, s + 512)
-            distance, echo = _echoes(block, centers[part], normals[part], config, fresnel_n)
-            beat = 2 * config.slope_hz_s * distance / config.c0_m_s
-            tone = torch.exp(2j * math.pi * beat[:, :, None] * time)
-            adc += ((echo * amplitudes[part])[:, :, None] * tone).sum(1)
-        spectrum = torch.fft.fft(adc, n=config.n_fft)[:, : config.num_range_bins]
-        profiles.append((spectrum / config.adc_samples).to(torch.complex64))
-    return Scan(torch.cat(profiles), aperture_positions, config)
+    positions = aperture_positions.to(device=device, dtype=torch.float64).contiguous()
+    centers = surfel_centers.to(torch.float64).contiguous()
+    normals = surfel_normals.to(torch.float64).contiguous()
+    amplitudes = torch.view_as_real(surfel_amplitudes.to(torch.complex128).reshape(-1).contiguous())
+    adc = torch.empty((len(positions), config.adc_samples, 2), dtype=torch.float64, device=device)
+    _lib.call(
+        "dsg_synthesize_adc", _lib.chirp(config, fresnel_n), float(config.sample_rate_hz), _lib.ptr(positions),
+        len(positions), _lib.ptr(centers), _lib.ptr(normals), _lib.ptr(amplitudes), len(centers), _lib.ptr(adc),
+        _lib.stream(device),
+    )  # fmt: skip
+    spectrum = torch.fft.fft(torch.view_as_complex(adc), n=config.n_fft)[:, : config.num_range_bins]
+    return Scan((spectrum / config.adc_samples).to(torch.complex64), aperture_positions, config)

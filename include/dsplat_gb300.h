@@ -287,6 +287,16 @@ int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, in
                     int32_t column_from, int32_t k_splits, double* out, int32_t ldo,
                     int32_t* status, void* stream);
 
+/* ADC-domain synthesis of an FMCW scan in float64 (reference: dsplat/groundtruth.py:58-90
+ * synthesize, :40-55 _echoes): adc[a, n] = sum_s amplitudes_s * (echo of surfel s at
+ * aperture a) * exp(2 pi i beat n / sample_rate), n < chirp->samples (at most 256).
+ * positions [A,3], centers/normals [S,3] and amplitudes [S] complex (interleaved) are
+ * float64; adc [A, samples] complex128 (interleaved). The range FFT (n_fft points, first
+ * num_bins, divided by samples) is left to the caller's FFT library. */
+int dsg_synthesize_adc(const DsgChirp* chirp, double sample_rate, const double* positions, int32_t apertures,
+                       const double* centers, const double* normals, const double* amplitudes, int32_t surfels,
+                       double* adc, void* stream);
+
 /* Workspace of dsg_backward_elimination, in bytes. */
 size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_complex);
 

@@ -305,3 +305,23 @@ def test_correlate_active_set_matches_the_full_launch(fmcw):
     live = torch.arange(210, device="cuda") % 70 < 23
     assert torch.equal(ac[live], corr[live]) and torch.equal(an[live], norm[live])
     assert float(ac[~live].abs().max()) == 0.0 and float(an[~live].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("pad,samples,fresnel", [(2, 128, 0.0), (1, 256, 1.6), (4, 100, 0.0)])
+def test_synthesize_matches_the_float64_oracle(pad, samples, fresnel):
+    """groundtruth.synthesize (dsg_synthesize_adc + torch.fft) against the float64 ADC
+    synthesis of the oracle: the same scan up to complex64 storage (rel-L2 1e-6). 300
+    surfels cover a partial 256-surfel chunk; 100 samples a partial 16-sample block."""
+    from dsplat.groundtruth import synthesize
+
+    config = _cfg(pad_factor=pad, adc_samples=samples)
+    positions = aperture_grid(6)
+    params = surfels(300, seed=41)
+    generator = torch.Generator().manual_seed(42)
+    amplitudes = torch.complex(torch.rand(300, generator=generator) + 0.5,
+                               torch.randn(300, generator=generator) * 0.3).cuda() * 0.01  # fmt: skip
+    scan = synthesize(positions, params["centers"], params["normals"], amplitudes, config, fresnel)
+    expected = ofmcw.synthesize(positions.cpu(), params["centers"].cpu(), params["normals"].cpu(), amplitudes.cpu(),
+                                config, fresnel)  # fmt: skip
+    assert scan.data.dtype == torch.complex64 and scan.data.shape == expected.shape
+    assert rel_l2(scan.data, expected) < 1e-6
