@@ -340,3 +340,93 @@ class FMCWModel:
         mask[: config.num_range_bins * oversample : oversample] = 1
         norm = torch.fft.ifft(torch.fft.fft(mask) * torch.fft.fft(kernel.abs().square())).real
         return RangeTable(torch.view_as_real(correlation).contiguous(), norm.contiguous(), oversample)
+
+
+# --- Initialization ---------------------------------------------------------------------
+
+
+@torch.no_grad()
+def migration(scan, points, aperture_shape, *, depth_samples=96, padding=2, frequency_chunk=16):
+    """Relative complex focusing strength of a planar raster scan at world-space points.
+
+    Reference: dsplat/fmcw.py:361-454. The scan must be a complete row-major planar raster
+    and the points lie on one side of it. The positive range bins are zero-filled back to
+    chirp samples with the residual-video-phase correction, every ADC sample's aperture
+    field is propagated by the angular spectrum (K = 4 pi f / c, every propagating replica
+    of an undersampled aperture kept), and the focused volume is interpolated at the
+    points. A scalar Green model without obliquity or Fresnel factors: an initializer,
+    not a calibrated reflectivity. The frequency sum of every (depth, kx, ky) runs in one
+    CUDA kernel (dsg_migration_focus); frequency_chunk is accepted for the reference's
+    signature and has no effect.
+    """
+    from .kernels import _lib
+
+    del frequency_chunk
+    nu, nv = aperture_shape
+    raster = scan.scan_positions_m.reshape(nu, nv, 3)
+    center = raster[nu // 2, nv // 2]
+    step_u = (raster[-1, 0] - raster[0, 0]) / (nu - 1)
+    step_v = (raster[0, -1] - raster[0, 0]) / (nv - 1)
+    du, dv = float(step_u.norm()), float(step_v.norm())
+    eu, ev = step_u / du, step_v / dv
+    local = (points - center) @ torch.stack([eu, ev, torch.linalg.cross(eu, ev)], -1)
+    local[:, 2] = local[:, 2].abs()
+    z_low, z_high = local[:, 2].min(), local[:, 2].max()
+    if float(z_high - z_low) < 1e-6:
+        depth_samples = 1
+    cfg = scan.fmcw_config
+    device, dtype = points.device, points.dtype
+    # back to chirp samples: undo the residual video phase, inverse range FFT
+    beat_hz = torch.arange(cfg.num_range_bins, device=device, dtype=dtype) * (cfg.sample_rate_hz / cfg.n_fft)
+    video = scan.data * torch.exp(1j * math.pi * beat_hz.square() / cfg.slope_hz_s)
+    adc = torch.fft.ifft(video, n=cfg.n_fft, dim=-1)[..., : cfg.adc_samples] * cfg.adc_samples
+    pu, pv = nu * padding, nv * padding
+    field = adc.new_zeros((cfg.adc_samples, pu, pv))
+    ou, ov = pu // 2 - nu // 2, pv // 2 - nv // 2
+    field[:, ou : ou + nu, ov : ov + nv] = adc.reshape(nu, nv, -1).permute(2, 0, 1)
+    spectrum = torch.fft.fftshift(torch.fft.fft2(torch.fft.ifftshift(field, dim=(-2, -1))), dim=(-2, -1))
+    times = cfg.adc_start_time_s + torch.arange(cfg.adc_samples, device=device, dtype=dtype) / cfg.sample_rate_hz
+    wavenumber = 4 * math.pi * (cfg.fc_hz + cfg.slope_hz_s * times) / cfg.c0_m_s
+    carrier = wavenumber.max() / 2
+    planes = torch.unique(local[:, 2])
+    uniform = len(planes) < 3 or torch.allclose(
+        planes.diff(), planes.diff().mean().expand(len(planes) - 1), atol=1e-7, rtol=1e-4
+    )
+    if len(planes) <= depth_samples and uniform:
+        depths = planes  # the points already lie on these regularly spaced planes
+    else:
+        # |kz - carrier| <= Kmax / 2: four samples per Nyquist interval in depth
+        count = max(depth_samples, 1 + math.ceil(float(z_high - z_low) * float(wavenumber.max()) * 2 / math.pi))
+        depths = torch.linspace(float(z_low), float(z_high), count, device=device, dtype=dtype)
+    # every propagating replica of the sampled aperture spectrum
+    copies_u = max(1, math.ceil(float(wavenumber.max()) * du / math.pi))
+    copies_v = max(1, math.ceil(float(wavenumber.max()) * dv / math.pi))
+    qu, qv = pu * copies_u, pv * copies_v
+    dx, dy = du / copies_u, dv / copies_v
+    kx = 2 * math.pi * torch.fft.fftshift(torch.fft.fftfreq(qu, d=dx, device=device, dtype=dtype))
+    ky = 2 * math.pi * torch.fft.fftshift(torch.fft.fftfreq(qv, d=dy, device=device, dtype=dtype))
+    spectrum_c = torch.view_as_real(spectrum.to(torch.complex64).contiguous()).contiguous()
+    depth32 = depths.to(torch.float32).contiguous()
+    focused = torch.empty((len(depths), qu, qv, 2), dtype=torch.float32, device=device)
+    _lib.call(
+        "dsg_migration_focus", _lib.ptr(spectrum_c), cfg.adc_samples, pu, pv,
+        _lib.ptr(wavenumber.to(torch.float32).contiguous()), _lib.ptr(kx.to(torch.float32).contiguous()),
+        _lib.ptr(ky.to(torch.float32).contiguous()), qu, qv, _lib.ptr(depth32), len(depths), _lib.ptr(focused),
+        _lib.stream(device),
+    )  # fmt: skip
+    pitch = local.new_tensor([dx, dy])
+    low = torch.floor(local[:, :2].min(0).values / pitch).long() - 2
+    high = torch.ceil(local[:, :2].max(0).values / pitch).long() + 2
+    a, b = int(low[0]) + qu // 2, int(high[0]) + qu // 2 + 1
+    c, d = int(low[1]) + qv // 2, int(high[1]) + qv // 2 + 1
+    planes_xy = torch.fft.fftshift(torch.fft.ifft2(torch.fft.ifftshift(torch.view_as_complex(focused), dim=(-2, -1))),
+                                   dim=(-2, -1))  # fmt: skip
+    # remove the carrier before interpolating (the band is then centred), restore it after
+    volume = planes_xy[:, a:b, c:d] * torch.exp(1j * carrier * depths)[:, None, None]
+    volume = volume * (copies_u * copies_v / cfg.adc_samples)
+    xy = 2 * (local[:, :2] - low * pitch) / ((high - low) * pitch) - 1
+    zz = 2 * (local[:, 2] - z_low) / (z_high - z_low) - 1 if len(depths) > 1 else torch.zeros_like(local[:, 2])
+    where = torch.stack([xy[:, 1], xy[:, 0], zz], -1).reshape(1, 1, 1, -1, 3)
+    channels = torch.view_as_real(volume).permute(3, 0, 1, 2)[None]
+    sampled = F.grid_sample(channels, where, mode="bilinear", align_corners=True).reshape(2, -1)
+    return torch.complex(sampled[0], sampled[1]) * torch.exp(-1j * carrier * local[:, 2])

@@ -90,6 +90,7 @@ SIGNATURES = {
     "dsg_distinct": (ctypes.c_int, [P, P, P, I32, I32, P, I32, P, F32, I32, P, P, P]),
     "dsg_elimination_workspace_bytes": (SZ, [I32, I32, I32]),
     "dsg_synthesize_adc": (ctypes.c_int, [CP, F64, P, I32, P, P, P, I32, P, P]),
+    "dsg_migration_focus": (ctypes.c_int, [P, I32, I32, I32, P, P, P, I32, I32, P, I32, P, P]),
     "dsg_backward_elimination": (ctypes.c_int, [P, P, I32, I32, P, I64, I32, P, SZ, P, P]),
     "dsg_direction": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P]),
     "dsg_trial": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P, P]),

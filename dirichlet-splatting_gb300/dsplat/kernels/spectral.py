@@ -88,7 +88,7 @@ class _Render(torch.autograd.Function):
     def backward(ctx, grad):
         centers, coeff, bins = ctx.saved_tensors
         gc, gb = _backward(ctx.grid, centers, coeff, bins, grad.contiguous())
-        return gc, gb, None, None
+        return gc.to(centers.dtype), gb, None, None  # the kernel works in float32
 
 
 def render(grid, centers, coefficients, bins):

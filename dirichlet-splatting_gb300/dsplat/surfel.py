@@ -16,6 +16,10 @@ functions carry that area chain around the CUDA kernels of dsplat.kernels.surfel
 
 from __future__ import annotations
 
+from dataclasses import dataclass
+
+import torch
+
 from .kernels import surfel as kernel
 
 
@@ -97,3 +101,85 @@ def correlate_orientations(config, positions, params, bank, residual, fresnel_n=
     )
     root = params["areas"].sqrt()[:, None]
     return corr * root, norm * root.square()
+
+
+# --- Range / Doppler / azimuth composition (13 degrees of freedom per surfel) ----------------
+# Reference: dsplat/surfel.py:132-196. A surfel has position [3], normal [3], area,
+# complex reflectivity, velocity [3] and complex material impedance; a monostatic
+# range/Doppler/azimuth sensor maps it to a point of a separable spectral grid, where the
+# spectral kernels (dsplat.kernels.spectral) render it. Gradients reach all thirteen
+# quantities through autograd and the hand-written spectral VJP.
+
+
+@dataclass(frozen=True)
+class Sensor:
+    """A range/Doppler/azimuth sensor: bins per axis and the chirp constants."""
+
+    shape: tuple[int, int, int] = (128, 32, 16)  # range, Doppler, azimuth bins
+    carrier_hz: float = 77e9
+    sample_rate_hz: float = 2e6
+    slope_hz_s: float = 20e12
+    chirp_interval_s: float = 60e-6
+    spacing_m: float | None = None  # array pitch; None: half a wavelength
+    wave_speed: float = 299792458.0
+
+    @property
+    def wavelength(self):
+        return self.wave_speed / self.carrier_hz
+
+
+def project(positions, velocities, sensor: Sensor, origin=None, array_axis=None):
+    """Fractional (range, Doppler, azimuth) bin coordinates [S, 3] of moving points.
+
+    range bin = 2 K r N_r / (c f_s); Doppler bin = 2 N_d T_c (v . u) / lambda; azimuth
+    bin = N_a d (u . axis) / lambda, with u the unit line of sight from the origin.
+    """
+    origin = positions.new_zeros(3) if origin is None else origin
+    axis = positions.new_tensor([1.0, 0.0, 0.0]) if array_axis is None else array_axis
+    offset = positions - origin
+    distance = offset.norm(dim=-1).clamp(min=1e-9)
+    sight = offset / distance[:, None]
+    n_range, n_doppler, n_azimuth = sensor.shape
+    pitch = sensor.wavelength / 2 if sensor.spacing_m is None else sensor.spacing_m
+    range_bin = distance * (2 * sensor.slope_hz_s / sensor.wave_speed * n_range / sensor.sample_rate_hz)
+    doppler_bin = (velocities * sight).sum(-1) * (2 * n_doppler * sensor.chirp_interval_s / sensor.wavelength)
+    azimuth_bin = (sight * axis).sum(-1) * (n_azimuth * pitch / sensor.wavelength)
+    return torch.stack([range_bin, doppler_bin, azimuth_bin], -1)
+
+
+def fresnel_te(cosine, impedance, ambient=1.0):
+    """TE reflection coefficient of a material with complex impedance (0 gives -1).
+
+    Where cos <= 0 the amplitude vanishes anyway; the coefficient is then -1, or 0 for a
+    matched interface, and is evaluated at a harmless cosine so no NaN reaches autograd.
+    """
+    eta = impedance / ambient
+    safe = torch.where(cosine > 0, cosine, torch.ones_like(cosine))
+    transmitted = torch.sqrt(1 - eta.square() * (1 - safe.square()) + 0j)
+    coefficient = (eta * safe - transmitted) / (eta * safe + transmitted)
+    outside = torch.where(eta == 1, torch.zeros_like(coefficient), -torch.ones_like(coefficient))
+    return torch.where(cosine > 0, coefficient, outside)
+
+
+def render_scene(positions, normals, areas, reflectivity, velocities, impedance, sensor: Sensor, *,
+                 origin=None, gamma=1.0, window="rect"):  # fmt: skip
+    """Coherent range/Doppler/azimuth cube of 13-DOF surfels; differentiable in all of them.
+
+    coefficient = reflectivity sqrt(area) cos^2 F_TE(cos) r^-gamma exp(4 pi i r / lambda),
+    placed at project(...) on a SpectralGrid(sensor.shape, window) and rendered by the
+    spectral kernel.
+    """
+    from .kernels import spectral as spectral_kernel
+    from .spectral import SpectralGrid
+
+    origin = positions.new_zeros(3) if origin is None else origin
+    toward = origin - positions
+    distance = toward.norm(dim=-1).clamp(min=1e-9)
+    unit = torch.nn.functional.normalize(normals, dim=-1)
+    cosine = (unit * toward / distance[:, None]).sum(-1).clamp(min=0)
+    coefficient = (reflectivity * areas.sqrt() * cosine.square() * fresnel_te(cosine, impedance)
+                   * distance.pow(-gamma))  # fmt: skip
+    coefficient = coefficient * torch.exp(4j * torch.pi * distance / sensor.wavelength)
+    grid = SpectralGrid(sensor.shape, window=window)
+    centers = project(positions, velocities, sensor, origin)
+    return spectral_kernel.render(grid, centers, coefficient, grid.bins(positions.device)).reshape(grid.shape)

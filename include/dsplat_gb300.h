@@ -297,6 +297,15 @@ int dsg_synthesize_adc(const DsgChirp* chirp, double sample_rate, const double* 
                        const double* centers, const double* normals, const double* amplitudes, int32_t surfels,
                        double* adc, void* stream);
 
+/* Angular-spectrum focusing of the range-migration initializer (reference:
+ * dsplat/fmcw.py:361-454, migration, its per-depth frequency sum): focused [depth_count,
+ * qu, qv] complex = sum_f spectrum[f, iu, iv] kz exp(-i kz depths[d]), kz = sqrt(max(k_f^2 -
+ * kx^2 - ky^2, 0)), iu = (x - qu/2 + pu/2) mod pu (likewise iv). spectrum [frequencies, pu,
+ * pv] complex, k [frequencies], kx [qu], ky [qv], depths [depth_count] float32. */
+int dsg_migration_focus(const float* spectrum, int32_t frequencies, int32_t pu, int32_t pv, const float* k,
+                        const float* kx, const float* ky, int32_t qu, int32_t qv, const float* depths,
+                        int32_t depth_count, float* focused, void* stream);
+
 /* Workspace of dsg_backward_elimination, in bytes. */
 size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_complex);
 

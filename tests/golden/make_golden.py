@@ -5,7 +5,9 @@ Run here, where the reference checkout exists (it never exists on the GPU machin
     python tests/golden/make_golden.py [/path/to/Dirichlet-Splatting]
 
 It imports the reference's own float64 oracles (tests/reference/kernel.py,
-tests/reference/oracle.py, dsplat/groundtruth.py) with a stub `slangtorch` module,
+tests/reference/oracle.py, tests/reference/physics.py, dsplat/groundtruth.py and the
+pure-torch dsplat/fmcw.py migration) with a stub
+`slangtorch` module,
 evaluates them on seeded inputs and writes the inputs and outputs to
 tests/golden/reference_oracles.npz. tests/test_oracle_golden.py then checks the
 repository's oracle/ against these vectors. The reference's Slang kernels are not
@@ -116,5 +118,90 @@ def main(root: Path) -> None:
     print("wrote", HERE / "reference_oracles.npz", sum(v.nbytes for v in out.values()) // 1024, "KiB")
 
 
+def scene_inputs(count=6, seed=3):
+    """Seeded 13-DOF surfels in front of a range/Doppler/azimuth sensor at the origin."""
+    g = torch.Generator().manual_seed(seed)
+    positions = torch.tensor([0.0, 0.0, 1.5]) + 0.3 * torch.randn(count, 3, generator=g, dtype=torch.float64)
+    normals = torch.nn.functional.normalize(-positions + 0.2 * torch.randn(count, 3, generator=g, dtype=torch.float64),
+                                            dim=1)  # fmt: skip
+    areas = 1e-3 * (1 + torch.rand(count, generator=g, dtype=torch.float64))
+    reflectivity = torch.complex(torch.rand(count, generator=g, dtype=torch.float64),
+                                 torch.rand(count, generator=g, dtype=torch.float64))  # fmt: skip
+    velocities = torch.randn(count, 3, generator=g, dtype=torch.float64)
+    impedance = torch.complex(1 + torch.rand(count, generator=g, dtype=torch.float64),
+                              0.1 * torch.rand(count, generator=g, dtype=torch.float64))  # fmt: skip
+    return positions, normals, areas, reflectivity, velocities, impedance
+
+
+def scene_cases(root: Path) -> None:
+    """The reference's float64 composed renderer (tests/reference/physics.py) and the
+    gradients of Re(conj(u) . cube) by autograd, written to reference_scene.npz."""
+    sys.modules.setdefault("slangtorch", types.ModuleType("slangtorch"))
+    sys.path.insert(0, str(root))
+    sys.path.insert(0, str(root / "tests"))
+    import reference.physics as physics  # noqa: E402
+    from dsplat.surfel import Sensor  # noqa: E402
+
+    out: dict[str, np.ndarray] = {}
+    for name, shape, window, gamma in (("rect", (32, 16, 8), "rect", 1.0), ("hann", (24, 12, 6), "hann", 2.0)):
+        inputs = [x.clone().requires_grad_() for x in scene_inputs(seed=len(out) + 3)]
+        sensor = Sensor(shape=shape)
+        cube = physics.render_scene(*inputs, sensor, window=window, gamma=gamma)
+        g = torch.Generator().manual_seed(7)
+        upstream = torch.complex(torch.randn(shape, generator=g, dtype=torch.float64),
+                                 torch.randn(shape, generator=g, dtype=torch.float64))  # fmt: skip
+        grads = torch.autograd.grad((upstream.conj() * cube).real.sum(), inputs)
+        keys = ("positions", "normals", "areas", "reflectivity", "velocities", "impedance")
+        for key, value, grad in zip(keys, inputs, grads, strict=True):
+            out[f"{name}_{key}"] = value.detach().numpy()
+            out[f"{name}_grad_{key}"] = grad.numpy()
+        out[f"{name}_upstream"] = upstream.numpy()
+        out[f"{name}_cube"] = cube.detach().numpy()
+        out[f"{name}_meta"] = np.array([gamma])
+    np.savez_compressed(HERE / "reference_scene.npz", **out)
+    print("wrote", HERE / "reference_scene.npz")
+
+
+def migration_cases(root: Path) -> None:
+    """The reference's range-migration initializer (dsplat/fmcw.py:361-454, pure torch) on
+    scans synthesized by its own groundtruth.synthesize, written to reference_migration.npz."""
+    sys.modules.setdefault("slangtorch", types.ModuleType("slangtorch"))
+    sys.path.insert(0, str(root))
+    import dsplat.fmcw as fmcw  # noqa: E402
+    import dsplat.groundtruth as groundtruth  # noqa: E402
+
+    out: dict[str, np.ndarray] = {}
+    config = fmcw.FMCWConfig()
+    side = 16
+    positions = groundtruth.planar_array(side, config.lambda_m / 4, standoff=0.3)
+    g = torch.Generator().manual_seed(19)
+    centers = torch.tensor([0.0, 0.0, 0.3]) + torch.tensor([0.006, 0.006, 0.004]) * (
+        2 * torch.rand(4, 3, generator=g) - 1)  # fmt: skip
+    normals = torch.tensor([0.0, 0.0, -1.0]).expand(4, 3).clone()
+    amplitudes = torch.complex(0.5 + torch.rand(4, generator=g), 0.2 * torch.randn(4, generator=g)) * 0.003
+    scan = groundtruth.synthesize(positions, centers, normals, amplitudes, config)
+    out["positions"], out["data"] = positions.numpy(), scan.data.numpy()
+    axis = torch.linspace(-0.008, 0.008, 17)
+    x, y = torch.meshgrid(axis, axis, indexing="ij")
+    plane = torch.stack([x.flatten(), y.flatten(), torch.full_like(x.flatten(), 0.3)], -1)
+    volume = torch.cat([plane[::3] + torch.tensor([0.0, 0.0, dz]) for dz in (-0.004, -0.001, 0.002, 0.005)])
+    for name, points, padding in (("plane", plane, 2), ("volume", volume, 3)):
+        strength = fmcw.migration(scan, points, (side, side), padding=padding)
+        out[f"{name}_points"], out[f"{name}_strength"] = points.numpy(), strength.numpy()
+        out[f"{name}_padding"] = np.array([padding])
+    np.savez_compressed(HERE / "reference_migration.npz", **out)
+    print("wrote", HERE / "reference_migration.npz")
+
+
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REFERENCE)
+    # --scene / --migration regenerate only reference_scene.npz / reference_migration.npz
+    flags = {"--scene", "--migration"}
+    args = [a for a in sys.argv[1:] if a not in flags]
+    root = Path(args[0]) if args else DEFAULT_REFERENCE
+    chosen = flags & set(sys.argv)
+    if not chosen:
+        main(root)
+    if not chosen or "--scene" in chosen:
+        scene_cases(root)
+    if not chosen or "--migration" in chosen:
+        migration_cases(root)

@@ -110,3 +110,26 @@ def test_oracle_derivatives_agree_with_central_differences():
             minus[s] -= shift[s]
             numeric = (objective(plus, normals) - objective(minus, normals)) / (2 * h)
             assert abs(numeric - float(gc[s, axis])) <= 1e-4 * float(gc.abs().max())
+
+
+def test_scene_oracle_matches_the_reference_physics_renderer():
+    """oracle.scene against tests/reference/physics.py (values and autograd gradients)."""
+    from dsplat.spectral import SpectralGrid
+    from dsplat.surfel import Sensor
+
+    from oracle import scene
+
+    golden = np.load(Path(__file__).parent / "golden" / "reference_scene.npz")
+    keys = ("positions", "normals", "areas", "reflectivity", "velocities", "impedance")
+    for name, shape, window in (("rect", (32, 16, 8), "rect"), ("hann", (24, 12, 6), "hann")):
+        inputs = [torch.from_numpy(golden[f"{name}_{k}"]).requires_grad_() for k in keys]
+        gamma = float(golden[f"{name}_meta"][0])
+        sensor = Sensor(shape=shape)
+        cube = scene.render_scene(*inputs, sensor, SpectralGrid(shape, window=window), gamma=gamma)
+        expected = torch.from_numpy(golden[f"{name}_cube"])
+        assert float((cube - expected).abs().max() / expected.abs().max()) < 1e-12
+        upstream = torch.from_numpy(golden[f"{name}_upstream"])
+        grads = torch.autograd.grad((upstream.conj() * cube).real.sum(), inputs)
+        for key, grad in zip(keys, grads, strict=True):
+            ref = torch.from_numpy(golden[f"{name}_grad_{key}"])
+            assert float((grad - ref).abs().max() / ref.abs().max().clamp(min=1e-300)) < 1e-10, key
