@@ -15,6 +15,7 @@ from math import ceil
 import torch
 
 from .kernels import search
+from .tracing import stage
 
 
 def certificate(model, params, residual, mode, *, gradient=False, normals=False, active=None):
@@ -255,23 +256,25 @@ def _graphed_ascent(iterate, iterations, params, value, grad, inverse):
     side.wait_stream(torch.cuda.current_stream(device))
     timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be timed inside a graph
     try:
-        with torch.cuda.stream(side):
-            state = iterate(params, value, grad, inverse)
-            static = ({k: v.clone() for k, v in state[0].items()}, state[1].clone(), state[2].clone(),
-                      state[3].clone())  # fmt: skip
-        torch.cuda.current_stream(device).wait_stream(side)
-        graph = torch.cuda.CUDAGraph()
-        before = _lib.library().dsg_launch_count()
-        with torch.cuda.graph(graph):
-            out = iterate(*static)
-            for key, v in out[0].items():
-                static[0][key].copy_(v)
-            static[1].copy_(out[1])
-            static[2].copy_(out[2])
-            static[3].copy_(out[3])
-        per_replay = _lib.library().dsg_launch_count() - before
-        for _ in range(iterations - 1):
-            graph.replay()
+        with stage("ascent.capture"):
+            with torch.cuda.stream(side):
+                state = iterate(params, value, grad, inverse)
+                static = ({k: v.clone() for k, v in state[0].items()}, state[1].clone(), state[2].clone(),
+                          state[3].clone())  # fmt: skip
+            torch.cuda.current_stream(device).wait_stream(side)
+            graph = torch.cuda.CUDAGraph()
+            before = _lib.library().dsg_launch_count()
+            with torch.cuda.graph(graph):
+                out = iterate(*static)
+                for key, v in out[0].items():
+                    static[0][key].copy_(v)
+                static[1].copy_(out[1])
+                static[2].copy_(out[2])
+                static[3].copy_(out[3])
+            per_replay = _lib.library().dsg_launch_count() - before
+        with stage("ascent.replay"):
+            for _ in range(iterations - 1):
+                graph.replay()
         _lib.REPLAYED_LAUNCHES += per_replay * (iterations - 1)
     finally:
         _lib.TIMERS = timers

@@ -52,6 +52,9 @@ __device__ __forceinline__ Cplx mul(Cplx a, Cplx b) {
 __device__ __forceinline__ double load_cg(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ Cplx load_cg(const Cplx* p) { return Cplx{__ldcg(&p->x), __ldcg(&p->y)}; }
 
+__device__ __forceinline__ double conj_of(double v) { return v; }
+__device__ __forceinline__ Cplx conj_of(Cplx v) { return Cplx{v.x, -v.y}; }
+
 template <typename T>
 __device__ __forceinline__ T zero();
 template <>
@@ -92,7 +95,7 @@ constexpr int kSplit = 8;  // warps sharing one row's sum over the earlier steps
 // b = W q, diag = real(W_ii), alive = 1, spent = 0.
 template <typename T>
 __global__ void init_kernel(const T* __restrict__ W, const T* __restrict__ q, int n, T* __restrict__ b,
-                            double* __restrict__ diag, uint8_t* __restrict__ alive,
+                            double* __restrict__ diag, double* __restrict__ wdiag, uint8_t* __restrict__ alive,
                             Pick* __restrict__ pick, unsigned* __restrict__ counter) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + warp;  // one row per warp
@@ -102,9 +105,46 @@ __global__ void init_kernel(const T* __restrict__ W, const T* __restrict__ q, in
     for (int o = 16; o > 0; o >>= 1) acc = add(acc, shfl_xor(acc, o));
     if (lane == 0) {
       b[i] = acc;
-      diag[i] = real_part(W[(size_t)i * n + i]);
+      diag[i] = wdiag[i] = real_part(W[(size_t)i * n + i]);
       alive[i] = 1;
     }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    pick->spent = 0;
+    *counter = 0;
+  }
+}
+
+// Factor form, W = X^H X with X = L^-1 lower triangular (row-major): y = X q, one warp per
+// row (this kernel), then b = X^H y and the diagonal sum_k |X_ki|^2 (factor_init_kernel).
+template <typename T>
+__global__ void factor_rows_kernel(const T* __restrict__ X, const T* __restrict__ q, int n, T* __restrict__ y) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (i >= n) return;
+  T acc = zero<T>();
+  for (int k = lane; k <= i; k += 32) acc = add(acc, mul(X[(size_t)i * n + k], q[k]));
+  for (int o = 16; o > 0; o >>= 1) acc = add(acc, shfl_xor(acc, o));
+  if (lane == 0) y[i] = acc;
+}
+
+template <typename T>
+__global__ void factor_init_kernel(const T* __restrict__ X, const T* __restrict__ y, int n, T* __restrict__ b,
+                                   double* __restrict__ diag, double* __restrict__ wdiag,
+                                   uint8_t* __restrict__ alive, Pick* __restrict__ pick,
+                                   unsigned* __restrict__ counter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    T acc = zero<T>();  // sum_k conj(X_ki) y_k = conj(sum_k X_ki conj(y_k))
+    double d = 0.0;
+    for (int k = i; k < n; ++k) {
+      const T x = X[(size_t)k * n + i];
+      acc = add(acc, mul_conj(x, y[k]));
+      d += abs2(x);
+    }
+    b[i] = conj_of(acc);
+    diag[i] = wdiag[i] = d;
+    alive[i] = 1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     pick->spent = 0;
@@ -116,7 +156,8 @@ template <typename T>
 __global__ void __launch_bounds__(kPickThreads) pick_kernel(
     const T* __restrict__ W, int n, int step, const T* __restrict__ b, const double* __restrict__ diag,
     const uint8_t* __restrict__ alive, const uint8_t* __restrict__ limited, long long limit,
-    const T* __restrict__ U, Pick* __restrict__ pick, int64_t* __restrict__ removed) {
+    const T* __restrict__ U, const double* __restrict__ wdiag, Pick* __restrict__ pick,
+    int64_t* __restrict__ removed) {
   __shared__ double s_cost[kPickThreads / 32];
   __shared__ int s_index[kPickThreads / 32];
   __shared__ double s_sum[kPickThreads / 32];
@@ -186,7 +227,7 @@ __global__ void __launch_bounds__(kPickThreads) pick_kernel(
   if (threadIdx.x == 0) {
     double total = 0.0;
     for (int w = 0; w < kPickThreads / 32; ++w) total += s_sum[w];
-    const double pivot = real_part(W[(size_t)j * n + j]) - total;
+    const double pivot = wdiag[j] - total;
     pick->index = j;
     pick->pivot = fmax(pivot, tiny);
     if (limited != nullptr && limited[j]) pick->spent += 1;
@@ -194,13 +235,18 @@ __global__ void __launch_bounds__(kPickThreads) pick_kernel(
   }
 }
 
-template <typename T>
+// W is the inverse itself, or with FACTOR its lower-triangular factor X (W = X^H X): the
+// column W_ij is then sum_k conj(X_ki) X_kj over k >= max(i, j), X's column j staged in
+// shared memory.
+template <typename T, bool FACTOR>
 __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
     const T* __restrict__ W, int n, int step, int count, const T* __restrict__ b_in, T* __restrict__ b_out,
-    double* __restrict__ diag, uint8_t* __restrict__ alive, T* __restrict__ U,
-    const uint8_t* __restrict__ limited, long long limit, const Pick* __restrict__ pick_in,
+    double* __restrict__ diag, const double* __restrict__ wdiag, uint8_t* __restrict__ alive,
+    T* __restrict__ U, const uint8_t* __restrict__ limited, long long limit, const Pick* __restrict__ pick_in,
     Pick* __restrict__ pick_out, Candidate* __restrict__ partials, unsigned* __restrict__ counter,
     int64_t* __restrict__ removed) {
+  extern __shared__ uint8_t s_dyn[];
+  __shared__ T s_partw[FACTOR ? kSplit : 1][kRows];
   __shared__ T s_part[kSplit][kRows];
   __shared__ T s_uj[256];
   __shared__ double s_red[kRows * kSplit / 32];
@@ -213,6 +259,16 @@ __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
   const long long spent = pick_in->spent;  // marked removals including j
   const bool spent_out = limited != nullptr && spent >= limit;
   const int i = blockIdx.x * kRows + lane;
+  T accw = zero<T>();
+  if (FACTOR) {
+    T* s_xj = reinterpret_cast<T*>(s_dyn);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) s_xj[k] = k >= j ? W[(size_t)k * n + j] : zero<T>();
+    __syncthreads();
+    const int k0 = max(j, (int)blockIdx.x * kRows);
+    if (i < n)
+      for (int k = k0 + warp; k < n; k += kSplit) accw = add(accw, mul_conj(W[(size_t)k * n + i], s_xj[k]));
+    s_partw[FACTOR ? warp : 0][lane] = accw;
+  }
   T acc = zero<T>();
   for (int t0 = 0; t0 < step; t0 += 256) {
     const int len = min(256, step - t0);
@@ -230,7 +286,15 @@ __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
     if (i < n) {
       T sum = s_part[0][lane];
       for (int w = 1; w < kSplit; ++w) sum = add(sum, s_part[w][lane]);
-      const T column = step ? sub(W[(size_t)i * n + j], sum) : W[(size_t)i * n + j];
+      T wij;
+      if (FACTOR) {
+        T total = s_partw[0][lane];
+        for (int w = 1; w < kSplit; ++w) total = add(total, s_partw[FACTOR ? w : 0][lane]);
+        wij = conj_of(total);
+      } else {
+        wij = W[(size_t)i * n + j];
+      }
+      const T column = step ? sub(wij, sum) : wij;
       const T bj = b_in[j];
       const T scaled = divide(column, sqrt(pivot));
       // b_i - w_i (b_j / pivot); the removed unknown keeps b = 0 and diag = 1 so that its
@@ -316,7 +380,7 @@ __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
   if (threadIdx.x == 0) {
     double total = 0.0;
     for (int w = 0; w < kRows * kSplit / 32; ++w) total += s_red[w];
-    const double pv = real_part(W[(size_t)jn * n + jn]) - total;
+    const double pv = wdiag[jn] - total;
     pick_out->index = jn;
     pick_out->pivot = fmax(pv, tiny);
     pick_out->spent = spent + (limited != nullptr && limited[jn] ? 1 : 0);
@@ -324,7 +388,7 @@ __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
   }
 }
 
-template <typename T>
+template <typename T, bool FACTOR>
 int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* limited, long long limit,
         void* workspace, int64_t* removed, cudaStream_t st) {
   const int blocks = (n + kRows - 1) / kRows;
@@ -332,23 +396,36 @@ int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* l
   T* b0 = reinterpret_cast<T*>(w);
   T* b1 = b0 + n;
   double* diag = reinterpret_cast<double*>(b1 + n);
-  T* U = reinterpret_cast<T*>(diag + n);
+  double* wdiag = diag + n;
+  T* U = reinterpret_cast<T*>(wdiag + n);
   Pick* picks = reinterpret_cast<Pick*>(U + (size_t)count * n);  // [2]
   Candidate* partials = reinterpret_cast<Candidate*>(picks + 2);
   unsigned* counter = reinterpret_cast<unsigned*>(partials + blocks);
   uint8_t* alive = reinterpret_cast<uint8_t*>(counter + 4);
   const T* W = reinterpret_cast<const T*>(inverse);
-  init_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, reinterpret_cast<const T*>(rhs), n, b0, diag, alive, picks,
-                                             counter);
-  pick_kernel<T><<<1, kPickThreads, 0, st>>>(W, n, 0, b0, diag, alive, limited, limit, U, picks, removed);
+  const T* q = reinterpret_cast<const T*>(rhs);
+  size_t smem = 0;
+  if (FACTOR) {
+    smem = (size_t)n * sizeof(T);
+    if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(step_kernel<T, FACTOR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+      return DSG_ERR_LAUNCH;
+    factor_rows_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, q, n, b1);  // y = X q in b1
+    factor_init_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(W, b1, n, b0, diag, wdiag, alive, picks, counter);
+  } else {
+    init_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, q, n, b0, diag, wdiag, alive, picks, counter);
+  }
+  pick_kernel<T><<<1, kPickThreads, 0, st>>>(W, n, 0, b0, diag, alive, limited, limit, U, wdiag, picks, removed);
   for (int step = 0; step < count; ++step) {
     const T* bi = (step & 1) ? b1 : b0;
     T* bo = (step & 1) ? b0 : b1;
-    step_kernel<T><<<blocks, kRows * kSplit, 0, st>>>(W, n, step, count, bi, bo, diag, alive, U, limited, limit,
-                                                      picks + (step & 1), picks + ((step + 1) & 1), partials,
-                                                      counter, removed);
+    step_kernel<T, FACTOR><<<blocks, kRows * kSplit, smem, st>>>(
+        W, n, step, count, bi, bo, diag, wdiag, alive, U, limited, limit, picks + (step & 1),
+        picks + ((step + 1) & 1), partials, counter, removed);
   }
-  dsg_count_launches(2 + count);
+  dsg_count_launches((FACTOR ? 3 : 2) + count);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 
@@ -360,7 +437,7 @@ size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_comp
   if (n <= 0 || count < 0) return 0;
   const size_t elem = is_complex ? 16 : 8;
   const size_t blocks = ((size_t)n + kRows - 1) / kRows;
-  return elem * 2 * (size_t)n + 8 * (size_t)n + elem * (size_t)count * n + 2 * sizeof(Pick) +
+  return elem * 2 * (size_t)n + 16 * (size_t)n + elem * (size_t)count * n + 2 * sizeof(Pick) +
          blocks * sizeof(Candidate) + 16 + (size_t)n + 64;
 }
 
@@ -374,8 +451,22 @@ int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, in
     return DSG_ERR_WORKSPACE;
   if (reinterpret_cast<uintptr_t>(workspace) & 15u) return DSG_ERR_ARGUMENT;
   cudaStream_t st = (cudaStream_t)stream;
-  return is_complex ? run<Cplx>(inverse, rhs, n, count, limited, limit, workspace, removed, st)
-                    : run<double>(inverse, rhs, n, count, limited, limit, workspace, removed, st);
+  return is_complex ? run<Cplx, false>(inverse, rhs, n, count, limited, limit, workspace, removed, st)
+                    : run<double, false>(inverse, rhs, n, count, limited, limit, workspace, removed, st);
+}
+
+int dsg_backward_elimination_factor(const void* factor_inverse, const void* rhs, int32_t n, int32_t count,
+                                    const uint8_t* limited, int64_t limit, int32_t is_complex, void* workspace,
+                                    size_t workspace_bytes, int64_t* removed, void* stream) {
+  if (n < 0 || count < 0 || count > n) return DSG_ERR_ARGUMENT;
+  if (count == 0 || n == 0) return DSG_OK;
+  if (!factor_inverse || !rhs || !removed) return DSG_ERR_ARGUMENT;
+  if (!workspace || workspace_bytes < dsg_elimination_workspace_bytes(n, count, is_complex))
+    return DSG_ERR_WORKSPACE;
+  if (reinterpret_cast<uintptr_t>(workspace) & 15u) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  return is_complex ? run<Cplx, true>(factor_inverse, rhs, n, count, limited, limit, workspace, removed, st)
+                    : run<double, true>(factor_inverse, rhs, n, count, limited, limit, workspace, removed, st);
 }
 
 }  // extern "C"

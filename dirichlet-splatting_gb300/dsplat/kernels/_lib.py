@@ -92,6 +92,9 @@ SIGNATURES = {
     "dsg_synthesize_adc": (ctypes.c_int, [CP, F64, P, I32, P, P, P, I32, P, P]),
     "dsg_migration_focus": (ctypes.c_int, [P, I32, I32, I32, P, P, P, I32, I32, P, I32, P, P]),
     "dsg_backward_elimination": (ctypes.c_int, [P, P, I32, I32, P, I64, I32, P, SZ, P, P]),
+    "dsg_backward_elimination_factor": (ctypes.c_int, [P, P, I32, I32, P, I64, I32, P, SZ, P, P]),
+    "dsg_triangular_inverse_workspace_bytes": (SZ, [I32, I32]),
+    "dsg_triangular_inverse": (ctypes.c_int, [P, I32, I32, P, SZ, P, P]),
     "dsg_direction": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P]),
     "dsg_trial": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P, P]),
     "dsg_energy_workspace_bytes": (SZ, [I64]),

@@ -103,3 +103,61 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0):
         int(limit), int(complex_mode), ptr(work), nbytes, ptr(removed), _lib.stream(device),
     )  # fmt: skip
     return removed
+
+
+TRTRI_LEAF = 512  # blocks at most this size go to trtri; larger ones split in two
+
+
+def triangular_inverse(factor):
+    """L^-1 of a lower-triangular float64 / complex128 Cholesky factor.
+
+    Recursive halving, [[A, 0], [B, C]]^-1 = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]: the
+    off-diagonal block is two float64 GEMMs (cuBLAS runs those at the float64 tensor rate),
+    the diagonal blocks of at most TRTRI_LEAF rows are inverted by dsg_triangular_inverse
+    (cuSOLVER trtri, several times slower per flop at this size).
+    """
+    complex_mode = factor.is_complex()
+    factor = factor.to(torch.complex128 if complex_mode else torch.float64)
+    n = len(factor)
+    if n <= TRTRI_LEAF:
+        return _trtri(factor.clone().contiguous())
+    k = (n // 2 + 31) // 32 * 32
+    head = triangular_inverse(factor[:k, :k])
+    tail = triangular_inverse(factor[k:, k:])
+    out = torch.zeros_like(factor)
+    out[:k, :k] = head
+    out[k:, k:] = tail
+    out[k:, :k] = -(tail @ (factor[k:, :k] @ head))
+    return out
+
+
+def _trtri(x):
+    """In place on a contiguous lower-triangular block: its inverse (dsg_triangular_inverse)."""
+    complex_mode = x.is_complex()
+    n = len(x)
+    info = torch.zeros((1,), dtype=torch.int32, device=x.device)
+    nbytes = _lib.query("dsg_triangular_inverse_workspace_bytes", n, int(complex_mode))
+    work, nbytes = _lib.workspace(nbytes, x.device)
+    call("dsg_triangular_inverse", ptr(x), n, int(complex_mode), ptr(work), nbytes, ptr(info), _lib.stream(x.device))
+    return x
+
+
+def backward_elimination_factor(factor_inverse, rhs, count, limited=None, limit=0):
+    """backward_elimination from X = L^-1 (the inverse being X^H X), dsg_backward_elimination_factor."""
+    n = len(factor_inverse)
+    device = factor_inverse.device
+    removed = torch.empty((count,), dtype=torch.long, device=device)
+    if count == 0:
+        return removed
+    complex_mode = factor_inverse.is_complex()
+    dtype = torch.complex128 if complex_mode else torch.float64
+    x = factor_inverse.to(dtype).contiguous()
+    q = rhs.to(dtype).contiguous()
+    lim = None if limited is None else limited.to(torch.uint8).contiguous()
+    nbytes = _lib.query("dsg_elimination_workspace_bytes", n, count, int(complex_mode))
+    work, nbytes = _lib.workspace(nbytes, device)
+    call(
+        "dsg_backward_elimination_factor", ptr(x), ptr(q), n, count, None if lim is None else ptr(lim),
+        int(limit), int(complex_mode), ptr(work), nbytes, ptr(removed), _lib.stream(device),
+    )  # fmt: skip
+    return removed

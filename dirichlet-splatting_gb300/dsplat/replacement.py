@@ -96,21 +96,44 @@ def replace_one(state, config, pool, screen=None):
 
 def regularized_inverse(h, floor):
     """Inverse of h + floor lambda_max(h) I in double precision, or None."""
-    factor = shifted_cholesky(h, floor)
-    return None if factor is None else torch.cholesky_inverse(factor)
+    with stage("inverse.cholesky"):
+        factor = shifted_cholesky(h, floor)
+    if factor is None:
+        return None
+    with stage("inverse.invert"):
+        return torch.cholesky_inverse(factor)
 
 
-def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, on_device=False):
+def regularized_inverse_factor(h, floor):
+    """X = L^-1 with L the factor of regularized_inverse's shifted system (inverse = X^H X).
+
+    The batched replacement eliminates from X: a triangular inverse (trtri) costs a quarter
+    of forming the inverse (potri) at float64 on this GPU.
+    """
+    with stage("inverse.cholesky"):
+        factor = shifted_cholesky(h, floor)
+    if factor is None:
+        return None
+    with stage("inverse.invert"):
+        return search.triangular_inverse(factor)
+
+
+def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, on_device=False, factored=False):
     """Remove count unknowns one at a time from the least squares with this inverse.
 
     With W the inverse of the current system and b = W q, deleting unknown j and
     refitting raises the objective by |b_j|^2 / W_jj; each step deletes the cheapest
     and continues with W - w w^H / W_jj (w = W[:, j]), kept as rank-one corrections.
     At most limit of the unknowns marked in limited are removed. Returns the removed
-    indices in order. on_device runs the loop as two small CUDA kernels per step
+    indices in order. on_device runs the loop as one CUDA kernel per step
     (dsg_backward_elimination) instead of about ten PyTorch launches; the arithmetic is
-    the same up to the order of the float64 sums.
+    the same up to the order of the float64 sums. factored means inverse is the factor X
+    of regularized_inverse_factor (the inverse being X^H X).
     """
+    if factored:
+        if on_device and inverse.is_cuda:
+            return search.backward_elimination_factor(inverse, rhs, count, limited, limit)
+        inverse = inverse.mH @ inverse
     if on_device and inverse.is_cuda:
         return search.backward_elimination(inverse, rhs, count, limited, limit)
     size = len(inverse)
@@ -267,8 +290,10 @@ def merge_support(state, config, pool, scores=None):
     real = config.real
     eye = torch.eye(len(gram), dtype=gram.dtype, device=gram.device)
     h = (gram.real if real else gram) + config.ridge * eye
+    factored = getattr(config, "batched", False) and h.is_cuda
     with stage("replace.inverse"):
-        inverse = regularized_inverse(h, len(h) * torch.finfo(h.real.dtype).eps)
+        floor = len(h) * torch.finfo(h.real.dtype).eps
+        inverse = regularized_inverse_factor(h, floor) if factored else regularized_inverse(h, floor)
     if inverse is None:
         return state, 0
     q = rhs.real if real else rhs
@@ -277,7 +302,8 @@ def merge_support(state, config, pool, scores=None):
     while True:
         with stage("replace.elimination"):
             removed = backward_elimination(inverse, q, len(chosen), None if limit is None else old,
-                                           limit or 0, on_device=getattr(config, "batched", False))  # fmt: skip
+                                           limit or 0, on_device=getattr(config, "batched", False),
+                                           factored=factored)  # fmt: skip
         gone = torch.zeros(len(q), device=q.device, dtype=torch.bool)
         gone[removed] = True
         owners = gone[:count].nonzero().flatten()

@@ -320,6 +320,24 @@ int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, in
                              const uint8_t* limited, int64_t limit, int32_t is_complex, void* workspace,
                              size_t workspace_bytes, int64_t* removed, void* stream);
 
+/* Backward elimination from the lower-triangular inverse factor X = L^-1 (row-major,
+ * strictly upper part zero) of the pooled system's Cholesky factor L instead of the
+ * inverse W = X^H X itself (reference: dsplat/replacement.py:93-140, regularized_inverse
+ * followed by backward_elimination): the same removals, W's columns formed on the fly. */
+int dsg_backward_elimination_factor(const void* factor_inverse, const void* rhs, int32_t n, int32_t count,
+                                    const uint8_t* limited, int64_t limit, int32_t is_complex, void* workspace,
+                                    size_t workspace_bytes, int64_t* removed, void* stream);
+
+/* Device workspace of dsg_triangular_inverse, in bytes. */
+size_t dsg_triangular_inverse_workspace_bytes(int32_t n, int32_t is_complex);
+
+/* In place: a row-major lower-triangular float64 (complex128 when is_complex) factor L [n,n]
+ * becomes L^-1 (cuSOLVER trtri). info (one int32 on the device) is nonzero when L is
+ * singular. Replaces the potri inside dsplat/replacement.py:93-101 (cholesky_inverse) on
+ * the batched path. */
+int dsg_triangular_inverse(void* factor, int32_t n, int32_t is_complex, void* workspace, size_t workspace_bytes,
+                           int32_t* info, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,3 +82,30 @@ def test_batched_steps_never_raise_the_objective(fmcw):
         state = step(state, config)
     objectives = [entry["objective"] for entry in state.history]
     assert all(b <= a for a, b in itertools.pairwise(objectives)) and objectives[-1] < objectives[0]
+
+
+@pytest.mark.parametrize("complex_mode", [False, True])
+def test_factor_form_elimination_equals_the_eager_loop(complex_mode):
+    """The batched replacement eliminates from X = L^-1 (trtri) instead of the inverse
+    X^H X (potri): the triangular inverse matches torch's and the removal order matches the
+    PyTorch loop on the full inverse, with and without a limit."""
+    from dsplat.kernels import search
+    from dsplat.replacement import backward_elimination, regularized_inverse, regularized_inverse_factor
+
+    generator = torch.Generator().manual_seed(7)
+    dtype = torch.complex128 if complex_mode else torch.float64
+    x = torch.randn(400, 90, generator=generator, dtype=dtype)
+    h = (x.mH @ x).cuda()
+    q = (x.mH @ torch.randn(400, generator=generator, dtype=dtype)).cuda()
+    floor = len(h) * torch.finfo(torch.float32).eps
+    factor = torch.linalg.cholesky(h)
+    inverse_factor = search.triangular_inverse(factor)
+    assert torch.allclose(inverse_factor, torch.linalg.inv(factor), rtol=1e-9, atol=1e-12)
+    inverse = regularized_inverse(h, floor)
+    xfac = regularized_inverse_factor(h, floor)
+    assert torch.allclose(xfac.mH @ xfac, inverse, rtol=1e-8, atol=1e-10 * float(inverse.abs().max()))
+    limited = torch.arange(90, device="cuda") < 50
+    for lim, lmt in ((None, 0), (limited, 7)):
+        eager = backward_elimination(inverse, q, 30, lim, lmt)
+        device = backward_elimination(xfac, q, 30, lim, lmt, on_device=True, factored=True)
+        assert torch.equal(eager, device)
