@@ -9,7 +9,7 @@ search kernels.
 
 from __future__ import annotations
 
-from dataclasses import dataclass
+from dataclasses import dataclass, replace
 from math import ceil
 
 import torch
@@ -158,18 +158,7 @@ def search_certificate(
     masks = {key: spec.mask(feasible[key]) for key, spec in specs.items()}
     controls = _controls(reference, center_spec, normal_spec, masks)
 
-    def ascent(params, gradient):
-        """Negative gradient in scaled tangent coordinates (the quantity minimized)."""
-        parts = [
-            spec.tangent(gradient[:, 3 * i : 3 * i + 3], params[key]) * masks[key] * spec.scale
-            for i, (key, spec) in enumerate(specs.items())
-        ]
-        return -torch.cat(parts, -1)
-
-    def score(params, gradient=False, active=None):
-        return certificate(model, params, residual, mode, gradient=gradient,
-                           normals="normals" in specs, active=active)  # fmt: skip
-
+    ascent, score = _closures(model, residual, masks, specs, mode)
     coarse_scores = score(feasible) if initial_scores is None else initial_scores
     ids = select_peaks(coarse_scores, feasible["centers"], config.peaks, config.separation)
     coarse = {key: value[ids] for key, value in feasible.items()}
@@ -181,18 +170,10 @@ def search_certificate(
     inverse = eye.clone()
     fractions = [0.5**backtrack for backtrack in range(config.backtracks)]
 
-    def iterate(params, value, grad, inverse):
-        """One batched ascent iteration; returns the new (params, value, grad, inverse)."""
-        direction = search.direction(inverse, grad, params["normals"], controls[1], config.trust_radius)
-        old = {key: v.clone() for key, v in params.items()}
-        params, accepted = _backtrack_batched(old, direction, controls, fractions, value, specs, score)
-        new_value, new_grad = score(params, True)
-        new_grad = ascent(params, new_grad)
-        inverse = _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye)
-        return params, new_value, new_grad, inverse
-
+    iterate = _iteration(model, residual, controls, masks, specs, config, mode, fractions, eye)
     if batched and config.iterations > 1 and reference.is_cuda:
-        params, value, grad, inverse = _graphed_ascent(iterate, config.iterations, params, value, grad, inverse)
+        params, value, grad, inverse = _cached_ascent(model, residual, controls, masks, specs, config, mode,
+                                                      fractions, eye, params, value, grad, inverse)  # fmt: skip
     else:
         for _ in range(config.iterations):
             if batched:
@@ -230,6 +211,91 @@ def search_certificate(
     return {key: v[order] for key, v in combined.items()}, scores[order]
 
 
+def _closures(model, residual, masks, specs, mode):
+    """ascent(params, gradient) and score(params, gradient, active) of one search."""
+
+    def ascent(params, gradient):
+        """Negative gradient in scaled tangent coordinates (the quantity minimized)."""
+        parts = [
+            spec.tangent(gradient[:, 3 * i : 3 * i + 3], params[key]) * masks[key] * spec.scale
+            for i, (key, spec) in enumerate(specs.items())
+        ]
+        return -torch.cat(parts, -1)
+
+    def score(params, gradient=False, active=None):
+        return certificate(model, params, residual, mode, gradient=gradient,
+                           normals="normals" in specs, active=active)  # fmt: skip
+
+    return ascent, score
+
+
+def _iteration(model, residual, controls, masks, specs, config, mode, fractions, eye):
+    """One batched ascent iteration (params, value, grad, inverse) -> the same, all on device."""
+    ascent, score = _closures(model, residual, masks, specs, mode)
+
+    def iterate(params, value, grad, inverse):
+        direction = search.direction(inverse, grad, params["normals"], controls[1], config.trust_radius)
+        old = {key: v.clone() for key, v in params.items()}
+        params, accepted = _backtrack_batched(old, direction, controls, fractions, value, specs, score)
+        new_value, new_grad = score(params, True)
+        new_grad = ascent(params, new_grad)
+        inverse = _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye)
+        return params, new_value, new_grad, inverse
+
+    return iterate
+
+
+_ASCENTS: dict = {}
+
+
+def _cached_ascent(model, residual, controls, masks, specs, config, mode, fractions, eye, params, value, grad,
+                   inverse):  # fmt: skip
+    """The batched ascent replayed from a CUDA graph kept across searches of the same shape.
+
+    The graph reads the apertures, the residual, the controls and masks from static
+    buffers that every search refills, so a later search of the same shapes and settings
+    replays all its iterations without capturing again. Models without a scan of
+    apertures capture per search (_graphed_ascent).
+    """
+    from .kernels import _lib
+
+    if not hasattr(model, "scan") or not hasattr(model, "fresnel_n"):
+        iterate = _iteration(model, residual, controls, masks, specs, config, mode, fractions, eye)
+        return _graphed_ascent(iterate, config.iterations, params, value, grad, inverse)
+    positions = model.scan.scan_positions_m
+    key = (repr(model.scan.fmcw_config), model.fresnel_n, tuple(positions.shape), tuple(residual.shape),
+           residual.dtype, mode, repr(specs), repr(config), tuple(fractions), positions.device,
+           tuple((k, tuple(v.shape), v.dtype) for k, v in params.items()), tuple(grad.shape))  # fmt: skip
+    entry = _ASCENTS.get(key)
+    if entry is None:
+        # everything the graph reads by address stays referenced by the cache entry
+        static_inputs = {"positions": positions.clone(), "residual": residual.clone(), "controls": controls.clone(),
+                         "masks": {k: m.clone() for k, m in masks.items()}, "eye": eye.clone()}  # fmt: skip
+        static_model = replace(model, scan=replace(model.scan, scan_positions_m=static_inputs["positions"]))
+        iterate = _iteration(static_model, static_inputs["residual"], static_inputs["controls"],
+                             static_inputs["masks"], specs, config, mode, fractions, static_inputs["eye"])  # fmt: skip
+        params, value, grad, inverse = _graphed_ascent(iterate, config.iterations, params, value, grad, inverse,
+                                                       keep=(key, static_inputs))  # fmt: skip
+        return params, value, grad, inverse
+    graph, static_inputs, static, per_replay = entry
+    static_inputs["positions"].copy_(positions)
+    static_inputs["residual"].copy_(residual)
+    static_inputs["controls"].copy_(controls)
+    for k, m in masks.items():
+        static_inputs["masks"][k].copy_(m)
+    for k, v in params.items():
+        static[0][k].copy_(v)
+    static[1].copy_(value)
+    static[2].copy_(grad)
+    static[3].copy_(inverse)
+    with stage("ascent.replay"):
+        for _ in range(config.iterations):
+            graph.replay()
+    _lib.REPLAYED_LAUNCHES += per_replay * config.iterations
+    return ({k: v.clone() for k, v in static[0].items()}, static[1].clone(), static[2].clone(),
+            static[3].clone())  # fmt: skip
+
+
 def _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye):
     """Damped BFGS update of each candidate's inverse Hessian (skipped where invalid)."""
     step = torch.cat([(params[k] - old[k]) / spec.scale for k, spec in specs.items()], -1)
@@ -242,7 +308,7 @@ def _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye):
     return torch.where(valid[:, None, None], updated, inverse)
 
 
-def _graphed_ascent(iterate, iterations, params, value, grad, inverse):
+def _graphed_ascent(iterate, iterations, params, value, grad, inverse, keep=None):
     """Run the batched ascent: one eager iteration, then the rest replayed from a CUDA graph.
 
     The iteration reads and writes only device tensors of fixed shapes, so the graph
@@ -276,6 +342,8 @@ def _graphed_ascent(iterate, iterations, params, value, grad, inverse):
             for _ in range(iterations - 1):
                 graph.replay()
         _lib.REPLAYED_LAUNCHES += per_replay * (iterations - 1)
+        if keep is not None:  # (key, static inputs) of _cached_ascent
+            _ASCENTS[keep[0]] = (graph, keep[1], static, per_replay)
     finally:
         _lib.TIMERS = timers
     return ({k: v.clone() for k, v in static[0].items()}, static[1].clone(), static[2].clone(),

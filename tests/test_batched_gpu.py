@@ -68,6 +68,17 @@ def test_batched_certificate_search_matches_the_sequential_search(fmcw):
                                          normal_spec=specs["normals"], batched=True)  # fmt: skip
     close(bat_scores, seq_scores, 1e-4)
     close(bat["centers"], seq["centers"], 1e-4)
+    # A second search of the same shapes replays the cached graph with new inputs: a
+    # different residual and start, against a fresh sequential search.
+    residual2 = residual * 0.7 + 0.3 * residual.flip(0)
+    start2 = dict(start, centers=start["centers"] + (2e-4 * torch.randn(start["centers"].shape,
+                                                                          generator=generator)).cuda())  # fmt: skip
+    seq2, seq2_scores = search_certificate(model, residual2, start2, specs["centers"], config, "real",
+                                           normal_spec=specs["normals"])  # fmt: skip
+    bat2, bat2_scores = search_certificate(model, residual2, start2, specs["centers"], config, "real",
+                                           normal_spec=specs["normals"], batched=True)  # fmt: skip
+    close(bat2_scores, seq2_scores, 1e-4)
+    close(bat2["centers"], seq2["centers"], 1e-4)
 
 
 def test_batched_steps_never_raise_the_objective(fmcw):
