@@ -15,7 +15,7 @@
 // CTA of 21 warps, persistent over work units of (aperture, 256 surfels):
 //   warps 0-15  geometry of the unit's 256 pairs (one per thread of warps 0-7), then the
 //               dictionary tiles, one K-subtile (32 bins of 128 surfels, 8 surfels per
-//               warp) per pipeline stage;
+//               warp, four bins per lane) per pipeline stage;
 //   warps 16-19 epilogue: tcgen05.ld of a finished accumulator, bf16 split, a transpose
 //               through shared memory, and row-contiguous stores of PT;
 //   warp 20     TMEM allocation, the TMA copy of U, and the MMA issue (one thread).
@@ -220,44 +220,46 @@ __global__ void __launch_bounds__(PTHREADS, 1)
           if (ok) {
             uint8_t* hi = stage_base + slot * STAGE_BYTES;
             uint8_t* lo = hi + A_SUB;
-            // A lane evaluates bins k, k + 1 of one row; the two half-warps take
-            // neighbouring rows, so a store instruction fills two whole 128-byte rows.
-            const int half = lane >> 4, pair = lane & 15;
-            const int k = j * 32 + 2 * pair;
-            const uint32_t pair_bytes = (uint32_t)(pair & 1) << 3;
-            const int chunk = pair >> 1;
+            // A lane evaluates four neighbouring bins of one row (one 16-byte chunk of the
+            // swizzled row); eight lanes fill a row, so a store instruction fills four rows.
+            const int quad = lane >> 3, pos = lane & 7;
+            const int k = j * 32 + 4 * pos;
 #pragma unroll
-            for (int i = 0; i < ROWS_PER_WARP / 2; ++i) {
-              const int row = warp * ROWS_PER_WARP + 2 * i + half;  // surfel within the tile
+            for (int i = 0; i < ROWS_PER_WARP / 4; ++i) {
+              const int row = warp * ROWS_PER_WARP + 4 * i + quad;  // surfel within the tile
               const float* r = recs + (u * TM + row) * REC;
               const float2 tl_lobe = *reinterpret_cast<const float2*>(r + 2 * P);
               const float tl = tl_lobe.x;
               const int m = k - __float_as_int(tl_lobe.y);  // bin offset from the lobe
-              float2 g0, g1;  // numerators of bins k and k + 1
+              float2 g[4];  // numerators of bins k .. k + 3
               if (P == 1) {
-                g0 = g1 = *reinterpret_cast<const float2*>(r);
+                g[0] = g[1] = g[2] = g[3] = *reinterpret_cast<const float2*>(r);
               } else if (P == 2) {
                 const float4 both = *reinterpret_cast<const float4*>(r);
                 const bool odd = (m & 1) != 0;
-                g0 = odd ? make_float2(both.z, both.w) : make_float2(both.x, both.y);
-                g1 = odd ? make_float2(both.x, both.y) : make_float2(both.z, both.w);
+                g[0] = g[2] = odd ? make_float2(both.z, both.w) : make_float2(both.x, both.y);
+                g[1] = g[3] = odd ? make_float2(both.x, both.y) : make_float2(both.z, both.w);
               } else {
-                g0 = *reinterpret_cast<const float2*>(r + 2 * (m & (P - 1)));
-                g1 = *reinterpret_cast<const float2*>(r + 2 * ((m + 1) & (P - 1)));
+#pragma unroll
+                for (int t = 0; t < 4; ++t) g[t] = *reinterpret_cast<const float2*>(r + 2 * ((m + t) & (P - 1)));
               }
-              const float2 t = table[m + c.N - 1];
-              const float c0 = cot_from(t.x, tl), c1 = cot_from(t.y, tl);
-              const float re0 = g0.x * c0 - g0.y, im0 = g0.y * c0 + g0.x;
-              const float re1 = g1.x * c1 - g1.y, im1 = g1.y * c1 + g1.x;
-              const __nv_bfloat162 h0 = __floats2bfloat162_rn(re0, im0);
-              const __nv_bfloat162 h1 = __floats2bfloat162_rn(re1, im1);
-              const __nv_bfloat162 l0 = __floats2bfloat162_rn(re0 - __low2float(h0), im0 - __high2float(h0));
-              const __nv_bfloat162 l1 = __floats2bfloat162_rn(re1 - __low2float(h1), im1 - __high2float(h1));
+              const float2 t01 = table[m + c.N - 1], t23 = table[m + c.N + 1];
+              const float tan4[4] = {t01.x, t01.y, t23.x, t23.y};
+              uint32_t hw[4], lw[4];
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const float cot = cot_from(tan4[t], tl);
+                const float re = g[t].x * cot - g[t].y, im = g[t].y * cot + g[t].x;
+                const __nv_bfloat162 h = __floats2bfloat162_rn(re, im);
+                const __nv_bfloat162 l = __floats2bfloat162_rn(re - __low2float(h), im - __high2float(h));
+                hw[t] = bf16x2_bits(h);
+                lw[t] = bf16x2_bits(l);
+              }
               // K-major, 128-byte swizzle: row, then the 16-byte chunk XOR (row mod 8)
               const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128) +
-                                   ((uint32_t)(chunk ^ (row & 7)) << 4) + pair_bytes;
-              *reinterpret_cast<uint2*>(hi + off) = make_uint2(bf16x2_bits(h0), bf16x2_bits(h1));
-              *reinterpret_cast<uint2*>(lo + off) = make_uint2(bf16x2_bits(l0), bf16x2_bits(l1));
+                                   ((uint32_t)(pos ^ (row & 7)) << 4);
+              *reinterpret_cast<uint4*>(hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+              *reinterpret_cast<uint4*>(lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           }
