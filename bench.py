@@ -39,7 +39,7 @@ for _path in (ROOT, ROOT / "dirichlet-splatting_gb300"):
 
 import torch  # noqa: E402
 
-METRIC = "DSFW steps/s (128^2 array, 2k surfels, batch 256)"
+METRIC = "DSFW steps/s (128² array, 2k surfels) mixed+batched vs plain FP32; equal NMSE"
 UNIT = "steps/s"
 WORKLOAD = "dsfw_sphere_cap_128x128_s2000_b256"
 
