@@ -84,3 +84,20 @@ def test_range_response_matches_the_oracle():
     config = FMCWConfig()
     got = range_response(config, 62.0, 90.8, 461, "cuda").cpu()
     torch.testing.assert_close(got, ofmcw.range_response(config, 62.0, 90.8, 461), rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("dimension,separation", [(1, 0.002), (2, 0.03), (3, 0.02), (4, 0.3)])
+def test_peaks_in_every_dimension_and_dense_clusters(dimension, separation):
+    """Clustered candidates (many suppressed, many taken), up to the 4096-peak limit; one to
+    three dimensions take the hashed single-warp kernel, four the block kernel."""
+    from dsplat.kernels import search
+
+    generator = torch.Generator().manual_seed(dimension)
+    seeds = torch.rand(300, dimension, generator=generator)
+    centers = seeds[torch.randint(0, 300, (20000,), generator=generator)]
+    centers = centers + 0.01 * torch.randn(20000, dimension, generator=generator)
+    scores = torch.rand(20000, generator=generator)
+    scores[::7] = -torch.inf
+    for count in (1, 300, 4096):
+        got = search.peaks(scores.cuda(), centers.cuda(), count, separation).cpu()
+        assert got.tolist() == osearch.peaks(scores, centers, count, separation).tolist(), count
