@@ -408,7 +408,9 @@ int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* l
   if (FACTOR) {
     smem = (size_t)n * sizeof(T);
     if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024 &&
+    cudaFuncAttributes attributes;
+    if (cudaFuncGetAttributes(&attributes, step_kernel<T, FACTOR>) != cudaSuccess) return DSG_ERR_LAUNCH;
+    if (smem + attributes.sharedSizeBytes > 48 * 1024 &&  // dynamic plus static above the default
         cudaFuncSetAttribute(step_kernel<T, FACTOR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
       return DSG_ERR_LAUNCH;

@@ -29,6 +29,7 @@ __global__ void range_gate_kernel(const float* __restrict__ points, int count,
 
 constexpr int kPeakThreads = 1024;
 constexpr int kMaxAccepted = 4096;  // peaks held in shared memory per launch
+constexpr size_t kStaticSmem = 8 * 1024;  // bound on the static shared arrays of these kernels
 
 // Greedy separated peaks over candidates visited in descending-score order (ties in
 // index order): a candidate is taken unless it lies within separation of one already
@@ -245,7 +246,7 @@ int dsg_peaks(const float* scores, const int32_t* order, const float* centers, i
   cudaMemsetAsync(output, 0xff, (size_t)peaks * sizeof(int32_t), (cudaStream_t)stream);
   if (count == 0) return status();
   const size_t smem = (size_t)peaks * dimension * sizeof(float);
-  if (smem > 48 * 1024 &&
+  if (smem + kStaticSmem > 48 * 1024 &&  // dynamic plus the static arrays above the default
       cudaFuncSetAttribute(peaks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
     return DSG_ERR_LAUNCH;
@@ -266,7 +267,7 @@ int dsg_distinct(const float* scores, const int32_t* order, const float* points,
     return DSG_ERR_ARGUMENT;
   const size_t smem = (size_t)(n_occupied + width) * dimension * sizeof(float);
   if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
-  if (smem > 48 * 1024 &&
+  if (smem + kStaticSmem > 48 * 1024 &&  // dynamic plus the static arrays above the default
       cudaFuncSetAttribute(distinct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return DSG_ERR_LAUNCH;

@@ -120,3 +120,22 @@ def test_factor_form_elimination_equals_the_eager_loop(complex_mode):
         eager = backward_elimination(inverse, q, 30, lim, lmt)
         device = backward_elimination(xfac, q, 30, lim, lmt, on_device=True, factored=True)
         assert torch.equal(eager, device)
+
+
+def test_factor_form_elimination_at_the_pooled_size():
+    """2256 unknowns (2000 support + 256 pooled), complex and real: the column of the
+    inverse factor staged in shared memory is 36 KB (complex), above the default 48 KB
+    once the static arrays are added."""
+    from dsplat.kernels import search
+    from dsplat.replacement import backward_elimination
+
+    for dtype in (torch.float64, torch.complex128):
+        generator = torch.Generator().manual_seed(11)
+        x = torch.randn(2600, 2256, generator=generator, dtype=dtype).cuda()
+        h = x.mH @ x
+        q = x.mH @ torch.randn(2600, generator=generator, dtype=dtype).cuda()
+        factor = search.triangular_inverse(torch.linalg.cholesky(h))
+        inverse = factor.mH @ factor
+        eager = backward_elimination(inverse, q, 12)
+        device = backward_elimination(factor, q, 12, on_device=True, factored=True)
+        assert torch.equal(eager, device)

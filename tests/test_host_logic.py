@@ -3,6 +3,8 @@ elimination, regularized inverses and utilities (CPU float64)."""
 
 from __future__ import annotations
 
+import math
+
 import pytest
 import torch
 
@@ -187,3 +189,24 @@ def test_row_basis_rank_of_the_sphere_cap_band():
     values = torch.linalg.svdvals(response)
     rank = int((values > torch.finfo(torch.float32).eps / 128 * values[0]).sum())
     assert 25 <= rank <= 35
+
+
+@pytest.mark.parametrize("complex_mode", [False, True])
+def test_refined_solve_reaches_float64_accuracy_or_declines(complex_mode):
+    """Float32 factor + float64 refinement: float64-accurate on a system of condition ~1e4,
+    and None (the float64 path takes over) on one of condition ~1e10."""
+    from dsplat.varpro import refined_solve
+
+    generator = torch.Generator().manual_seed(3)
+    dtype = torch.complex128 if complex_mode else torch.float64
+    q, _ = torch.linalg.qr(torch.randn(80, 80, generator=generator, dtype=dtype))
+    rhs = torch.randn(80, generator=generator, dtype=dtype)
+    for condition, expect in ((1e4, True), (1e10, False)):
+        values = torch.logspace(0, -math.log10(condition), 80, dtype=torch.float64)
+        h = (q * values.to(dtype)) @ q.mH
+        x = refined_solve(h, rhs)
+        if expect:
+            exact = torch.linalg.solve(h, rhs)
+            assert float((x - exact).norm() / exact.norm()) < 1e-10
+        else:
+            assert x is None
