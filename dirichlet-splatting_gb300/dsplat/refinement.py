@@ -48,7 +48,7 @@ def reduced_system(model, params, target, specs, config, rows):
     cross[atoms.repeat_interleave(da.shape[-1]), columns] += (
         (da.conj() * residual[:, None, None]).sum(0).flatten() / m
     )
-    db = -solve(h, cross.real if config.real else cross)
+    db = -solve(h, cross.real if config.real else cross, refined=getattr(config, "batched", False))
     reduced = j + a @ db.to(a.dtype)
     normal = (reduced.H @ reduced / m + config.ridge * db.H @ db).real
     gradient = (reduced.H @ residual / m + config.ridge * db.H @ b).real
@@ -82,7 +82,7 @@ def dense_slide(state, config, screen=None):
         normal, gradient = reduced_system(state.model, state.params, state.target,
                                           state.parameters, config, rows)  # fmt: skip
         scale = normal.diag().clamp(min=normal.diag().max() * 1e-6 + 1e-30)
-        delta = solve(normal + config.damping * torch.diag(scale), -gradient)
+        delta = solve(normal + config.damping * torch.diag(scale), -gradient, refined=getattr(config, "batched", False))
         delta = delta.reshape(len(state.coefficients), -1)
         length = delta.norm(dim=1, keepdim=True).clamp(min=1e-30)
         delta *= (config.trust_radius / length).clamp(max=1)

@@ -66,45 +66,57 @@ def shifted_cholesky(h, floor):
     return None
 
 
-def refined_solve(h, rhs, iterations=4, tolerance=1e-11):
-    """Float64 solve from a float32 Cholesky factor and float64 iterative refinement.
+def refined_solve(h, rhs, iterations=3, tolerance=1e-13):
+    """Solve of a float64 system from a float32 Cholesky factor with float64 refinement.
 
-    On this GPU a float32 factorization costs a sixth of the float64 one; each refinement
-    step is a float64 residual and a float32 triangular solve. Returns None (the caller
-    then factors in float64) when the float32 factor fails or the refined residual stays
-    above tolerance relative to the right-hand side, which happens only for systems whose
-    condition number approaches 1 / float32 epsilon.
+    On this GPU a float32 factorization costs a seventh of the float64 one; each
+    refinement step is a float64 residual and a float32 triangular solve pair. Returns
+    None (the caller then factors in float64) when the float32 factor fails or the
+    normwise backward error |q - h x| / (|h|_F |x| + |q|) stays above tolerance, which
+    happens only for systems whose condition number approaches 1 / float32 epsilon. One
+    device read decides both.
     """
     low = torch.complex64 if h.is_complex() else torch.float32
     chol, info = torch.linalg.cholesky_ex(h.to(low))
-    if int(info) != 0:
-        return None
     q = rhs[:, None] if rhs.ndim == 1 else rhs
     q = q.to(h.dtype)
     x = torch.cholesky_solve(q.to(low), chol).to(h.dtype)
     for _ in range(iterations):
-        residual = q - h @ x
-        x = x + torch.cholesky_solve(residual.to(low), chol).to(h.dtype)
-    residual = (q - h @ x).norm() / q.norm().clamp(min=1e-300)
-    if not float(residual) <= tolerance:
+        x = x + torch.cholesky_solve((q - h @ x).to(low), chol).to(h.dtype)
+    error = (q - h @ x).norm() / (torch.linalg.matrix_norm(h) * x.norm() + q.norm()).clamp(min=1e-300)
+    if not bool((info == 0) & (error <= tolerance)):  # a failed factor leaves NaN in error
         return None
     return x[:, 0] if rhs.ndim == 1 else x
 
 
-def solve(h, rhs):
+def solve(h, rhs, refined=False):
     """Hermitian solve; a singular system is shifted to where a pseudoinverse would truncate.
 
     The shift len(h) eps lambda_max only moves the solution along near-null directions,
-    which the prediction does not see.
+    which the prediction does not see. refined solves the shifted float64 system with
+    refined_solve (float32 factor, float64 refinement) before factoring it in float64;
+    both give its solution to float64 accuracy before the cast back to the input type.
     """
     q = rhs[:, None] if rhs.ndim == 1 else rhs
     chol, info = torch.linalg.cholesky_ex(h)
     if int(info) != 0:
-        chol = shifted_cholesky(h, len(h) * torch.finfo(h.real.dtype).eps)
+        floor = len(h) * torch.finfo(h.real.dtype).eps
+        if refined and h.is_cuda:
+            x = shifted_refined_solve(h, q, floor)
+            if x is not None:
+                return (x[:, 0] if rhs.ndim == 1 else x).to(rhs.dtype)
+        chol = shifted_cholesky(h, floor)
     if chol is None:  # every column is zero: nothing to fit
         return torch.zeros_like(rhs)
     x = torch.cholesky_solve(q.to(chol.dtype), chol).to(q.dtype)
     return x[:, 0] if rhs.ndim == 1 else x
+
+
+def shifted_refined_solve(h, q, floor):
+    """(h + floor lambda_max(h) I)^-1 q at the first shift of shifted_cholesky, or None."""
+    matrix = h.to(torch.complex128 if h.is_complex() else torch.float64, copy=True)
+    matrix.diagonal().add_(floor * largest_eigenvalue(matrix))
+    return refined_solve(matrix, q)
 
 
 def row_chunk(model, columns, config):
@@ -210,19 +222,13 @@ def normal_equations(model, params, target, config):
 def fit_coefficients(gram, rhs, config):
     """Minimizer of b^H G b - 2 Re(b^H q) + ridge |b|^2 in the configured domain.
 
-    With DSFWConfig.batched a float64 system is first solved by refined_solve (float32
-    factor, float64 refinement); solve's float64 path takes over when that does not
-    converge, so the coefficients agree to float64 accuracy either way.
+    With DSFWConfig.batched a system that needs solve's shifted float64 factorization is
+    first solved by refined_solve; the coefficients agree to float64 accuracy either way.
     """
     if config.real:
         gram, rhs = gram.real, rhs.real
     eye = torch.eye(len(gram), dtype=gram.dtype, device=gram.device)
-    h = gram + config.ridge * eye
-    if getattr(config, "batched", False) and h.is_cuda and h.dtype in (torch.float64, torch.complex128):
-        x = refined_solve(h, rhs)
-        if x is not None:
-            return x.to(rhs.dtype)
-    return solve(h, rhs)
+    return solve(gram + config.ridge * eye, rhs, refined=getattr(config, "batched", False))
 
 
 def rendered_loss(model, params, coefficients, target, ridge):

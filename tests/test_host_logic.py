@@ -210,3 +210,20 @@ def test_refined_solve_reaches_float64_accuracy_or_declines(complex_mode):
             assert float((x - exact).norm() / exact.norm()) < 1e-10
         else:
             assert x is None
+
+
+def test_shifted_refined_solve_matches_the_float64_shift():
+    """A float32 Gram of rank n/2 fails float32 Cholesky; its shifted system solved from a
+    float32 factor with float64 refinement equals the float64 factorization's solution."""
+    from dsplat.varpro import shifted_cholesky, shifted_refined_solve
+
+    generator = torch.Generator().manual_seed(5)
+    n = 200
+    a = torch.randn(3 * n, n // 2, generator=generator) @ torch.randn(n // 2, n, generator=generator) / n
+    h = a.T @ a / len(a)
+    assert int(torch.linalg.cholesky_ex(h)[1]) != 0
+    q = torch.randn(n, 1, generator=generator)
+    floor = n * torch.finfo(torch.float32).eps
+    expected = torch.cholesky_solve(q.double(), shifted_cholesky(h, floor))
+    x = shifted_refined_solve(h, q, floor)
+    assert x is not None and float((x - expected).norm() / expected.norm()) < 1e-10
