@@ -259,6 +259,8 @@ def _cached_ascent(model, residual, controls, masks, specs, config, mode, fracti
     """
     from .kernels import _lib
 
+    if _fusable(model, params, fractions):
+        return _fused_ascent(model, residual, controls, specs, config, mode, fractions, params, value, grad, inverse)
     if not hasattr(model, "scan") or not hasattr(model, "fresnel_n"):
         iterate = _iteration(model, residual, controls, masks, specs, config, mode, fractions, eye)
         return _graphed_ascent(iterate, config.iterations, params, value, grad, inverse)
@@ -294,6 +296,115 @@ def _cached_ascent(model, residual, controls, masks, specs, config, mode, fracti
     _lib.REPLAYED_LAUNCHES += per_replay * config.iterations
     return ({k: v.clone() for k, v in static[0].items()}, static[1].clone(), static[2].clone(),
             static[3].clone())  # fmt: skip
+
+
+def _fusable(model, params, fractions):
+    """Surfel models on CUDA whose candidates carry centers, normals and areas only."""
+    return (hasattr(model, "scan") and hasattr(model, "sensor") and hasattr(model, "fresnel_n")
+            and sorted(params) == ["areas", "centers", "normals"] and params["centers"].is_cuda
+            and 1 <= len(fractions) <= 16)  # fmt: skip
+
+
+def _fused_iteration(model, residual, power, controls, specs, config, mode, fractions):
+    """One batched ascent iteration on the state buffers, in place, in eight launches.
+
+    The correlations run on the surfel kernels without the area factors, which the
+    fused kernels apply: dsg_trials, the full-step correlation, dsg_ascent_partition,
+    the active-set correlation of the smaller fractions, dsg_ascent_select, the
+    correlation gradient and dsg_ascent_update replace the PyTorch algebra of
+    _iteration (the same arithmetic, up to the order of float sums).
+    """
+    from .kernels import surfel as kernel
+
+    chirp, positions = model.sensor
+    shaped = residual.reshape(model.shape)
+    real_mode = mode == "real"
+    spec = search.ascent_spec(specs)
+    move_normals = "normals" in specs
+
+    def iterate(params, value, grad, inverse):
+        centers, normals, areas = params["centers"], params["normals"], params["areas"]
+        direction = search.direction(inverse, grad, normals, controls[1], config.trust_radius)
+        trial_centers, trial_normals = search.trials(centers, normals, direction, controls, fractions)
+        corr, norm = kernel.correlate(chirp, positions, trial_centers[0], trial_normals[0], shaped, model.fresnel_n)
+        improved, position, pending, batch_centers, batch_normals = search.ascent_partition(
+            corr, norm, areas, power, real_mode, value, trial_centers, trial_normals)  # fmt: skip
+        corr2 = norm2 = None
+        if len(fractions) > 1:
+            corr2, norm2 = kernel.correlate(chirp, positions, batch_centers, batch_normals, shaped, model.fresnel_n,
+                                            active=(pending, len(value)))  # fmt: skip
+        new_centers, new_normals, accepted = search.ascent_select(
+            corr2, norm2, areas, power, real_mode, value, improved, position, trial_centers, trial_normals,
+            centers, normals, move_normals)  # fmt: skip
+        c, n, dc, dn = kernel.correlate_gradient(chirp, positions, new_centers, new_normals, shaped, model.fresnel_n,
+                                                 move_normals)  # fmt: skip
+        search.ascent_update(spec, c, n, dc, dn, areas, power, real_mode, new_centers, new_normals, accepted,
+                             centers, normals, value, grad, inverse)  # fmt: skip
+
+    return iterate
+
+
+def _fused_ascent(model, residual, controls, specs, config, mode, fractions, params, value, grad, inverse):
+    """The fused batched ascent, its graph kept across searches of the same shapes.
+
+    The state (parameters, value, gradient, inverse) and the inputs (apertures, residual
+    and its power, controls) live in static buffers that every search refills; the first
+    search runs one iteration eagerly (the capture's warm-up), captures the next and
+    replays it, a later one replays every iteration.
+    """
+    from .kernels import _lib
+
+    positions = model.scan.scan_positions_m
+    key = ("fused", repr(model.scan.fmcw_config), model.fresnel_n, tuple(positions.shape), tuple(residual.shape),
+           residual.dtype, mode, repr(specs), repr(config), tuple(fractions), positions.device,
+           tuple((k, tuple(v.shape)) for k, v in params.items()), tuple(grad.shape))  # fmt: skip
+    power = residual.abs().square().sum().double().clamp(min=1e-30).reshape(1)
+    entry = _ASCENTS.get(key)
+    if entry is not None:
+        graph, inputs, state, per_replay = entry
+        inputs["positions"].copy_(positions)
+        inputs["residual"].copy_(residual)
+        inputs["controls"].copy_(controls)
+        inputs["power"].copy_(power)
+        for k, v in params.items():
+            state[0][k].copy_(v)
+        state[1].copy_(value)
+        state[2].copy_(grad)
+        state[3].copy_(inverse)
+        with stage("ascent.replay"):
+            for _ in range(config.iterations):
+                graph.replay()
+        _lib.REPLAYED_LAUNCHES += per_replay * config.iterations
+    else:
+        inputs = {"positions": positions.clone(), "residual": residual.contiguous().clone(),
+                  "controls": controls.contiguous().clone(), "power": power.clone()}  # fmt: skip
+        state = ({k: v.float().contiguous().clone() for k, v in params.items()}, value.float().contiguous().clone(),
+                 grad.float().contiguous().clone(), inverse.float().contiguous().clone())  # fmt: skip
+        static_model = replace(model, scan=replace(model.scan, scan_positions_m=inputs["positions"]))
+        iterate = _fused_iteration(static_model, inputs["residual"], inputs["power"], inputs["controls"], specs,
+                                   config, mode, fractions)  # fmt: skip
+        device = value.device
+        side = torch.cuda.Stream(device)
+        side.wait_stream(torch.cuda.current_stream(device))
+        timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be timed inside a graph
+        try:
+            with stage("ascent.capture"):
+                with torch.cuda.stream(side):
+                    iterate(*state)
+                torch.cuda.current_stream(device).wait_stream(side)
+                graph = torch.cuda.CUDAGraph()
+                before = _lib.library().dsg_launch_count()
+                with torch.cuda.graph(graph):
+                    iterate(*state)
+                per_replay = _lib.library().dsg_launch_count() - before
+            with stage("ascent.replay"):
+                for _ in range(config.iterations - 1):
+                    graph.replay()
+            _lib.REPLAYED_LAUNCHES += per_replay * (config.iterations - 1)
+            _ASCENTS[key] = (graph, inputs, state, per_replay)
+        finally:
+            _lib.TIMERS = timers
+    return ({k: v.clone() for k, v in state[0].items()}, state[1].clone(), state[2].clone(), state[3].clone())
 
 
 def _bfgs_update(inverse, old, params, grad, new_grad, accepted, specs, eye):

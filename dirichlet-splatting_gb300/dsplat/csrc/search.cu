@@ -1,6 +1,6 @@
 // Candidate kernels of the spatial search: range gate, greedy separated peaks, the
-// per-candidate quasi-Newton direction and the trial step (reference:
-// dsplat/kernels/search.slang:1-109).
+// per-candidate quasi-Newton direction and the trial step, one fraction or all the
+// backtracking fractions of an iteration (reference: dsplat/kernels/search.slang:1-109).
 #include <cuda_runtime.h>
 #include <math.h>
 #include "dsplat_gb300.h"
@@ -199,13 +199,12 @@ __global__ void direction_kernel(const float* __restrict__ inverse,
   for (int j = 0; j < width; ++j) output[i * width + j] = d[j] * scale;
 }
 
-__global__ void trial_kernel(const float* __restrict__ centers, const float* __restrict__ normals,
-                             const float* __restrict__ direction,
-                             const float* __restrict__ controls, int count, int width,
-                             float fraction, float* __restrict__ out_centers,
-                             float* __restrict__ out_normals) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
+// One candidate's trial step: centers move by fraction * scale * direction on their
+// free axes and are clamped to the box; normals (width 6) move and are renormalized.
+__device__ __forceinline__ void trial_one(const float* __restrict__ centers, const float* __restrict__ normals,
+                                          const float* __restrict__ direction,
+                                          const float* __restrict__ controls, int i, int width, float fraction,
+                                          float* __restrict__ out_centers, float* __restrict__ out_normals) {
   float n[3], len2 = 0.0f;
   for (int j = 0; j < 3; ++j) {
     const float c = centers[3 * i + j] + fraction * controls[j] * direction[i * width + j];
@@ -217,6 +216,34 @@ __global__ void trial_kernel(const float* __restrict__ centers, const float* __r
   }
   const float inv = width == 6 ? 1.0f / sqrtf(len2) : 1.0f;
   for (int j = 0; j < 3; ++j) out_normals[3 * i + j] = width == 6 ? n[j] * inv : normals[3 * i + j];
+}
+
+__global__ void trial_kernel(const float* __restrict__ centers, const float* __restrict__ normals,
+                             const float* __restrict__ direction,
+                             const float* __restrict__ controls, int count, int width,
+                             float fraction, float* __restrict__ out_centers,
+                             float* __restrict__ out_normals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  trial_one(centers, normals, direction, controls, i, width, fraction, out_centers, out_normals);
+}
+
+constexpr int kMaxFractions = 16;
+struct Fractions {
+  float value[kMaxFractions];
+};
+
+// Every backtracking fraction of an iteration in one launch: blockIdx.y picks the
+// fraction, whose trials fill rows [y * count, (y + 1) * count) of the outputs.
+__global__ void trials_kernel(const float* __restrict__ centers, const float* __restrict__ normals,
+                              const float* __restrict__ direction, const float* __restrict__ controls,
+                              int count, int width, Fractions fractions, float* __restrict__ out_centers,
+                              float* __restrict__ out_normals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const size_t row = (size_t)blockIdx.y * count * 3;
+  trial_one(centers, normals, direction, controls, i, width, fractions.value[blockIdx.y], out_centers + row,
+            out_normals + row);
 }
 
 int status() { return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH; }
@@ -299,6 +326,24 @@ int dsg_trial(const float* centers, const float* normals, const float* direction
     return DSG_ERR_ARGUMENT;
   trial_kernel<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
       centers, normals, direction, controls, count, width, fraction, out_centers, out_normals);
+  dsg_count_launches(1);
+  return status();
+}
+
+int dsg_trials(const float* centers, const float* normals, const float* direction,
+               const float* controls, int32_t count, int32_t width, const float* fractions,
+               int32_t fraction_count, float* out_centers, float* out_normals, void* stream) {
+  if (count < 0 || (width != 3 && width != 6) || fraction_count < 1 || fraction_count > kMaxFractions ||
+      !fractions)
+    return DSG_ERR_ARGUMENT;
+  if (count == 0) return DSG_OK;
+  if (!centers || !normals || !direction || !controls || !out_centers || !out_normals)
+    return DSG_ERR_ARGUMENT;
+  Fractions f{};
+  for (int b = 0; b < fraction_count; ++b) f.value[b] = fractions[b];
+  const dim3 grid((unsigned)((count + 127) / 128), (unsigned)fraction_count);
+  trials_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(centers, normals, direction, controls, count, width, f,
+                                                        out_centers, out_normals);
   dsg_count_launches(1);
   return status();
 }

@@ -54,7 +54,17 @@ I64 = ctypes.c_int64
 F32 = ctypes.c_float
 F64 = ctypes.c_double
 SZ = ctypes.c_size_t
+class AscentSpec(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32),
+        ("normalize", ctypes.c_int32 * 2),
+        ("scale", ctypes.c_float * 2),
+        ("mask", ctypes.c_float * 6),
+    ]
+
+
 CP = ctypes.POINTER(Chirp)
+AP = ctypes.POINTER(AscentSpec)
 GP = ctypes.POINTER(Grid)
 
 # name: (restype, argtypes); the order and types follow include/dsplat_gb300.h.
@@ -97,6 +107,10 @@ SIGNATURES = {
     "dsg_triangular_inverse": (ctypes.c_int, [P, I32, I32, P, SZ, P, P]),
     "dsg_direction": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P]),
     "dsg_trial": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P, P]),
+    "dsg_trials": (ctypes.c_int, [P, P, P, P, I32, I32, P, I32, P, P, P]),
+    "dsg_ascent_partition": (ctypes.c_int, [P, P, P, P, I32, P, I32, P, P, I32, P, P, P, P, P, P]),
+    "dsg_ascent_select": (ctypes.c_int, [P, P, P, P, I32, P, I32, P, P, P, P, I32, P, P, I32, P, P, P, P]),
+    "dsg_ascent_update": (ctypes.c_int, [AP, P, P, P, P, P, P, I32, I32, P, P, P, P, P, P, P, P, P]),
     "dsg_energy_workspace_bytes": (SZ, [I64]),
     "dsg_energy": (ctypes.c_int, [P, P, I64, P, P, SZ, P]),
     "dsg_range_response": (ctypes.c_int, [F64, F64, I32, I32, I32, I32, P, P]),

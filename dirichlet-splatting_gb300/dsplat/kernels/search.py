@@ -3,6 +3,7 @@ the reference's dsplat/kernels/search.py bindings of search.slang)."""
 
 from __future__ import annotations
 
+import ctypes
 import math
 
 import torch
@@ -82,6 +83,80 @@ def trial(centers, normals, direction, controls, fraction):
         width, float(fraction), ptr(out_centers), ptr(out_normals), _lib.stream(centers.device),
     )  # fmt: skip
     return out_centers, out_normals
+
+
+def trials(centers, normals, direction, controls, fractions):
+    """trial for every fraction in one launch: centers and normals [len(fractions), count, 3]."""
+    count, width = direction.shape
+    centers, normals = f32(centers), f32(normals)
+    shape = (len(fractions), count, 3)
+    out_centers, out_normals = centers.new_empty(shape), normals.new_empty(shape)
+    values = (ctypes.c_float * len(fractions))(*fractions)
+    call(
+        "dsg_trials", ptr(centers), ptr(normals), ptr(f32(direction)), ptr(f32(controls)), count, width,
+        ctypes.addressof(values), len(fractions), ptr(out_centers), ptr(out_normals), _lib.stream(centers.device),
+    )  # fmt: skip
+    return out_centers, out_normals
+
+
+def ascent_spec(specs):
+    """DsgAscentSpec of a search's ParameterConfigs (centers, and normals when present)."""
+    groups = list(specs.values())
+    spec = _lib.AscentSpec()
+    spec.width = 3 * len(groups)
+    for k, group in enumerate(groups):
+        spec.normalize[k] = int(group.normalize)
+        spec.scale[k] = float(group.scale)
+        flags = group.trainable if isinstance(group.trainable, tuple) else (group.trainable,) * 3
+        for j in range(3):
+            spec.mask[3 * k + j] = 1.0 if flags[j] else 0.0
+    return spec
+
+
+def ascent_partition(corr, norm, areas, power, real_mode, value, trial_centers, trial_normals):
+    """Full-step improvement flags, slots of the stable pending-first partition, the pending
+    count (device) and the batch rows of the smaller fractions at those slots."""
+    fractions, count = trial_centers.shape[:2]
+    device = value.device
+    improved = torch.empty(count, dtype=torch.uint8, device=device)
+    position = torch.empty(count, dtype=torch.int32, device=device)
+    pending = torch.empty(1, dtype=torch.int32, device=device)
+    rows = max(fractions - 1, 0) * count
+    batch_centers = torch.empty((rows, 3), dtype=torch.float32, device=device)
+    batch_normals = torch.empty((rows, 3), dtype=torch.float32, device=device)
+    call(
+        "dsg_ascent_partition", ptr(torch.view_as_real(corr)), ptr(norm), ptr(f32(areas)), ptr(power), int(real_mode),
+        ptr(value), count, ptr(trial_centers), ptr(trial_normals), fractions, ptr(improved), ptr(position),
+        ptr(pending), ptr(batch_centers) if rows else None, ptr(batch_normals) if rows else None,
+        _lib.stream(device),
+    )  # fmt: skip
+    return improved, position, pending, batch_centers, batch_normals
+
+
+def ascent_select(corr, norm, areas, power, real_mode, value, improved, position, trial_centers, trial_normals,
+                  centers, normals, move_normals):  # fmt: skip
+    """New centers and normals (the first improving fraction, else unchanged) and accepted."""
+    fractions, count = trial_centers.shape[:2]
+    new_centers, new_normals = torch.empty_like(centers), torch.empty_like(normals)
+    accepted = torch.empty(count, dtype=torch.uint8, device=value.device)
+    call(
+        "dsg_ascent_select", None if corr is None else ptr(torch.view_as_real(corr)), ptr(norm), ptr(f32(areas)),
+        ptr(power), int(real_mode), ptr(value), count, ptr(improved), ptr(position), ptr(trial_centers),
+        ptr(trial_normals), fractions, ptr(centers), ptr(normals), int(move_normals), ptr(new_centers),
+        ptr(new_normals), ptr(accepted), _lib.stream(value.device),
+    )  # fmt: skip
+    return new_centers, new_normals, accepted
+
+
+def ascent_update(spec, corr, norm, dcorr, dnorm, areas, power, real_mode, new_centers, new_normals, accepted,
+                  centers, normals, value, gradient, inverse):  # fmt: skip
+    """Value, ascent gradient, BFGS inverse and parameters of every candidate, in place."""
+    call(
+        "dsg_ascent_update", ctypes.byref(spec), ptr(torch.view_as_real(corr)), ptr(norm),
+        ptr(torch.view_as_real(dcorr)), ptr(dnorm), ptr(f32(areas)), ptr(power), int(real_mode), len(value),
+        ptr(new_centers), ptr(new_normals), ptr(accepted), ptr(centers), ptr(normals), ptr(value), ptr(gradient),
+        ptr(inverse), _lib.stream(value.device),
+    )  # fmt: skip
 
 
 def backward_elimination(inverse, rhs, count, limited=None, limit=0):

@@ -228,6 +228,61 @@ int dsg_trial(const float* centers, const float* normals, const float* direction
               const float* controls, int32_t count, int32_t width, float fraction,
               float* out_centers, float* out_normals, void* stream);
 
+/* dsg_trial for every backtracking fraction in one launch: fractions is a HOST array of
+ * fraction_count <= 16 values; out_centers / out_normals [fraction_count, count, 3]
+ * (reference: dsplat/certificate.py:164-167, the trials of search_certificate). */
+int dsg_trials(const float* centers, const float* normals, const float* direction,
+               const float* controls, int32_t count, int32_t width, const float* fractions,
+               int32_t fraction_count, float* out_centers, float* out_normals, void* stream);
+
+/* Constants of one certificate ascent: width 3 (centers) or 6 (centers and normals)
+ * and, per group (0 centers, 1 normals), whether it is a unit vector, the length of one
+ * solver step and the free components (mask 1) (reference: dsplat/parameters.py:15-83
+ * ParameterConfig.mask / scale / normalize). */
+typedef struct {
+  int32_t width;
+  int32_t normalize[2];
+  float scale[2];
+  float mask[6];
+} DsgAscentSpec;
+
+/* Batched backtracking, first phase. corr [count, 2] and norm [count] are the unscaled
+ * correlations of the full-step trials (dsg_surfel_correlate); with areas [count] and
+ * the residual power |r|^2 (one device double) they give each candidate's certificate
+ * (reference: dsplat/certificate.py:11-37), compared with value [count]. improved[i] is
+ * 1 where the full step raised it; the others ("pending") come first in a stable
+ * partition: position[i] is candidate i's slot, pending (device) their number, and batch
+ * row r - 1 of batch_centers / batch_normals [(fraction_count - 1) * count, 3] holds
+ * trial fraction r of trial_centers / trial_normals [fraction_count, count, 3] at the
+ * slots (reference: dsplat/certificate.py:163-177, the backtracking loop). One CTA. */
+int dsg_ascent_partition(const float* corr, const float* norm, const float* areas, const double* power,
+                         int32_t real_mode, const float* value, int32_t count, const float* trial_centers,
+                         const float* trial_normals, int32_t fraction_count, uint8_t* improved,
+                         int32_t* position, int32_t* pending, float* batch_centers, float* batch_normals,
+                         void* stream);
+/* Batched backtracking, second phase: corr / norm [(fraction_count - 1) * count] are the
+ * correlations of the batch rows (dsg_surfel_correlate_active with the pending count).
+ * Each candidate takes the first fraction whose finite certificate exceeds value:
+ * new_centers / new_normals receive the trial (normals only if move_normals) or the
+ * current parameters, accepted[i] whether one was taken. */
+int dsg_ascent_select(const float* corr, const float* norm, const float* areas, const double* power,
+                      int32_t real_mode, const float* value, int32_t count, const uint8_t* improved,
+                      const int32_t* position, const float* trial_centers, const float* trial_normals,
+                      int32_t fraction_count, const float* centers, const float* normals, int32_t move_normals,
+                      float* new_centers, float* new_normals, uint8_t* accepted, void* stream);
+/* End of a batched ascent iteration: corr, norm, dcorr [count, width, 2] and dnorm
+ * [count, width] are the unscaled correlation gradient at new_centers / new_normals
+ * (dsg_surfel_correlate_gradient). Writes the certificate value, the negated gradient in
+ * scaled tangent coordinates and the damped BFGS update of inverse [count, width, width]
+ * (only where accepted and the curvature condition holds), and moves centers / normals
+ * to the new parameters; all in place (reference: dsplat/certificate.py:136-142 ascent,
+ * :178-194 the BFGS update). */
+int dsg_ascent_update(const DsgAscentSpec* spec, const float* corr, const float* norm, const float* dcorr,
+                      const float* dnorm, const float* areas, const double* power, int32_t real_mode,
+                      int32_t count, const float* new_centers, const float* new_normals, const uint8_t* accepted,
+                      float* centers, float* normals, float* value, float* gradient, float* inverse,
+                      void* stream);
+
 /* ---- Reductions and the row-basis response ----------------------------------------- */
 
 /* Workspace of dsg_energy, in bytes. */

@@ -139,3 +139,111 @@ def test_factor_form_elimination_at_the_pooled_size():
         eager = backward_elimination(inverse, q, 12)
         device = backward_elimination(factor, q, 12, on_device=True, factored=True)
         assert torch.equal(eager, device)
+
+
+@pytest.mark.parametrize("mode,with_normals,frozen_z", [("real", True, False), ("complex", True, False),
+                                                        ("real", False, True)])  # fmt: skip
+def test_fused_ascent_iterations_match_the_pytorch_iterations(fmcw, mode, with_normals, frozen_z):
+    """Three iterations of the fused kernels (dsg_trials, dsg_ascent_partition,
+    dsg_ascent_select, dsg_ascent_update) against the PyTorch iteration on the same state:
+    the same accepted steps, centers within a thousandth of their step scale, normals within
+    1e-5, values, gradients and BFGS inverses within 1e-4."""
+    from dsplat import ParameterConfig
+    from dsplat.certificate import CertificateSearchConfig, _closures, _controls, _fused_iteration, _iteration
+
+    model, params, _ = fmcw
+    residual = model.scan.data
+    generator = torch.Generator().manual_seed(4)
+    start = {k: v.repeat(6, *([1] * (v.ndim - 1))).contiguous() for k, v in params.items()}
+    start["centers"] = (start["centers"] + (3e-4 * torch.randn(start["centers"].shape, generator=generator)).cuda())
+    base = fmcw_specs()
+    center_spec = base["centers"]
+    if frozen_z:
+        center_spec = ParameterConfig(trainable=(True, True, False), scale=0.0005, lower=(-0.02, -0.02, 0.28),
+                                      upper=(0.02, 0.02, 0.32))  # fmt: skip
+    specs = {"centers": center_spec}
+    if with_normals:
+        specs["normals"] = base["normals"]
+    masks = {key: spec.mask(start[key]) for key, spec in specs.items()}
+    controls = _controls(start["centers"], center_spec, specs.get("normals"), masks)
+    config = CertificateSearchConfig(peaks=30, separation=0, iterations=3)
+    fractions = [0.5**b for b in range(config.backtracks)]
+    ascent, score = _closures(model, residual, masks, specs, mode)
+    value, grad = score(start, True)
+    grad = ascent(start, grad)
+    count, dim = grad.shape
+    eye = torch.eye(dim, device="cuda").expand(count, dim, dim)
+    reference = (dict(start), value, grad, eye.clone())
+    state = ({k: v.clone() for k, v in start.items()}, value.clone(), grad.clone(), eye.contiguous().clone())
+    iterate = _iteration(model, residual, controls, masks, specs, config, mode, fractions, eye)
+    power = residual.abs().square().sum().double().clamp(min=1e-30).reshape(1)
+    fused = _fused_iteration(model, residual, power, controls, specs, config, mode, fractions)
+    for _ in range(config.iterations):
+        reference = iterate(*reference)
+        fused(*state)
+        moved = (state[0]["centers"] != start["centers"]).any(1)
+        expected_moved = (reference[0]["centers"] != start["centers"]).any(1)
+        assert torch.equal(moved, expected_moved)
+        close(state[0]["centers"], reference[0]["centers"], 2e-6)
+        close(state[0]["normals"], reference[0]["normals"], 1e-5)
+        close(state[1], reference[1], 1e-4)
+        close(state[2], reference[2], 1e-4)
+        close(state[3], reference[3], 1e-4)
+    if frozen_z:
+        assert torch.equal(state[0]["centers"][:, 2], start["centers"][:, 2])
+
+
+@pytest.mark.parametrize("count", [1, 1000, 3000])
+def test_ascent_partition_is_the_stable_pending_first_order(count):
+    """dsg_ascent_partition over several 1024-candidate chunks: the slots are the inverse
+    of the stable argsort of the improvement flags, the pending count and the batch rows
+    follow them, and the selection takes the first improving fraction."""
+    from dsplat.kernels import search
+
+    generator = torch.Generator().manual_seed(count)
+    fractions = 4
+    corr = torch.complex(torch.randn(count, generator=generator), torch.randn(count, generator=generator)).cuda()
+    norm = torch.rand(count, generator=generator).cuda() + 0.5
+    areas = torch.rand(count, generator=generator).cuda() + 0.5
+    value = torch.rand(count, generator=generator).cuda()
+    power = torch.tensor([1.7], dtype=torch.float64, device="cuda")
+    trial_centers = torch.randn(fractions, count, 3, generator=generator).cuda()
+    trial_normals = torch.randn(fractions, count, 3, generator=generator).cuda()
+    improved, position, pending, batch_centers, batch_normals = search.ascent_partition(
+        corr, norm, areas, power, True, value, trial_centers, trial_normals)  # fmt: skip
+    c = (corr * areas.sqrt()).to(torch.complex128)
+    certificate = (c.real.square() / (norm * areas).double() / 1.7).float()
+    expected = certificate > value
+    assert torch.equal(improved.bool(), expected)
+    order = torch.argsort(expected.to(torch.int8), stable=True)
+    assert torch.equal(position.long(), torch.argsort(order))
+    assert int(pending) == int((~expected).sum())
+    rows = batch_centers.reshape(fractions - 1, count, 3)
+    assert torch.equal(rows, trial_centers[1:, order])
+    assert torch.equal(batch_normals.reshape(fractions - 1, count, 3), trial_normals[1:, order])
+    # second phase: raw correlations of the batch rows, area applied by slot owner
+    corr2 = torch.complex(torch.randn((fractions - 1) * count, generator=generator),
+                          torch.zeros((fractions - 1) * count)).cuda()  # fmt: skip
+    norm2 = torch.ones((fractions - 1) * count, device="cuda")
+    centers, normals = torch.zeros(count, 3, device="cuda"), torch.zeros(count, 3, device="cuda")
+    new_centers, new_normals, accepted = search.ascent_select(
+        corr2, norm2, areas, power, True, value, improved, position, trial_centers, trial_normals, centers,
+        normals, True)  # fmt: skip
+    owner_root, owner_area = areas.sqrt()[order].repeat(fractions - 1), areas[order].repeat(fractions - 1)
+    scaled = (corr2.real * owner_root).double()
+    later = (scaled.square() / (norm2 * owner_area).double() / 1.7).float().reshape(fractions - 1, count)
+    better = later > value[order][None]
+    slot_pending = torch.arange(count, device="cuda") < int(pending)
+    better &= slot_pending[None]
+    for i in range(0, count, max(1, count // 97)):
+        if expected[i]:
+            assert bool(accepted[i]) and torch.equal(new_centers[i], trial_centers[0, i])
+            continue
+        p = int(position[i])
+        hits = better[:, p].nonzero().flatten()
+        if len(hits):
+            r = int(hits[0]) + 1
+            assert bool(accepted[i]) and torch.equal(new_centers[i], trial_centers[r, i])
+            assert torch.equal(new_normals[i], trial_normals[r, i])
+        else:
+            assert not bool(accepted[i]) and torch.equal(new_centers[i], centers[i])
