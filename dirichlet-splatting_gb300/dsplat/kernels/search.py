@@ -180,36 +180,18 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0):
     return removed
 
 
-TRTRI_LEAF = 512  # blocks at most this size go to trtri; larger ones split in two
-
-
 def triangular_inverse(factor):
-    """L^-1 of a lower-triangular float64 / complex128 Cholesky factor.
+    """L^-1 of a lower-triangular float64 / complex128 Cholesky factor (dsg_triangular_inverse).
 
     Recursive halving, [[A, 0], [B, C]]^-1 = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]: the
-    off-diagonal block is two float64 GEMMs (cuBLAS runs those at the float64 tensor rate),
-    the diagonal blocks of at most TRTRI_LEAF rows are inverted by dsg_triangular_inverse
-    (cuSOLVER trtri, several times slower per flop at this size).
+    off-diagonal block is two triangular products (cuBLAS trmm), diagonal blocks of at most
+    512 rows go to cuSOLVER trtri (several times slower per flop at larger sizes).
     """
     complex_mode = factor.is_complex()
-    factor = factor.to(torch.complex128 if complex_mode else torch.float64)
-    n = len(factor)
-    if n <= TRTRI_LEAF:
-        return _trtri(factor.clone().contiguous())
-    k = (n // 2 + 31) // 32 * 32
-    head = triangular_inverse(factor[:k, :k])
-    tail = triangular_inverse(factor[k:, k:])
-    out = torch.zeros_like(factor)
-    out[:k, :k] = head
-    out[k:, k:] = tail
-    out[k:, :k] = -(tail @ (factor[k:, :k] @ head))
-    return out
-
-
-def _trtri(x):
-    """In place on a contiguous lower-triangular block: its inverse (dsg_triangular_inverse)."""
-    complex_mode = x.is_complex()
+    x = factor.to(torch.complex128 if complex_mode else torch.float64).clone().contiguous()
     n = len(x)
+    if n == 0:
+        return x
     info = torch.zeros((1,), dtype=torch.int32, device=x.device)
     nbytes = _lib.query("dsg_triangular_inverse_workspace_bytes", n, int(complex_mode))
     work, nbytes = _lib.workspace(nbytes, x.device)

@@ -387,8 +387,9 @@ int dsg_backward_elimination_factor(const void* factor_inverse, const void* rhs,
 size_t dsg_triangular_inverse_workspace_bytes(int32_t n, int32_t is_complex);
 
 /* In place: a row-major lower-triangular float64 (complex128 when is_complex) factor L [n,n]
- * becomes L^-1 (cuSOLVER trtri). info (one int32 on the device) is nonzero when L is
- * singular. Replaces the potri inside dsplat/replacement.py:93-101 (cholesky_inverse) on
+ * becomes L^-1 (recursive halving: cuBLAS trmm for the off-diagonal blocks, cuSOLVER trtri
+ * for diagonal blocks of at most 512 rows). info (one int32 on the device) receives the
+ * 1-based row of the first zero diagonal element, 0 when L is nonsingular. Replaces the potri inside dsplat/replacement.py:93-101 (cholesky_inverse) on
  * the batched path. */
 int dsg_triangular_inverse(void* factor, int32_t n, int32_t is_complex, void* workspace, size_t workspace_bytes,
                            int32_t* info, void* stream);

@@ -247,3 +247,21 @@ def test_ascent_partition_is_the_stable_pending_first_order(count):
             assert torch.equal(new_normals[i], trial_normals[r, i])
         else:
             assert not bool(accepted[i]) and torch.equal(new_centers[i], centers[i])
+
+
+@pytest.mark.parametrize("n", [1, 37, 512, 513, 1000, 2256])
+@pytest.mark.parametrize("complex_mode", [False, True])
+def test_triangular_inverse_across_the_recursion(n, complex_mode):
+    """dsg_triangular_inverse at sizes on both sides of the 512-row trtri blocks and through
+    two levels of trmm halving: L^-1 to 1e-11 (well conditioned factor), zero above the
+    diagonal, status 0."""
+    from dsplat.kernels import search
+
+    dtype = torch.complex128 if complex_mode else torch.float64
+    generator = torch.Generator(device="cuda").manual_seed(n)
+    x = torch.randn(2 * n + 3, n, dtype=dtype, device="cuda", generator=generator)
+    factor = torch.linalg.cholesky(x.mH @ x / len(x) + 0.1 * torch.eye(n, dtype=dtype, device="cuda"))
+    inverse = search.triangular_inverse(factor)
+    expected = torch.linalg.inv(factor)
+    assert float((inverse - expected).norm() / expected.norm()) < 1e-11
+    assert float(inverse.triu(1).abs().max()) == 0.0 if n > 1 else True
