@@ -74,7 +74,7 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
     home = Path(nvcc).resolve().parent.parent
     temporary = LIBRARY.with_suffix(".so.tmp")
     link = [nvcc, ARCH, "-shared", "-o", str(temporary), *[str(obj) for obj, _ in results],
-            f"-L{home / 'lib64'}", "-lcublas", "-lcusolver"]
+            f"-L{home / 'lib64'}", "-lcublas"]
     done = subprocess.run(link, capture_output=True, text=True)
     if done.returncode != 0:
         raise RuntimeError(f"link failed:\n{done.stderr}")

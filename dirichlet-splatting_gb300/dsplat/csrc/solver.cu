@@ -5,98 +5,112 @@
 //
 //   [[A, 0], [B, C]]^-1 = [[A^-1, 0], [-C^-1 B A^-1, C^-1]],
 //
-// with the off-diagonal block formed by two triangular products (cuBLAS trmm, half the
-// flops of the general products) and diagonal blocks of at most kLeaf rows inverted by
-// cuSOLVER's trtri.
+// with the split points on multiples of kBlock rows: one launch first inverts every
+// kBlock-row diagonal block (a CTA per block, forward substitution in shared memory, a
+// thread per column), then the off-diagonal blocks are formed bottom-up by two cuBLAS trmm
+// each (half the flops of general products).
 #include <cublas_v2.h>
+#include <cuComplex.h>
 #include <cuda_runtime.h>
-#include <cusolverDn.h>
 #include <stdint.h>
 #include <mutex>
-#include <vector>
 #include "dsplat_gb300.h"
 
 void dsg_count_launches(int kernels);
 
 namespace {
 
-constexpr int64_t kLeaf = 512;
+constexpr int kBlock = 64;
+constexpr int kNoZero = 0x7f7f7f7f;  // every byte 0x7f: set by one memset
 
-std::mutex g_solver_mutex;
-cusolverDnHandle_t g_solvers[64] = {};
+std::mutex g_blas_mutex;
 cublasHandle_t g_blas[64] = {};
-
-cusolverDnHandle_t solver_for_current_device() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lock(g_solver_mutex);
-  if (!g_solvers[dev] && cusolverDnCreate(&g_solvers[dev]) != CUSOLVER_STATUS_SUCCESS) g_solvers[dev] = nullptr;
-  return g_solvers[dev];
-}
 
 cublasHandle_t blas_for_current_device() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lock(g_solver_mutex);
+  std::lock_guard<std::mutex> lock(g_blas_mutex);
   if (!g_blas[dev] && cublasCreate(&g_blas[dev]) != CUBLAS_STATUS_SUCCESS) g_blas[dev] = nullptr;
   return g_blas[dev];
 }
 
-// Rows of the first diagonal block: about half, rounded up to a multiple of 32.
-int64_t split(int64_t n) { return (n / 2 + 31) / 32 * 32; }
-
-// A row-major lower-triangular L is, read column-major, the upper-triangular L^T; trtri of
-// that gives (L^-1)^T column-major, which is L^-1 row-major in the same buffer.
-bool leaf_sizes(cusolverDnHandle_t h, void* a, int64_t n, int64_t ld, bool complex_mode, size_t* device,
-                size_t* host) {
-  return cusolverDnXtrtri_bufferSize(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_DIAG_NON_UNIT, n,
-                                     complex_mode ? CUDA_C_64F : CUDA_R_64F, a, ld, device, host) ==
-         CUSOLVER_STATUS_SUCCESS;
-}
+// Rows of the first diagonal block: about half, rounded up to a multiple of kBlock.
+int64_t split(int64_t n) { return (n / 2 + kBlock - 1) / kBlock * kBlock; }
 
 size_t scratch_bytes(int64_t n, bool complex_mode) {
-  if (n <= kLeaf) return 0;
+  if (n <= kBlock) return 0;
   const int64_t k = split(n);
   return (size_t)k * (size_t)(n - k) * (complex_mode ? 16 : 8);
 }
 
-// The first nonzero status of the diagonal blocks, as the row of the whole factor.
-__global__ void merge_info(int32_t* total, const int32_t* block, int64_t first_row) {
-  if (*total == 0 && *block > 0) *total = (int32_t)(*block + first_row);
+size_t align256(size_t bytes) { return (bytes + 255) / 256 * 256; }
+
+__device__ __forceinline__ double mul_add(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ cuDoubleComplex mul_add(cuDoubleComplex a, cuDoubleComplex b, cuDoubleComplex c) {
+  return make_cuDoubleComplex(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double unit_minus(bool diagonal, double s) { return (diagonal ? 1.0 : 0.0) - s; }
+__device__ __forceinline__ cuDoubleComplex unit_minus(bool diagonal, cuDoubleComplex s) {
+  return make_cuDoubleComplex((diagonal ? 1.0 : 0.0) - s.x, -s.y);
+}
+__device__ __forceinline__ double divide(double a, double b) { return a / b; }
+__device__ __forceinline__ cuDoubleComplex divide(cuDoubleComplex a, cuDoubleComplex b) { return cuCdiv(a, b); }
+__device__ __forceinline__ bool is_zero(double a) { return a == 0.0; }
+__device__ __forceinline__ bool is_zero(cuDoubleComplex a) { return a.x == 0.0 && a.y == 0.0; }
+template <typename T>
+__device__ __forceinline__ T zero_of();
+template <>
+__device__ __forceinline__ double zero_of<double>() { return 0.0; }
+template <>
+__device__ __forceinline__ cuDoubleComplex zero_of<cuDoubleComplex>() { return make_cuDoubleComplex(0.0, 0.0); }
+
+// In place on the diagonal block of rows [kBlock * blockIdx.x, +kBlock) of a row-major
+// lower-triangular matrix (leading dimension ld): the block becomes its inverse. Thread j
+// owns column j; row i of the inverse is (e_i - sum_{k<i} L_ik X_k) / L_ii, so the block
+// is overwritten row by row (rows above i already hold X, row i still holds L).
+template <typename T>
+__global__ void __launch_bounds__(kBlock) block_inverse_kernel(T* __restrict__ a, int n, int64_t ld,
+                                                               int* __restrict__ first_zero) {
+  extern __shared__ __align__(16) unsigned char raw[];
+  T* x = reinterpret_cast<T*>(raw);  // [kBlock][kBlock]
+  const int r0 = blockIdx.x * kBlock;
+  const int size = min(kBlock, n - r0);
+  const int j = threadIdx.x;
+  const T zero = zero_of<T>();
+  for (int i = 0; i < kBlock; ++i)
+    x[i * kBlock + j] = (i < size && j <= i) ? a[(size_t)(r0 + i) * ld + r0 + j] : zero;
+  __syncthreads();
+  for (int i = 0; i < size; ++i) {
+    T sum = zero;
+    for (int k = 0; k < i; ++k) sum = mul_add(x[i * kBlock + k], x[k * kBlock + j], sum);
+    const T diagonal = x[i * kBlock + i];
+    __syncthreads();  // row i is read by every thread before it is overwritten
+    if (j == 0 && is_zero(diagonal)) atomicMin(first_zero, r0 + i + 1);
+    x[i * kBlock + j] = j <= i ? divide(unit_minus(i == j, sum), diagonal) : zero;
+    __syncthreads();
+  }
+  for (int i = 0; i < size; ++i)
+    if (j <= i) a[(size_t)(r0 + i) * ld + r0 + j] = x[i * kBlock + j];
+}
+
+__global__ void finish_info(const int* __restrict__ first_zero, int32_t* __restrict__ info) {
+  *info = *first_zero == kNoZero ? 0 : *first_zero;
 }
 
 struct Inverter {
-  cusolverDnHandle_t solver;
   cublasHandle_t blas;
   bool complex_mode;
   size_t element;
-  uint8_t* leaf_workspace;
-  size_t leaf_bytes;
   void* scratch;  // k x (n - k) of the top level, the largest product
-  int32_t* info;        // of the whole factor
-  int32_t* block_info;  // of one diagonal block
-  cudaStream_t stream;
-  std::vector<uint8_t>* host_buffer;
 
-  // In place on the block at a (row-major, leading dimension ld) of n rows, whose first
-  // row is row first of the whole factor.
-  bool invert(uint8_t* a, int64_t n, int64_t ld, int64_t first) const {
-    if (n <= kLeaf) {
-      size_t device = 0, host = 0;
-      if (!leaf_sizes(solver, a, n, ld, complex_mode, &device, &host) || device > leaf_bytes) return false;
-      if (host_buffer->size() < host) host_buffer->resize(host);
-      if (cusolverDnXtrtri(solver, CUBLAS_FILL_MODE_UPPER, CUBLAS_DIAG_NON_UNIT, n,
-                           complex_mode ? CUDA_C_64F : CUDA_R_64F, a, ld, leaf_workspace, device,
-                           host ? host_buffer->data() : nullptr, host, block_info) != CUSOLVER_STATUS_SUCCESS)
-        return false;
-      merge_info<<<1, 1, 0, stream>>>(info, block_info, first);
-      dsg_count_launches(2);
-      return cudaGetLastError() == cudaSuccess;
-    }
+  // The off-diagonal blocks of the n rows at a (leading dimension ld), bottom-up; the
+  // diagonal blocks of kBlock rows are inverted already.
+  bool combine(uint8_t* a, int64_t n, int64_t ld) const {
+    if (n <= kBlock) return true;
     const int64_t k = split(n), m = n - k;
-    uint8_t* lower = a + (size_t)k * ld * element;   // B: rows k.., columns ..k
-    uint8_t* corner = lower + (size_t)k * element;   // C
-    if (!invert(a, k, ld, first) || !invert(corner, m, ld, first + k)) return false;
+    uint8_t* lower = a + (size_t)k * ld * element;  // B: rows k.., columns ..k
+    uint8_t* corner = lower + (size_t)k * element;  // C
+    if (!combine(a, k, ld) || !combine(corner, m, ld)) return false;
     // Column-major views: A^-T (k x k upper), B^T (k x m), C^-T (m x m upper).
     // T^T = A^-T B^T into the scratch (k x m, leading dimension k), then
     // (-C^-1 B A^-1)^T = -T^T C^-T over B^T.
@@ -124,7 +138,18 @@ struct Inverter {
   }
 };
 
-size_t align256(size_t bytes) { return (bytes + 255) / 256 * 256; }
+template <typename T>
+int invert_blocks(void* factor, int n, cudaStream_t stream, int* first_zero) {
+  const size_t smem = (size_t)kBlock * kBlock * sizeof(T);
+  if (smem > 48 * 1024 &&  // no static shared memory in this kernel
+      cudaFuncSetAttribute(block_inverse_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return DSG_ERR_LAUNCH;
+  block_inverse_kernel<T><<<(n + kBlock - 1) / kBlock, kBlock, smem, stream>>>(static_cast<T*>(factor), n, n,
+                                                                              first_zero);
+  dsg_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
+}
 
 }  // namespace
 
@@ -132,11 +157,7 @@ extern "C" {
 
 size_t dsg_triangular_inverse_workspace_bytes(int32_t n, int32_t is_complex) {
   if (n <= 0) return 0;
-  cusolverDnHandle_t h = solver_for_current_device();
-  size_t device = 0, host = 0;
-  const int64_t leaf = n < kLeaf ? n : kLeaf;
-  if (!h || !leaf_sizes(h, nullptr, leaf, n, is_complex != 0, &device, &host)) device = (size_t)1 << 20;
-  return align256(device) + align256(scratch_bytes(n, is_complex != 0)) + 256;
+  return align256(scratch_bytes(n, is_complex != 0)) + 256;
 }
 
 int dsg_triangular_inverse(void* factor, int32_t n, int32_t is_complex, void* workspace, size_t workspace_bytes,
@@ -144,27 +165,25 @@ int dsg_triangular_inverse(void* factor, int32_t n, int32_t is_complex, void* wo
   if (n < 0) return DSG_ERR_ARGUMENT;
   if (n == 0) return DSG_OK;
   if (!factor || !info) return DSG_ERR_ARGUMENT;
-  cusolverDnHandle_t h = solver_for_current_device();
-  cublasHandle_t b = blas_for_current_device();
-  if (!h || !b) return DSG_ERR_LIBRARY;
   const bool complex_mode = is_complex != 0;
-  size_t device = 0, host = 0;
-  const int64_t leaf = n < kLeaf ? n : kLeaf;
-  if (!leaf_sizes(h, factor, leaf, n, complex_mode, &device, &host)) return DSG_ERR_LIBRARY;
   const size_t scratch = scratch_bytes(n, complex_mode);
-  const size_t needed = align256(device) + align256(scratch) + sizeof(int32_t);
-  if (!workspace || workspace_bytes < needed) return DSG_ERR_WORKSPACE;
+  if (!workspace || workspace_bytes < align256(scratch) + sizeof(int)) return DSG_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
   uint8_t* base = static_cast<uint8_t*>(workspace);
-  thread_local std::vector<uint8_t> host_buffer;
-  if (cusolverDnSetStream(h, (cudaStream_t)stream) != CUSOLVER_STATUS_SUCCESS ||
-      cublasSetStream(b, (cudaStream_t)stream) != CUBLAS_STATUS_SUCCESS)
-    return DSG_ERR_LIBRARY;
-  int32_t* block_info = reinterpret_cast<int32_t*>(base + align256(device) + align256(scratch));
-  if (cudaMemsetAsync(info, 0, sizeof(int32_t), (cudaStream_t)stream) != cudaSuccess) return DSG_ERR_LAUNCH;
-  const Inverter inverter{h, b, complex_mode, (size_t)(complex_mode ? 16 : 8), base, align256(device),
-                          scratch ? base + align256(device) : nullptr, info, block_info, (cudaStream_t)stream,
-                          &host_buffer};
-  return inverter.invert(static_cast<uint8_t*>(factor), n, n, 0) ? DSG_OK : DSG_ERR_LIBRARY;
+  int* first_zero = reinterpret_cast<int*>(base + align256(scratch));
+  if (cudaMemsetAsync(first_zero, 0x7f, sizeof(int), st) != cudaSuccess) return DSG_ERR_LAUNCH;
+  const int launched = complex_mode ? invert_blocks<cuDoubleComplex>(factor, n, st, first_zero)
+                                    : invert_blocks<double>(factor, n, st, first_zero);
+  if (launched != DSG_OK) return launched;
+  if (n > kBlock) {
+    cublasHandle_t b = blas_for_current_device();
+    if (!b || cublasSetStream(b, st) != CUBLAS_STATUS_SUCCESS) return DSG_ERR_LIBRARY;
+    const Inverter inverter{b, complex_mode, (size_t)(complex_mode ? 16 : 8), scratch ? base : nullptr};
+    if (!inverter.combine(static_cast<uint8_t*>(factor), n, n)) return DSG_ERR_LIBRARY;
+  }
+  finish_info<<<1, 1, 0, st>>>(first_zero, info);
+  dsg_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 
 }  // extern "C"

@@ -183,9 +183,9 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0):
 def triangular_inverse(factor):
     """L^-1 of a lower-triangular float64 / complex128 Cholesky factor (dsg_triangular_inverse).
 
-    Recursive halving, [[A, 0], [B, C]]^-1 = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]: the
-    off-diagonal block is two triangular products (cuBLAS trmm), diagonal blocks of at most
-    512 rows go to cuSOLVER trtri (several times slower per flop at larger sizes).
+    Recursive halving, [[A, 0], [B, C]]^-1 = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]: every
+    64-row diagonal block is inverted by one forward-substitution launch, each off-diagonal
+    block is two triangular products (cuBLAS trmm).
     """
     complex_mode = factor.is_complex()
     x = factor.to(torch.complex128 if complex_mode else torch.float64).clone().contiguous()

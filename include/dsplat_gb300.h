@@ -387,8 +387,8 @@ int dsg_backward_elimination_factor(const void* factor_inverse, const void* rhs,
 size_t dsg_triangular_inverse_workspace_bytes(int32_t n, int32_t is_complex);
 
 /* In place: a row-major lower-triangular float64 (complex128 when is_complex) factor L [n,n]
- * becomes L^-1 (recursive halving: cuBLAS trmm for the off-diagonal blocks, cuSOLVER trtri
- * for diagonal blocks of at most 512 rows). info (one int32 on the device) receives the
+ * becomes L^-1 (every 64-row diagonal block inverted by forward substitution in one launch,
+ * then recursive halving with cuBLAS trmm for the off-diagonal blocks). info (one int32 on the device) receives the
  * 1-based row of the first zero diagonal element, 0 when L is nonsingular. Replaces the potri inside dsplat/replacement.py:93-101 (cholesky_inverse) on
  * the batched path. */
 int dsg_triangular_inverse(void* factor, int32_t n, int32_t is_complex, void* workspace, size_t workspace_bytes,

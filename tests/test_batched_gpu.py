@@ -249,12 +249,12 @@ def test_ascent_partition_is_the_stable_pending_first_order(count):
             assert not bool(accepted[i]) and torch.equal(new_centers[i], centers[i])
 
 
-@pytest.mark.parametrize("n", [1, 37, 512, 513, 1000, 2256])
+@pytest.mark.parametrize("n", [1, 37, 64, 65, 128, 513, 1000, 2256])
 @pytest.mark.parametrize("complex_mode", [False, True])
 def test_triangular_inverse_across_the_recursion(n, complex_mode):
-    """dsg_triangular_inverse at sizes on both sides of the 512-row trtri blocks and through
-    two levels of trmm halving: L^-1 to 1e-11 (well conditioned factor), zero above the
-    diagonal, status 0."""
+    """dsg_triangular_inverse at sizes on both sides of the 64-row diagonal blocks and
+    through several levels of trmm halving: L^-1 to 1e-11 (well conditioned factor), zero
+    above the diagonal."""
     from dsplat.kernels import search
 
     dtype = torch.complex128 if complex_mode else torch.float64
@@ -265,3 +265,21 @@ def test_triangular_inverse_across_the_recursion(n, complex_mode):
     expected = torch.linalg.inv(factor)
     assert float((inverse - expected).norm() / expected.norm()) < 1e-11
     assert float(inverse.triu(1).abs().max()) == 0.0 if n > 1 else True
+
+
+def test_triangular_inverse_reports_the_first_zero_pivot():
+    """A zero on the diagonal at row 70 (second 64-row block) gives status 71."""
+    from dsplat.kernels import _lib, search
+    from dsplat.kernels._lib import call, ptr
+
+    n = 200
+    factor = torch.eye(n, dtype=torch.float64, device="cuda") * 2
+    factor[70, 70] = 0.0
+    factor[150, 150] = 0.0
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nbytes = _lib.query("dsg_triangular_inverse_workspace_bytes", n, 0)
+    work, nbytes = _lib.workspace(nbytes, factor.device)
+    call("dsg_triangular_inverse", ptr(factor), n, 0, ptr(work), nbytes, ptr(info), _lib.stream(factor.device))
+    assert int(info) == 71
+    healthy = search.triangular_inverse(torch.eye(n, dtype=torch.float64, device="cuda") * 2)
+    assert torch.equal(healthy, torch.eye(n, dtype=torch.float64, device="cuda") * 0.5)
