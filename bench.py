@@ -329,7 +329,7 @@ def _roofline(totals, timers, work, args):
     flops = work.get(name)
     if flops:
         # FP32-issue-bound kernels (splat forward / JVP / VJP, certificate correlations, the
-        # normal bank): SURVEY-convention FP32 flops per pair-bin or pair-normal over the
+        # normal bank): FP32 flops per pair-bin or pair-normal (the work-unit counts) over the
         # launches' time, against the nominal FP32 rate at the measured maximum SM clock
         # (152 SMs x 128 lanes x 2 flops); the measured-peaks file has no FP32 figure.
         mhz = peaks.get("sm_max_mhz", 2070.0)

@@ -569,43 +569,35 @@ __global__ void __launch_bounds__(128) reduce_kernel(Consts c, const float* __re
   }
 }
 
-// Double-precision, fixed-order sum of chunk partials; scatters to the outputs.
+// Double-precision, fixed-order sum of chunk partials; scatters to the outputs. A thread
+// owns one value of one candidate (adjacent threads take adjacent values, so a warp reads
+// whole partial records) and adds its chunks in order.
 template <int MODE>
 __global__ void chunk_sum_kernel(const float* __restrict__ partial, int S, int chunks,
                                  float* __restrict__ o0, float* __restrict__ o1,
                                  float* __restrict__ o2, float* __restrict__ o3) {
   constexpr int NV = ModeInfo<MODE>::NV;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= S) return;
-  double t[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) t[v] = 0.0;
-  for (int g = 0; g < chunks; ++g) {
-    const float* p = partial + ((size_t)s * chunks + g) * NV;
-#pragma unroll
-    for (int v = 0; v < NV; ++v) t[v] += (double)p[v];
-  }
+  const long long index = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (index >= (long long)S * NV) return;
+  const int s = (int)(index / NV), v = (int)(index % NV);
+  const float* p = partial + (size_t)s * chunks * NV + v;
+  double t = 0.0;
+  for (int g = 0; g < chunks; ++g) t += (double)p[(size_t)g * NV];
+  const float out = (float)t;
   if (MODE == 0) {  // corr [S,2], norm [S]
-    o0[2 * s] = (float)t[0];
-    o0[2 * s + 1] = (float)t[1];
-    o1[s] = (float)t[2];
+    if (v < 2) o0[2 * s + v] = out;
+    else o1[s] = out;
   } else if (MODE == 3) {  // grad centers [S,3], normals [S,3], weights [S,2]
-    for (int j = 0; j < 3; ++j) {
-      o0[3 * s + j] = (float)t[j];
-      o1[3 * s + j] = (float)t[3 + j];
-    }
-    o2[2 * s] = (float)t[6];
-    o2[2 * s + 1] = (float)t[7];
+    if (v < 3) o0[3 * s + v] = out;
+    else if (v < 6) o1[3 * s + v - 3] = out;
+    else o2[2 * s + v - 6] = out;
   } else {  // corr, norm, dcorr [S,W,2], dnorm [S,W]
     constexpr int W = ModeInfo<MODE>::W;
-    o0[2 * s] = (float)t[0];
-    o0[2 * s + 1] = (float)t[1];
-    o1[s] = (float)t[2];
-    for (int j = 0; j < W; ++j) {
-      o2[(s * W + j) * 2] = (float)t[3 + j];
-      o2[(s * W + j) * 2 + 1] = (float)t[3 + W + j];
-      o3[s * W + j] = (float)t[3 + 2 * W + j];
-    }
+    if (v < 2) o0[2 * s + v] = out;
+    else if (v == 2) o1[s] = out;
+    else if (v < 3 + W) o2[((size_t)s * W + v - 3) * 2] = out;
+    else if (v < 3 + 2 * W) o2[((size_t)s * W + v - 3 - W) * 2 + 1] = out;
+    else o3[(size_t)s * W + v - 3 - 2 * W] = out;
   }
 }
 
@@ -811,10 +803,11 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
                                 0.5f * t + 2.0f * t2 - 1.5f * t3, -0.5f * t2 + 0.5f * t3};
           float2 v = make_float2(0.f, 0.f);
           float nn = 0.0f;
+          int first = (base - 1) % size;  // the taps base - 1 .. base + 2, wrapped
+          if (first < 0) first += size;
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            int k = (base + i - 1) % size;
-            if (k < 0) k += size;
+            const int k = first + i < size ? first + i : first + i - size;
             const float2 tv = ldg2(table + (size_t)a * size + k);
             v.x += wts[i] * tv.x;
             v.y += wts[i] * tv.y;
@@ -1014,7 +1007,8 @@ struct ReduceLaunch {
     const int nch = (A + chunk_len - 1) / chunk_len;
     dim3 grid((S + 15) / 16, nch);
     kern<<<grid, 128, smem, st>>>(c, pos, A, cen, nrm, w, S, res, chunk_len, nch, partial, active, period);
-    chunk_sum_kernel<MODE><<<(S + 127) / 128, 128, 0, st>>>(partial, S, nch, o0, o1, o2, o3);
+    const long long values = (long long)S * ModeInfo<MODE>::NV;
+    chunk_sum_kernel<MODE><<<(unsigned)((values + 255) / 256), 256, 0, st>>>(partial, S, nch, o0, o1, o2, o3);
     dsg_count_launches(2);
     return launch_status();
   }
