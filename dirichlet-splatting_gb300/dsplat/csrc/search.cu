@@ -29,7 +29,16 @@ __global__ void range_gate_kernel(const float* __restrict__ points, int count,
 
 constexpr int kPeakThreads = 1024;
 constexpr int kMaxAccepted = 4096;  // peaks held in shared memory per launch
-constexpr size_t kStaticSmem = 8 * 1024;  // bound on the static shared arrays of these kernels
+
+// Opt a kernel in to `dynamic` bytes of dynamic shared memory when that and its static
+// arrays exceed the default 48 KB.
+template <typename Kernel>
+bool allow_shared(Kernel kernel, size_t dynamic) {
+  cudaFuncAttributes attributes;
+  if (cudaFuncGetAttributes(&attributes, kernel) != cudaSuccess) return false;
+  if (dynamic + attributes.sharedSizeBytes <= 48 * 1024) return true;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dynamic) == cudaSuccess;
+}
 
 // Greedy separated peaks over candidates visited in descending-score order (ties in
 // index order): a candidate is taken unless it lies within separation of one already
@@ -46,8 +55,10 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
                                                              int* __restrict__ output) {
   extern __shared__ float taken_xyz[];  // [peaks][dimension]
   __shared__ int alive[kPeakThreads];
+  __shared__ int alive_list[kPeakThreads];  // the chunk's survivors, in order
+  __shared__ int warp_alive[kPeakThreads / 32];
   __shared__ int n_taken;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float sep2 = separation * separation;
   if (tid == 0) n_taken = 0;
   __syncthreads();
@@ -63,7 +74,9 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
       for (int j = 0; j < dimension; ++j) c[j] = centers[(size_t)index * dimension + j];
     }
     const int taken_now = n_taken;
-    for (int t = 0; ok && t < taken_now; ++t) {
+    // Latest peaks first: a suppressed candidate mostly lies near a recent, slightly
+    // better one, so its scan ends early (the outcome does not depend on the order).
+    for (int t = taken_now - 1; ok && t >= 0; --t) {
       float d2 = 0.0f;
       for (int j = 0; j < dimension; ++j) {
         const float d = c[j] - taken_xyz[t * dimension + j];
@@ -72,9 +85,19 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
       if (d2 < sep2) ok = false;
     }
     alive[tid] = ok ? 1 : 0;
+    const unsigned ballot = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) warp_alive[warp] = __popc(ballot);
+    __syncthreads();
+    int before = __popc(ballot & ((1u << lane) - 1u)), survivors = 0;
+    for (int w = 0; w < kPeakThreads / 32; ++w) {
+      before += w < warp ? warp_alive[w] : 0;
+      survivors += warp_alive[w];
+    }
+    if (ok) alive_list[before] = tid;
     __syncthreads();
     const int limit = min(kPeakThreads, count - base);
-    for (int k = 0; k < limit; ++k) {
+    for (int q = 0; q < survivors; ++q) {
+      const int k = alive_list[q];
       if (!alive[k]) continue;       // uniform
       const int slot = n_taken;      // uniform
       if (slot >= peaks) break;
@@ -94,6 +117,7 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
       if (tid == 0) n_taken = slot + 1;
       __syncthreads();
     }
+    __syncthreads();  // the chunk's flags and lists are read by every thread before reuse
   }
 }
 
@@ -168,6 +192,7 @@ __global__ void __launch_bounds__(kPeakThreads) distinct_kernel(
       if (tid == 0) n_kept = slot + 1;
       __syncthreads();
     }
+    __syncthreads();  // the chunk's flags are read by every thread before reuse
   }
   if (tid == 0) *kept_count = n_kept;
 }
@@ -273,10 +298,7 @@ int dsg_peaks(const float* scores, const int32_t* order, const float* centers, i
   cudaMemsetAsync(output, 0xff, (size_t)peaks * sizeof(int32_t), (cudaStream_t)stream);
   if (count == 0) return status();
   const size_t smem = (size_t)peaks * dimension * sizeof(float);
-  if (smem + kStaticSmem > 48 * 1024 &&  // dynamic plus the static arrays above the default
-      cudaFuncSetAttribute(peaks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess)
-    return DSG_ERR_LAUNCH;
+  if (!allow_shared(peaks_kernel, smem)) return DSG_ERR_LAUNCH;
   peaks_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(scores, order, centers, count,
                                                                dimension, peaks, separation, output);
   dsg_count_launches(1);
@@ -294,10 +316,7 @@ int dsg_distinct(const float* scores, const int32_t* order, const float* points,
     return DSG_ERR_ARGUMENT;
   const size_t smem = (size_t)(n_occupied + width) * dimension * sizeof(float);
   if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
-  if (smem + kStaticSmem > 48 * 1024 &&  // dynamic plus the static arrays above the default
-      cudaFuncSetAttribute(distinct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
-    return DSG_ERR_LAUNCH;
+  if (!allow_shared(distinct_kernel, smem)) return DSG_ERR_LAUNCH;
   distinct_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(
       scores, order, points, count, dimension, occupied, n_occupied, period, separation, width,
       output, kept_count);
