@@ -227,3 +227,40 @@ def test_shifted_refined_solve_matches_the_float64_shift():
     expected = torch.cholesky_solve(q.double(), shifted_cholesky(h, floor))
     x = shifted_refined_solve(h, q, floor)
     assert x is not None and float((x - expected).norm() / expected.norm()) < 1e-10
+
+
+def test_ascent_spec_packs_the_parameter_configs():
+    """DsgAscentSpec of the certificate ascent: width, unit-vector flags, scales and the
+    free-component masks of centers (one frozen axis) and normals."""
+    from dsplat import ParameterConfig
+    from dsplat.kernels.search import ascent_spec
+
+    specs = {"centers": ParameterConfig(trainable=(True, False, True), scale=5e-4),
+             "normals": ParameterConfig(scale=0.1, normalize=True)}  # fmt: skip
+    spec = ascent_spec(specs)
+    assert spec.width == 6
+    assert list(spec.normalize) == [0, 1]
+    assert list(spec.scale) == pytest.approx([5e-4, 0.1])
+    assert list(spec.mask) == [1.0, 0.0, 1.0, 1.0, 1.0, 1.0]
+    centers_only = ascent_spec({"centers": ParameterConfig(scale=2.0)})
+    assert centers_only.width == 3 and list(centers_only.mask)[:3] == [1.0, 1.0, 1.0]
+
+
+def test_fused_ascent_takes_only_surfel_candidates():
+    """The fused ascent needs a surfel model on CUDA whose candidates hold centers, normals
+    and areas, and at most 16 backtracking fractions; anything else keeps the PyTorch loop."""
+    from types import SimpleNamespace
+
+    from dsplat.certificate import _fusable
+
+    class Tensorish:
+        is_cuda = True
+
+    model = SimpleNamespace(scan=None, sensor=None, fresnel_n=0.0)
+    surfel = {"centers": Tensorish(), "normals": Tensorish(), "areas": Tensorish()}
+    assert _fusable(model, surfel, [1.0, 0.5])
+    assert not _fusable(model, dict(surfel, reflectivity=Tensorish()), [1.0])
+    assert not _fusable(model, surfel, [0.5**b for b in range(17)])
+    assert not _fusable(SimpleNamespace(sensor=None, fresnel_n=0.0), surfel, [1.0])
+    host = dict(surfel, centers=SimpleNamespace(is_cuda=False))
+    assert not _fusable(model, host, [1.0])
