@@ -8,7 +8,7 @@
 // One kernel per step on the caller's stream, in float64 (real or complex), after an
 // initial pick of the first unknown:
 //   step_kernel (n / 32 CTAs) the column w_i = W_ij - sum_t U[t][i] conj(U[t][j]) with the
-//   sum split over 8 warps, then b, U[step] and the diagonal, and each CTA's masked argmin
+//   sum split over 16 warps, then b, U[step] and the diagonal, and each CTA's masked argmin
 //   of the next costs; the last CTA to finish (an atomic count, no waiting) reduces those,
 //   computes the next pivot W_jj - sum_t |U[t][j]|^2 and writes the next pick.
 // The argmin takes the first minimum and counts NaN as minimal, as torch.argmin. The
@@ -90,7 +90,7 @@ __device__ __forceinline__ bool precedes(double b, int ib, double a, int ia) {
 
 constexpr int kPickThreads = 1024;
 constexpr int kRows = 32;  // rows per update CTA
-constexpr int kSplit = 8;  // warps sharing one row's sum over the earlier steps
+constexpr int kSplit = 16;  // warps sharing one row's sums (over the factor's rows and the earlier steps)
 
 // b = W q, diag = real(W_ii), alive = 1, spent = 0.
 template <typename T>
