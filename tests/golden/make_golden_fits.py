@@ -250,14 +250,16 @@ def _record(state):
             "centers": state.params["centers"].tolist()}  # fmt: skip
 
 
-def run_scenes(dsplat, device="cpu", names=None):
+def run_scenes(dsplat, device="cpu", names=None, configure=None):
     """Every scene through the given `dsplat` package; {name: {"history", "centers"}}.
 
     The same code runs the reference (on the CPU, through the oracle shims) and the GB300
-    package (on CUDA), so the two records differ only by the implementation.
+    package (on CUDA), so the two records differ only by the implementation. configure
+    maps each scene's DSFWConfig to the one used (the GB300 package's batched mode).
     """
     results = {}
     wanted = (lambda name: True) if names is None else (lambda name: name in names)
+    setup = configure or (lambda cfg: cfg)
 
     # FMCW: merged replacement from a displaced start, screened joint Gauss-Newton.
     config = dsplat.FMCWConfig()
@@ -275,6 +277,7 @@ def run_scenes(dsplat, device="cpu", names=None):
     }.items():  # fmt: skip
         if not wanted(name):
             continue
+        cfg = setup(cfg)
         state = dsplat.initialize(model, data, surfels(5, seed=9, device=device), cfg, candidates=truth,
                                   parameters=fmcw_specs(dsplat))  # fmt: skip
         for _ in range(4):
@@ -291,7 +294,7 @@ def run_scenes(dsplat, device="cpu", names=None):
                       cpu_truth["normals"] + 0.05 * torch.randn(5, 3, generator=generator), dim=1),
                   "areas": cpu_truth["areas"].clone()}  # fmt: skip
         nearby = {k: v.to(device) for k, v in nearby.items()}
-        cfg = dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0, lm_steps=2)
+        cfg = setup(dsplat.DSFWConfig(batch=5, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0, lm_steps=2))
         state = dsplat.initialize(model, data, surfels(5, seed=9, device=device), cfg, candidates=nearby,
                                   parameters=fmcw_specs(dsplat))  # fmt: skip
         for _ in range(6):
@@ -306,7 +309,7 @@ def run_scenes(dsplat, device="cpu", names=None):
         specs["centers"] = dsplat.ParameterConfig(scale=0.0005, **bounds)
         search = dsplat.SpatialSearchConfig(proposal_apertures=64, refine_apertures=64, normal_candidates=8,
                                             cache_peaks=32, full_peaks=8)  # fmt: skip
-        cfg = dsplat.DSFWConfig(batch=8, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0)
+        cfg = setup(dsplat.DSFWConfig(batch=8, lm_gain_ratio=0, joint_apertures=0, screen_apertures=0))
         state = dsplat.initialize(model, data, surfels(5, seed=9, device=device), cfg, parameters=specs)
         for _ in range(3):
             state = dsplat.step(state, cfg, search)
@@ -321,8 +324,8 @@ def run_scenes(dsplat, device="cpu", names=None):
         target = smodel.render({"centers": centers}, b)
         wrong = centers.clone()
         wrong[1] = torch.tensor([20.0, 2.0], device=device)
-        cfg = dsplat.DSFWConfig(coefficients="complex", replacement="utility", lm_solver="dense",
-                                lm_rows=grid.size, lm_gain_ratio=0, lm_steps=3)  # fmt: skip
+        cfg = setup(dsplat.DSFWConfig(coefficients="complex", replacement="utility", lm_solver="dense",
+                                      lm_rows=grid.size, lm_gain_ratio=0, lm_steps=3))  # fmt: skip
         specs = {"centers": dsplat.ParameterConfig(period=grid.shape, scale=0.5)}
         state = dsplat.initialize(smodel, target, {"centers": wrong}, cfg,
                                   candidates={"centers": grid.bins(device)}, parameters=specs)  # fmt: skip

@@ -39,11 +39,18 @@ def _scenes():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("batched", [False, True])
 @pytest.mark.parametrize("name", sorted(REFERENCE))
-def test_fit_follows_the_reference_solver(name):
+def test_fit_follows_the_reference_solver(name, batched):
+    """Plain mode, and batched mode (DSFWConfig(batched=True): device elimination from the
+    inverse factor, fused certificate ascent, refined shifted solves), against the same
+    reference records and bands."""
+    from dataclasses import replace
+
     import dsplat
 
-    ours = _scenes()(dsplat, "cuda", names={name})[name]
+    configure = (lambda cfg: replace(cfg, batched=True)) if batched else None
+    ours = _scenes()(dsplat, "cuda", names={name}, configure=configure)[name]
     theirs = REFERENCE[name]
     assert len(ours["history"]) == len(theirs["history"])
     spread = theirs["spread"]
