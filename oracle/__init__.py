@@ -16,4 +16,7 @@ fmcw      surfel columns, analytic derivatives, render / JVP / VJP / correlation
 spectral  separable atoms and derivatives (tests/reference/oracle.py:10-31)
 search    range gate, greedy peaks, quasi-Newton direction and trial step
           (dsplat/kernels/search.slang:7-109)
+scene     the 13-DOF range/Doppler/azimuth renderer (dsplat/surfel.py:132-196,
+          tests/reference/physics.py:11-25)
+solver    the float64 VarPro refit timed as the CPU baseline (dsplat/varpro.py)
 """
