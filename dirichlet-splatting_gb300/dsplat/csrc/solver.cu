@@ -37,10 +37,14 @@ cublasHandle_t blas_for_current_device() {
 // Rows of the first diagonal block: about half, rounded up to a multiple of kBlock.
 int64_t split(int64_t n) { return (n / 2 + kBlock - 1) / kBlock * kBlock; }
 
+// The largest k x (n - k) product over every level of the halving: the top level's is not
+// always the largest (n = 130 splits 128 + 2, and the 128-row half needs 64 x 64).
 size_t scratch_bytes(int64_t n, bool complex_mode) {
   if (n <= kBlock) return 0;
   const int64_t k = split(n);
-  return (size_t)k * (size_t)(n - k) * (complex_mode ? 16 : 8);
+  const size_t here = (size_t)k * (size_t)(n - k) * (complex_mode ? 16 : 8);
+  const size_t left = scratch_bytes(k, complex_mode), right = scratch_bytes(n - k, complex_mode);
+  return here > left ? (here > right ? here : right) : (left > right ? left : right);
 }
 
 size_t align256(size_t bytes) { return (bytes + 255) / 256 * 256; }
@@ -101,7 +105,7 @@ struct Inverter {
   cublasHandle_t blas;
   bool complex_mode;
   size_t element;
-  void* scratch;  // k x (n - k) of the top level, the largest product
+  void* scratch;  // the largest k x (n - k) product of the halving
 
   // The off-diagonal blocks of the n rows at a (leading dimension ld), bottom-up; the
   // diagonal blocks of kBlock rows are inverted already.

@@ -65,3 +65,53 @@ def test_cpu_tensors_are_refused():
     with pytest.raises(DsplatKernelError, match="CUDA"):
         kernel.render(FMCWConfig(), torch.zeros(4, 3), torch.zeros(2, 3), torch.zeros(2, 3),
                       torch.ones(2, dtype=torch.complex64), 0.0)  # fmt: skip
+
+
+def _inverse_scratch(n, element):
+    """Largest k (n - k) product over the triangular inverse's halving (64-row leaves)."""
+    if n <= 64:
+        return 0
+    k = (n // 2 + 63) // 64 * 64
+    return max(k * (n - k) * element, _inverse_scratch(k, element), _inverse_scratch(n - k, element))
+
+
+def test_triangular_inverse_workspace_covers_every_level():
+    """The workspace holds the top level's product (the largest at every depth) and the
+    zero-pivot word; no CUDA call is needed to size it."""
+    from dsplat.kernels import _lib
+
+    lib = _lib.library()
+    assert lib.dsg_triangular_inverse_workspace_bytes(0, 0) == 0
+    for n in list(range(1, 300)) + [511, 512, 513, 1000, 2256, 4097]:
+        for complex_mode, element in ((0, 8), (1, 16)):
+            need = (_inverse_scratch(n, element) + 255) // 256 * 256 + 4
+            assert lib.dsg_triangular_inverse_workspace_bytes(n, complex_mode) >= need, (n, complex_mode)
+
+
+def test_new_batched_entry_points_validate_on_the_host():
+    """Bad widths, fraction counts and sizes return DSG_ERR_ARGUMENT (1) and a short
+    workspace DSG_ERR_WORKSPACE (3) before anything touches the GPU."""
+    from dsplat.kernels import _lib
+
+    lib = _lib.library()
+    fractions = (ctypes.c_float * 17)(*([1.0] * 17))
+    fake = ctypes.c_void_p(16)  # never dereferenced: validation fails first
+    assert lib.dsg_trials(fake, fake, fake, fake, 4, 6, ctypes.addressof(fractions), 17, fake, fake, None) == 1
+    assert lib.dsg_trials(fake, fake, fake, fake, 4, 5, ctypes.addressof(fractions), 8, fake, fake, None) == 1
+    assert lib.dsg_ascent_partition(fake, fake, fake, fake, 1, fake, 4, fake, fake, 0, fake, fake, fake, fake,
+                                    fake, None) == 1  # fmt: skip
+    assert lib.dsg_ascent_partition(fake, fake, fake, fake, 1, fake, -1, fake, fake, 8, fake, fake, fake, fake,
+                                    fake, None) == 1  # fmt: skip
+    assert lib.dsg_ascent_select(fake, fake, fake, fake, 1, fake, 4, fake, fake, fake, fake, 17, fake, fake, 1,
+                                 fake, fake, fake, None) == 1  # fmt: skip
+    spec = _lib.AscentSpec()
+    spec.width = 4
+    assert lib.dsg_ascent_update(ctypes.byref(spec), fake, fake, fake, fake, fake, fake, 1, 4, fake, fake, fake,
+                                 fake, fake, fake, fake, fake, None) == 1  # fmt: skip
+    spec.width, spec.scale[0] = 3, 0.0
+    assert lib.dsg_ascent_update(ctypes.byref(spec), fake, fake, fake, fake, fake, fake, 1, 4, fake, fake, fake,
+                                 fake, fake, fake, fake, fake, None) == 1  # fmt: skip
+    info = ctypes.c_int32(0)
+    assert lib.dsg_triangular_inverse(fake, -1, 0, None, 0, ctypes.byref(info), None) == 1
+    assert lib.dsg_triangular_inverse(fake, 100, 0, None, 0, ctypes.byref(info), None) == 3
+    assert lib.dsg_triangular_inverse(fake, 100, 0, fake, 8, ctypes.byref(info), None) == 3

@@ -249,11 +249,12 @@ def test_ascent_partition_is_the_stable_pending_first_order(count):
             assert not bool(accepted[i]) and torch.equal(new_centers[i], centers[i])
 
 
-@pytest.mark.parametrize("n", [1, 37, 64, 65, 128, 513, 1000, 2256])
+@pytest.mark.parametrize("n", [1, 37, 64, 65, 128, 130, 150, 513, 1000, 2256])
 @pytest.mark.parametrize("complex_mode", [False, True])
 def test_triangular_inverse_across_the_recursion(n, complex_mode):
     """dsg_triangular_inverse at sizes on both sides of the 64-row diagonal blocks and
-    through several levels of trmm halving: L^-1 to 1e-11 (well conditioned factor), zero
+    through several levels of trmm halving (130 and 150 split 128 + 2 and 128 + 22, where a
+    lower level's product is the largest): L^-1 to 1e-11 (well conditioned factor), zero
     above the diagonal."""
     from dsplat.kernels import search
 
