@@ -18,6 +18,7 @@ import io
 import json
 import sys
 import tempfile
+import types
 from pathlib import Path
 from types import SimpleNamespace
 
@@ -38,7 +39,9 @@ def surface(generator, count, radius, noise):
 
 
 def main(root: Path):
+    sys.modules.setdefault("slangtorch", types.ModuleType("slangtorch"))  # the Slang loader is not needed here
     sys.path.insert(0, str(root))
+    from dsplat import FMCWConfig, Scan  # noqa: E402
     from examples import common, evaluation  # noqa: E402
 
     out = {}
@@ -88,6 +91,17 @@ def main(root: Path):
         for name in ("reconstruction.ply", "history.json", "metrics.json"):
             out["save_" + name.replace(".", "_")] = np.frombuffer((Path(folder) / name).read_bytes(), dtype=np.uint8)
         out["save_printed"] = np.frombuffer(printed.getvalue().encode(), dtype=np.uint8)
+    # progress lines: report every fifth iteration, describe a scan and its chirp
+    with contextlib.redirect_stdout(io.StringIO()) as printed:
+        for entry in ({"iteration": 10, "nmse": 0.0123456789, "replaced": 2},
+                      {"iteration": 11, "nmse": 0.5},
+                      {"iteration": 0, "nmse": 1.0, "lm_accepted": 1}):  # fmt: skip
+            common.report(entry)
+        for config in (FMCWConfig(), FMCWConfig(bandwidth_hz=4e9, adc_samples=128, pad_factor=2)):
+            scan = Scan(torch.zeros((64, config.num_range_bins), dtype=torch.complex64),
+                        torch.zeros((64, 3)), config)  # fmt: skip
+            common.describe(scan)
+    out["progress_printed"] = np.frombuffer(printed.getvalue().encode(), dtype=np.uint8)
     np.savez_compressed(HERE / "reference_io.npz", **out)
     print("wrote", HERE / "reference_io.npz", len(out), "arrays", json.dumps(sorted(out)[:4]))
 

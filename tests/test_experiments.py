@@ -2,7 +2,8 @@
 
 tests/golden/reference_io.npz holds what the reference's examples/evaluation.py and
 examples/common.py produced on seeded inputs (tests/golden/make_golden_io.py): surface
-metrics, diverse selections, PLY files and a saved result folder. Host-side only.
+metrics, diverse selections, PLY files, a saved result folder and the progress lines.
+Host-side only.
 """
 
 from __future__ import annotations
@@ -143,15 +144,17 @@ def test_output_folder_records_arguments_and_configs(tmp_path):
     assert default.preset == "demo" and default.iterations is None and default.output is None
 
 
-def test_progress_lines():
-    from dsplat import FMCWConfig
+def test_progress_lines_match_the_reference():
+    """report every fifth iteration and describe of two chirps, as the reference prints them."""
+    from dsplat import FMCWConfig, Scan
     from dsplat.experiments import describe, report
 
     with contextlib.redirect_stdout(io.StringIO()) as printed:
-        report({"iteration": 10, "nmse": 0.0123456789, "replaced": 2})
-        report({"iteration": 11, "nmse": 0.5})
-        describe(SimpleNamespace(fmcw_config=FMCWConfig(), data=torch.zeros(64, 128, dtype=torch.complex64)))
-    lines = printed.getvalue().splitlines()
-    assert lines[0] == "DSFW   10 NMSE 0.0123457 replaced=2 LM=0"
-    assert lines[1] == "scan       complex64 [64, 128]: 64 apertures x 128 positive range bins"
-    assert lines[2].startswith("chirp      ") and "ADC samples" in lines[2] and lines[2].endswith("mm per range bin")
+        for entry in ({"iteration": 10, "nmse": 0.0123456789, "replaced": 2},
+                      {"iteration": 11, "nmse": 0.5},
+                      {"iteration": 0, "nmse": 1.0, "lm_accepted": 1}):  # fmt: skip
+            report(entry)
+        for config in (FMCWConfig(), FMCWConfig(bandwidth_hz=4e9, adc_samples=128, pad_factor=2)):
+            describe(Scan(torch.zeros((64, config.num_range_bins), dtype=torch.complex64), torch.zeros((64, 3)),
+                          config))  # fmt: skip
+    assert printed.getvalue() == _text("progress_printed")
