@@ -115,3 +115,45 @@ def test_new_batched_entry_points_validate_on_the_host():
     assert lib.dsg_triangular_inverse(fake, -1, 0, None, 0, ctypes.byref(info), None) == 1
     assert lib.dsg_triangular_inverse(fake, 100, 0, None, 0, ctypes.byref(info), None) == 3
     assert lib.dsg_triangular_inverse(fake, 100, 0, fake, 8, ctypes.byref(info), None) == 3
+
+
+def _prototypes():
+    """{name: (return type, [parameter declarations])} of every entry point in the header."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    text = re.sub(r"typedef struct\s*\{.*?\}\s*\w+\s*;", "", text, flags=re.S)
+    found = {}
+    for match in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(dsg_\w+)\s*\(([^)]*)\)\s*;", text):
+        params = [p.strip() for p in match.group(3).split(",") if p.strip() and p.strip() != "void"]
+        found[match.group(2)] = (" ".join(match.group(1).split()), params)
+    return found
+
+
+def test_bindings_match_the_header_prototypes():
+    """Every ctypes signature has the header's parameter count, and pointer / integer /
+    floating kinds agree position by position; return types map to int, size_t or char*."""
+    from dsplat.kernels import _lib
+
+    prototypes = _prototypes()
+    assert set(prototypes) == set(declared())
+    for name, (ret, params) in prototypes.items():
+        restype, argtypes = _lib.SIGNATURES[name]
+        assert len(argtypes) == len(params), (name, len(argtypes), params)
+        for position, (declaration, kind) in enumerate(zip(params, argtypes, strict=True)):
+            if "*" in declaration:
+                assert kind is ctypes.c_void_p or issubclass(kind, ctypes._Pointer) or kind is ctypes.c_char_p, (
+                    name, position, declaration, kind)  # fmt: skip
+            elif declaration.startswith(("float", "const float")):
+                assert kind is ctypes.c_float, (name, position, declaration)
+            elif declaration.startswith(("double", "const double")):
+                assert kind is ctypes.c_double, (name, position, declaration)
+            elif declaration.startswith(("int64_t", "long long")):
+                assert kind is ctypes.c_int64, (name, position, declaration)
+            elif declaration.startswith("size_t"):
+                assert kind is ctypes.c_size_t, (name, position, declaration)
+            else:
+                assert kind is ctypes.c_int32, (name, position, declaration)
+        expected = {"int": ctypes.c_int, "size_t": ctypes.c_size_t, "const char*": ctypes.c_char_p,
+                    "const char *": ctypes.c_char_p, "int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64,
+                    "void": None}  # fmt: skip
+        assert ret in expected, (name, ret)
+        assert restype is expected[ret], (name, ret, restype)
