@@ -15,6 +15,13 @@ from .tracing import stage
 from .varpro import accept, fit_coefficients, pcg, screen_bar, solve
 
 
+def probe_signs(shape, seed, device):
+    """Successive Rademacher bit draws (0 / 1) of a device generator seeded with seed."""
+    generator = torch.Generator(device=device).manual_seed(seed)
+    while True:
+        yield torch.randint(0, 2, shape, device=device, generator=generator)
+
+
 def trainable(params, specs):
     return [(key, spec) for key, spec in specs.items() if spec.mask(params[key]).any()]
 
@@ -159,10 +166,10 @@ def joint_system(model, params, coefficients, target, specs, config, seed):
         return result
 
     gradient = adjoint(model.render(params, b) - target) / normalization + ridge_gradient
-    generator = torch.Generator(device=b.device).manual_seed(seed)
+    draws = probe_signs((*target.shape, 2), seed, b.device)
     diagonal = torch.zeros_like(gradient)
     for _ in range(config.cg_probes):
-        signs = torch.randint(0, 2, (*target.shape, 2), device=b.device, generator=generator)
+        signs = next(draws)
         probe = torch.view_as_complex((2 * signs - 1).to(target.real.dtype))
         diagonal += adjoint(probe).square() / normalization
     diagonal = diagonal / config.cg_probes + ridge_diagonal

@@ -2,7 +2,7 @@
 
 Run here, where the reference checkout exists (it never exists on the GPU machine):
 
-    python tests/golden/make_golden.py [/path/to/Dirichlet-Splatting]
+    python tests/golden/make_golden.py /path/to/Dirichlet-Splatting   (or set DSPLAT_REFERENCE)
 
 It imports the reference's own float64 oracles (tests/reference/kernel.py,
 tests/reference/oracle.py, tests/reference/physics.py, dsplat/groundtruth.py and the
@@ -24,7 +24,19 @@ import numpy as np
 import torch
 
 HERE = Path(__file__).resolve().parent
-DEFAULT_REFERENCE = Path("/root/reference")
+
+
+def reference_root(args):
+    """The reference checkout: the first argument, else $DSPLAT_REFERENCE; there is no default."""
+    import os
+
+    value = args[0] if args else os.environ.get("DSPLAT_REFERENCE")
+    if not value:
+        raise SystemExit("name the reference checkout: an argument or DSPLAT_REFERENCE=/path/to/Dirichlet-Splatting")
+    root = Path(value)
+    if not (root / "dsplat").is_dir():
+        raise SystemExit(f"{root} holds no dsplat package")
+    return root
 
 
 def import_reference(root: Path):
@@ -197,7 +209,7 @@ if __name__ == "__main__":
     # --scene / --migration regenerate only reference_scene.npz / reference_migration.npz
     flags = {"--scene", "--migration"}
     args = [a for a in sys.argv[1:] if a not in flags]
-    root = Path(args[0]) if args else DEFAULT_REFERENCE
+    root = reference_root(args)
     chosen = flags & set(sys.argv)
     if not chosen:
         main(root)

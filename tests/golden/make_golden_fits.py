@@ -2,7 +2,7 @@
 
 Run here, where the reference checkout exists:
 
-    python tests/golden/make_golden_fits.py [/path/to/Dirichlet-Splatting]
+    python tests/golden/make_golden_fits.py /path/to/Dirichlet-Splatting   (or set DSPLAT_REFERENCE)
 
 The reference's Python solver (dsplat/dsfw.py, varpro.py, replacement.py,
 refinement.py, certificate.py, parameters.py, fmcw.py, spectral.py) runs unmodified;
@@ -29,7 +29,19 @@ import torch
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-DEFAULT_REFERENCE = Path("/root/reference")
+
+
+def reference_root(args):
+    """The reference checkout: the first argument, else $DSPLAT_REFERENCE; there is no default."""
+    import os
+
+    value = args[0] if args else os.environ.get("DSPLAT_REFERENCE")
+    if not value:
+        raise SystemExit("name the reference checkout: an argument or DSPLAT_REFERENCE=/path/to/Dirichlet-Splatting")
+    root = Path(value)
+    if not (root / "dsplat").is_dir():
+        raise SystemExit(f"{root} holds no dsplat package")
+    return root
 
 
 # Relative perturbation of every model-kernel output (0: exact oracle values). Runs with
@@ -367,4 +379,4 @@ def main(root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REFERENCE)
+    main(reference_root(sys.argv[1:]))

@@ -2,7 +2,7 @@
 
 Run here, where the reference checkout exists (it never exists on the GPU machine):
 
-    python tests/golden/make_golden_io.py [/path/to/Dirichlet-Splatting]
+    python tests/golden/make_golden_io.py /path/to/Dirichlet-Splatting   (or set DSPLAT_REFERENCE)
 
 It imports the reference's examples/evaluation.py (geometry_metrics, write_ply) and
 examples/common.py (select_diverse, save_result), runs them on seeded inputs and writes
@@ -26,7 +26,19 @@ import numpy as np
 import torch
 
 HERE = Path(__file__).resolve().parent
-DEFAULT_REFERENCE = Path("/root/reference")
+
+
+def reference_root(args):
+    """The reference checkout: the first argument, else $DSPLAT_REFERENCE; there is no default."""
+    import os
+
+    value = args[0] if args else os.environ.get("DSPLAT_REFERENCE")
+    if not value:
+        raise SystemExit("name the reference checkout: an argument or DSPLAT_REFERENCE=/path/to/Dirichlet-Splatting")
+    root = Path(value)
+    if not (root / "dsplat").is_dir():
+        raise SystemExit(f"{root} holds no dsplat package")
+    return root
 
 
 def surface(generator, count, radius, noise):
@@ -107,4 +119,4 @@ def main(root: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REFERENCE)
+    main(reference_root(sys.argv[1:]))

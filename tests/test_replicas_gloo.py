@@ -39,7 +39,7 @@ def _rank(rank, world, port, folder):
         calls.append(threads)
         return {"value": 0.5, "unit": "steps/s", "cores": 1, "kind": "port", "sample": "stub"}
 
-    bench.cpu_baseline = fake_baseline
+    bench.full_refit_baseline = fake_baseline
     got_world, got_rank, local = bench._distributed()
     bench._barrier(got_world)
     slowest = bench._max_over_ranks(1.5 + got_rank, got_world, torch.device("cpu"))
