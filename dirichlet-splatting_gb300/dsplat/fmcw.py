@@ -1,21 +1,23 @@
-"""FMCW sensor: chirp configuration, scans and the surfel measurement model.
+"""FMCW sensor: chirp constants, scans and the surfel measurement model.
 
 A linear chirp (carrier fc, bandwidth B) sampled by adc_samples ADC samples and
 zero-padded to n_fft gives, per aperture, the positive range bins
-data[A, K] = FFT(ADC, n_fft)[:K] / adc_samples. A surfel at range r appears at bin
+data[A, K] = FFT(ADC, n_fft)[:K] / adc_samples. A surfel at range r shows up at bin
 r / spacing (spacing = c / (2 B pad)) as the Dirichlet kernel of the range FFT times
-the chirp phase. FMCWModel is the measurement model of the solver: rendering and
-derivatives on the CUDA kernels, streamed least-squares blocks projected onto the
-row basis of the range response, seeded aperture subsets, the range gate and the
-FFT range table of the spatial search. Behaviour follows the reference's
-dsplat/fmcw.py:62-388.
+its carrier phase.
+
+FMCWModel is the solver's measurement model. Rendering and derivatives run on the CUDA
+kernels (dsplat.surfel -> libdsplat_gb300.so); least-squares rows are streamed in whole
+aperture blocks and projected onto an orthonormal basis of the range responses that
+the fit's box can produce (a rank r << K subspace per block, from a float64 SVD on
+the host); aperture subsets are drawn from a seeded CPU generator so they match the
+reference's draws. Behaviour: the reference's dsplat/fmcw.py:29-454.
 """
 
 from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field, replace
-from math import ceil, floor
 from typing import NamedTuple
 
 import torch
@@ -75,77 +77,88 @@ class Scan:
     fmcw_config: FMCWConfig
 
 
-# --- Row basis of the range response ---------------------------------------------------------
+# --- Row basis of the range responses --------------------------------------------------------
 
-PEAKS_PER_BIN = 16  # peak positions per range bin sampled for the response SVD
+RESPONSE_SAMPLES_PER_BIN = 16  # peak positions per range bin in the sampled response matrix
 
 
 @dataclass(frozen=True)
 class RowBasis:
-    """Orthonormal projection of observation rows stored as consecutive aperture blocks."""
+    """An orthonormal projection U^H of the rows of consecutive aperture blocks."""
 
     adjoint: torch.Tensor  # complex [rank, bins] = U^H
-    interleaved: torch.Tensor  # real [2 rank, 2 bins] acting on (re, im) row pairs
+    interleaved: torch.Tensor  # real [2 rank, 2 bins]: U^H acting on (re, im) pairs
 
     def reduce(self, values):
-        """Complex rows [blocks * bins, ...] to [blocks * rank, ...]."""
+        """Complex rows [blocks * bins, ...] -> [blocks * rank, ...]."""
+        bins = self.adjoint.shape[1]
         tail = values.shape[1:]
-        rows = values.reshape(-1, self.adjoint.shape[1], tail.numel())
-        return (self.adjoint @ rows).reshape(-1, *tail)
+        stacked = values.reshape(-1, bins, tail.numel())
+        return torch.matmul(self.adjoint, stacked).reshape(-1, *tail)
 
     def reduce_major(self, rows):
-        """Real rows ordered bin by bin, (2 k + part) * blocks + block, in one product."""
+        """Real rows in bin-major order ((2 k + part) * blocks + block) reduced in one product."""
         tail = rows.shape[1:]
-        flat = rows.reshape(self.interleaved.shape[1], -1)
-        return project(self.interleaved, flat).reshape(-1, *tail)
+        return project(self.interleaved, rows.reshape(self.interleaved.shape[1], -1)).reshape(-1, *tail)
+
+
+def _interleave(adjoint):
+    """The real [2 r, 2 K] matrix of a complex [r, K] one acting on (re, im) pairs."""
+    r, k = adjoint.shape
+    re, im = adjoint.real, adjoint.imag
+    blocks = torch.stack((torch.stack((re, -im), -1), torch.stack((im, re), -1)), 1)  # [r, 2, K, 2]
+    return blocks.reshape(2 * r, 2 * k)
 
 
 def response_basis(config, low, high, device):
-    """Row basis of all peak positions in [low, high] bins, or None when it spans every bin.
+    """Row basis of every peak position in [low, high] bins, or None if it needs every bin.
 
-    Singular values below eps / 128 of the largest are dropped, so the normal
-    equations keep float32 precision. The SVD runs on the host in float64.
+    The range responses of peaks spread over the band span a subspace of low numerical
+    rank; singular directions below eps / 128 of the largest are dropped (the normal
+    equations then keep float32 accuracy). The SVD runs on the host in float64.
     """
-    count = max(2 * config.adc_samples, int(PEAKS_PER_BIN * (high - low)) + 1)
+    count = max(2 * config.adc_samples, int(RESPONSE_SAMPLES_PER_BIN * (high - low)) + 1)
     response = range_response(config, low, high, count, device).cpu()
-    vectors, values, _ = torch.linalg.svd(response, full_matrices=False)
-    rank = int((values > torch.finfo(torch.float32).eps / 128 * values[0]).sum())
-    if rank >= config.num_range_bins:
+    left, sigma, _ = torch.linalg.svd(response, full_matrices=False)
+    keep = int((sigma > sigma[0] * (torch.finfo(torch.float32).eps / 128)).sum())
+    if keep >= config.num_range_bins:
         return None
-    adjoint = vectors[:, :rank].mH
-    interleaved = torch.zeros((2 * rank, 2 * config.num_range_bins), dtype=torch.float64)
-    interleaved[0::2, 0::2] = adjoint.real
-    interleaved[0::2, 1::2] = -adjoint.imag
-    interleaved[1::2, 0::2] = adjoint.imag
-    interleaved[1::2, 1::2] = adjoint.real
-    return RowBasis(adjoint.to(device, torch.complex64), interleaved.to(device, torch.float32))
+    adjoint = left[:, :keep].mH
+    return RowBasis(adjoint.to(device, torch.complex64), _interleave(adjoint).to(device, torch.float32))
 
 
 class RangeTable(NamedTuple):
-    """FFT-interpolated range correlations of a residual; they only rank proposals."""
+    """FFT-interpolated range correlations of a residual; used to rank proposals only."""
 
     correlation: torch.Tensor  # [apertures, n_fft * oversample, 2]
-    norm: torch.Tensor  # [n_fft * oversample]; carries the observed-bin mask
+    norm: torch.Tensor  # [n_fft * oversample], carrying the observed-bin mask
     oversample: int
 
 
 # --- Measurement model -----------------------------------------------------------------------
 
 
+def _seeded_order(count, seed):
+    """The aperture order of a seeded CPU generator (the same draws as the reference)."""
+    return torch.randperm(count, generator=torch.Generator().manual_seed(seed))
+
+
 @dataclass(frozen=True)
 class FMCWModel:
-    """Surfels measured by an FMCW scan.
+    """Surfels {centers [S, 3], normals [S, 3], areas [S]} seen by an FMCW scan.
 
-    params = {centers [S, 3], normals [S, 3], areas [S]}; the coefficients are
-    reflectivities. prepare returns a copy carrying the row basis of the centers'
-    box; block_bases memoizes the narrower bases of aperture blocks.
+    The coefficients are reflectivities. prepare() returns a copy carrying the row basis
+    of the centers' box and per-aperture bands; block_basis memoizes the narrower bases
+    of aperture blocks by their band.
     """
 
     scan: Scan
     fresnel_n: float = 0.0  # known refractive index of the surfels; <= 1 for none
     basis: RowBasis | None = None
-    bands: tuple | None = None  # host arrays: per-aperture lowest and highest peak bin
+    bands: tuple | None = None  # host arrays: per-aperture nearest and farthest box bin
     block_bases: dict = field(default_factory=dict, repr=False)
+
+    # -- shape ---------------------------------------------------------------------------------
 
     @property
     def shape(self):
@@ -166,102 +179,107 @@ class FMCWModel:
 
     @property
     def sensor(self):
-        """The chirp configuration and the sensor positions [A, 3]."""
+        """(chirp configuration, sensor positions [A, 3])."""
         return self.scan.fmcw_config, self.scan.scan_positions_m
 
-    def sample_apertures(self, count, seed):
-        """Sorted ids of a seeded set of whole apertures and the model restricted to them.
+    # -- subsets ---------------------------------------------------------------------------------
 
-        The subset keeps sensor, material and the shared row basis, not the
-        per-aperture bands. The same seed selects the same apertures as
-        sample_rows with count * bins rows.
+    def sample_apertures(self, count, seed):
+        """Sorted ids of count seeded apertures and this model restricted to them.
+
+        The subset keeps the sensor, the material and the shared row basis, not the
+        per-aperture bands; the same seed picks the apertures sample_rows picks.
         """
-        order = torch.randperm(self.shape[0], generator=torch.Generator().manual_seed(seed))
-        ids = order[: max(1, count)].sort().values.to(self.scan.data.device)
-        scan = replace(
-            self.scan,
-            data=self.scan.data[ids].contiguous(),
-            scan_positions_m=self.scan.scan_positions_m[ids].contiguous(),
-        )
-        return ids, replace(self, scan=scan, bands=None, block_bases={})
+        picked = _seeded_order(self.apertures, seed)[: max(1, count)]
+        ids = torch.sort(picked).values.to(self.scan.data.device)
+        sub = Scan(self.scan.data[ids].contiguous(), self.scan.scan_positions_m[ids].contiguous(),
+                   self.scan.fmcw_config)  # fmt: skip
+        return ids, replace(self, scan=sub, bands=None, block_bases={})
 
     def sample_rows(self, count, seed, device):
+        """Row ids of the whole profiles of count // bins seeded apertures (in draw order)."""
         bins = self.shape[1]
-        order = torch.randperm(self.shape[0], generator=torch.Generator().manual_seed(seed))
-        chosen = order[: max(1, count // bins)].to(device)
-        return (chosen[:, None] * bins + torch.arange(bins, device=device)).flatten()
+        picked = _seeded_order(self.apertures, seed)[: max(1, count // bins)].to(device)
+        return (picked[:, None] * bins + torch.arange(bins, device=device)[None]).reshape(-1)
+
+    # -- row bases -------------------------------------------------------------------------------
 
     def prepare(self, specs):
         """This model with the row basis of every center inside the centers' box.
 
-        The band of range bins runs from the nearest to the farthest box point seen by
-        any aperture, widened by one bin. Without a finite box, or when the band would
-        wrap around the FFT, the basis covers every peak position.
+        Each aperture's band runs from its nearest to its farthest box point, widened by
+        one bin; the shared band covers all apertures. Without a finite box, or when the
+        band would wrap around the FFT, the basis covers every peak position.
         """
-        lower, upper = specs["centers"].lower, specs["centers"].upper
         config, positions = self.sensor
         low, high, bands = 0.0, float(config.n_fft), None
+        lower, upper = specs["centers"].lower, specs["centers"].upper
         if lower is not None and upper is not None:
-            lo = positions.new_tensor(lower).expand(3)
-            hi = positions.new_tensor(upper).expand(3)
-            nearest_point = torch.minimum(torch.maximum(positions, lo), hi)
-            farthest_point = torch.where((positions - lo).abs() > (positions - hi).abs(), lo, hi)
-            spacing = config.range_bin_spacing_m
-            near_bins = ((positions - nearest_point).norm(dim=1) / spacing - 1).clamp(min=0)
-            far_bins = (positions - farthest_point).norm(dim=1) / spacing + 1
-            near, far = float(near_bins.min()), float(far_bins.max())
-            if far - near < config.n_fft:
-                low, high = near, far
-                bands = (near_bins.cpu().numpy(), far_bins.cpu().numpy())
+            box_low = positions.new_tensor(lower).expand(3)
+            box_high = positions.new_tensor(upper).expand(3)
+            closest = positions.clamp(min=box_low, max=box_high)
+            farthest = torch.where((positions - box_low).abs() > (positions - box_high).abs(), box_low, box_high)
+            per_bin = 1.0 / config.range_bin_spacing_m
+            near = ((positions - closest).norm(dim=1) * per_bin - 1).clamp(min=0)
+            far = (positions - farthest).norm(dim=1) * per_bin + 1
+            span = torch.stack((near.min(), far.max())).tolist()
+            if span[1] - span[0] < config.n_fft:
+                low, high = span
+                bands = (near.cpu().numpy(), far.cpu().numpy())
         basis = response_basis(config, low, high, positions.device)
         return replace(self, basis=basis, bands=bands, block_bases={})
 
     def block_basis(self, rows):
-        """Row basis of a block of whole apertures, never larger than the shared one.
+        """Row basis of a block of whole apertures, never wider than the shared one.
 
-        The block's band is the union of its apertures' bands rounded outward to
-        whole critical range samples, so few distinct bases arise; they are built from
-        host-side bands and never wait on the device.
+        The block's band is the union of its apertures' bands rounded outward to whole
+        multiples of the pad factor (critical range samples), so few distinct bases exist;
+        they come from host-side bands and never wait on the device.
         """
         if self.bands is None or self.basis is None:
             return self.basis
         bins, step = self.shape[1], self.scan.fmcw_config.pad_factor
-        first, last = rows.start // bins, -(-rows.stop // bins)
-        key = (
-            floor(self.bands[0][first:last].min() / step) * step,
-            ceil(self.bands[1][first:last].max() / step) * step,
-        )
-        if key not in self.block_bases:
+        first, stop = rows.start // bins, -(-rows.stop // bins)
+        near, far = self.bands[0][first:stop].min(), self.bands[1][first:stop].max()
+        band = (math.floor(near / step) * step, math.ceil(far / step) * step)
+        basis = self.block_bases.get(band)
+        if basis is None:
             config, positions = self.sensor
-            basis = response_basis(config, float(key[0]), float(key[1]), positions.device)
-            narrower = basis is not None and len(basis.adjoint) < len(self.basis.adjoint)
-            self.block_bases[key] = basis if narrower else self.basis
-        return self.block_bases[key]
+            own = response_basis(config, float(band[0]), float(band[1]), positions.device)
+            basis = own if own is not None and own.adjoint.shape[0] < self.basis.adjoint.shape[0] else self.basis
+            self.block_bases[band] = basis
+        return basis
 
     def blocks(self, params, target, real, chunk):
-        """Least-squares blocks of whole apertures, projected onto the row basis.
+        """Projected least-squares blocks (rows a, data y) of whole apertures.
 
-        Real blocks are ordered bin by bin so that one product projects them.
+        Real blocks are bin-major, so one product per block projects them.
         """
         config, positions = self.sensor
         bins = self.shape[1]
-        flat = target.flatten()
+        flat = target.reshape(-1)
         for start in range(0, self.size, chunk):
             rows = slice(start, min(start + chunk, self.size))
             basis = self.block_basis(rows)
             if real:
                 block = positions[rows.start // bins : rows.stop // bins]
                 a = surfel.design(config, block, params, self.fresnel_n, real=True)
-                y = torch.view_as_real(flat[rows]).reshape(len(block), 2 * bins).T.reshape(-1)
-                yield (a, y) if basis is None else (basis.reduce_major(a), basis.reduce_major(y))
+                y = torch.view_as_real(flat[rows]).reshape(len(block), 2 * bins).t().reshape(-1)
+                if basis is not None:
+                    a, y = basis.reduce_major(a), basis.reduce_major(y)
             else:
                 a, y = self.design(params, rows), flat[rows]
-                yield (a, y) if basis is None else (basis.reduce(a), basis.reduce(y))
+                if basis is not None:
+                    a, y = basis.reduce(a), basis.reduce(y)
+            yield a, y
 
-    def _apertures(self, rows):
-        """Apertures of arbitrary row ids, each row's index among them, and its bin."""
-        apertures, inverse = torch.unique(rows // self.shape[1], return_inverse=True)
-        return self.scan.scan_positions_m[apertures], inverse, rows % self.shape[1]
+    # -- dictionary rows ---------------------------------------------------------------------------
+
+    def _rows_by_aperture(self, rows):
+        """(positions of the distinct apertures of rows, each row's aperture index, its bin)."""
+        bins = self.shape[1]
+        apertures, which = torch.unique(torch.div(rows, bins, rounding_mode="floor"), return_inverse=True)
+        return self.scan.scan_positions_m[apertures], which, torch.remainder(rows, bins)
 
     def design(self, params, rows):
         """Complex dictionary rows [rows, S]; a slice must cover whole apertures."""
@@ -270,24 +288,24 @@ class FMCWModel:
         if isinstance(rows, slice):
             block = positions[rows.start // bins : -(-rows.stop // bins)]
             return surfel.design(config, block, params, self.fresnel_n)
-        block, inverse, ids = self._apertures(rows)
-        a = surfel.design(config, block, params, self.fresnel_n)
-        return a.reshape(len(block), bins, -1)[inverse, ids]
+        block, which, bin_ids = self._rows_by_aperture(rows)
+        full = surfel.design(config, block, params, self.fresnel_n)
+        return full.reshape(len(block), bins, -1)[which, bin_ids]
 
     def jacobian(self, params, rows, atoms, keys):
         """Column derivatives [rows, atoms, D] for the given parameter keys and row ids."""
-        block, inverse, ids = self._apertures(rows)
-        selected = {key: value[atoms] for key, value in params.items()}
-        derivatives = surfel.jacobian(self.scan.fmcw_config, block, selected, self.fresnel_n)
-        return {key: derivatives[key][inverse, ids] for key in keys}
+        block, which, bin_ids = self._rows_by_aperture(rows)
+        subset = {key: value[atoms] for key, value in params.items()}
+        derivatives = surfel.jacobian(self.scan.fmcw_config, block, subset, self.fresnel_n)
+        return {key: derivatives[key][which, bin_ids] for key in keys}
+
+    # -- model products (CUDA kernels) -------------------------------------------------------------
 
     def render(self, params, coefficients):
         return surfel.render(*self.sensor, params, coefficients, self.fresnel_n)
 
     def jvp(self, params, coefficients, tangent, delta_coefficients):
-        return surfel.jvp(
-            *self.sensor, params, coefficients, tangent, delta_coefficients, self.fresnel_n
-        )
+        return surfel.jvp(*self.sensor, params, coefficients, tangent, delta_coefficients, self.fresnel_n)
 
     def vjp(self, params, coefficients, upstream):
         return surfel.vjp(*self.sensor, params, coefficients, upstream, self.fresnel_n)
@@ -296,53 +314,94 @@ class FMCWModel:
         return surfel.correlate(*self.sensor, params, residual.reshape(self.shape), self.fresnel_n, active)
 
     def correlate_gradient(self, params, residual, include_normals=False):
-        return surfel.correlate_gradient(
-            *self.sensor, params, residual.reshape(self.shape), self.fresnel_n, include_normals
-        )
+        return surfel.correlate_gradient(*self.sensor, params, residual.reshape(self.shape), self.fresnel_n,
+                                         include_normals)  # fmt: skip
 
     def correlate_orientations(self, params, residual, bank, table=None):
-        return surfel.correlate_orientations(
-            *self.sensor, params, bank, residual.reshape(self.shape), self.fresnel_n, table
-        )
+        return surfel.correlate_orientations(*self.sensor, params, bank, residual.reshape(self.shape),
+                                             self.fresnel_n, table)  # fmt: skip
+
+    # -- spatial-search helpers --------------------------------------------------------------------
 
     @torch.no_grad()
     def range_gate(self, points, measurement, relative_power, margin_cells, min_fraction):
-        """Points whose spherical range falls in a measured range interval at enough apertures.
+        """Points whose range falls inside a measured range interval at enough apertures.
 
-        32 evenly spaced apertures threshold their profile relative to its own peak,
-        dilate every interval above it by margin_cells range resolutions, and a point
-        must hit an interval at min_fraction of the apertures with signal.
+        32 evenly spaced apertures with signal threshold their profile against its own
+        peak, every interval above the threshold is dilated by margin_cells range
+        resolutions, and a point must hit an interval at min_fraction of them
+        (dsg_range_gate).
         """
         config, positions = self.sensor
-        count = min(32, len(measurement))
-        ids = torch.linspace(0, len(measurement) - 1, count, device=points.device).long()
+        ids = torch.linspace(0, len(measurement) - 1, min(32, len(measurement)), device=points.device).long()
         power = measurement[ids].abs().square()
-        peak = power.max(-1).values
-        informative = peak > peak.max() * 1e-6
-        power, peak = power[informative], peak[informative]
+        peak = power.amax(-1)
+        seen = peak > peak.max() * 1e-6
+        power, peak = power[seen], peak[seen]
         spacing = config.range_bin_spacing_m
-        radius = math.ceil(margin_cells * config.range_resolution_m / spacing)
-        above = (power >= relative_power * peak[:, None]).float()[:, None]
-        intervals = F.max_pool1d(above, 2 * radius + 1, stride=1, padding=radius)[:, 0].int()
-        return search.range_gate(points, positions[ids][informative], intervals, spacing, min_fraction)
+        reach = math.ceil(margin_cells * config.range_resolution_m / spacing)
+        hot = (power >= relative_power * peak[:, None]).float().unsqueeze(1)
+        intervals = F.max_pool1d(hot, 2 * reach + 1, stride=1, padding=reach).squeeze(1).int()
+        return search.range_gate(points, positions[ids][seen], intervals, spacing, min_fraction)
 
     @torch.no_grad()
     def range_table(self, residual, oversample=8):
-        """Oversampled FFT range correlations of the residual for proposal scores."""
+        """Oversampled FFT range correlations of the residual for proposal scores.
+
+        The profiles go back to their ADC samples (inverse FFT), then forward again into
+        n_fft * oversample points: the correlation with a unit echo at every off-grid
+        range. norm is the matching |kernel|^2 over the observed bins.
+        """
         config = self.scan.fmcw_config
         n, samples = config.n_fft, config.adc_samples
-        size = n * oversample
-        residual = residual.reshape(self.shape)
-        coefficients = torch.fft.ifft(residual, n=n, dim=-1)[..., :samples] * (n / samples)
-        correlation = torch.fft.fft(coefficients, n=size, dim=-1)
-        kernel = torch.fft.fft(residual.real.new_ones(samples), n=size) / samples
-        mask = residual.real.new_zeros(size)
-        mask[: config.num_range_bins * oversample : oversample] = 1
-        norm = torch.fft.ifft(torch.fft.fft(mask) * torch.fft.fft(kernel.abs().square())).real
+        fine = n * oversample
+        profiles = residual.reshape(self.shape)
+        adc = torch.fft.ifft(profiles, n=n, dim=-1)[..., :samples] * (n / samples)
+        correlation = torch.fft.fft(adc, n=fine, dim=-1)
+        window = torch.fft.fft(profiles.real.new_ones(samples), n=fine) / samples
+        observed = profiles.real.new_zeros(fine)
+        observed[: config.num_range_bins * oversample : oversample] = 1
+        norm = torch.fft.ifft(torch.fft.fft(observed) * torch.fft.fft(window.abs().square())).real
         return RangeTable(torch.view_as_real(correlation).contiguous(), norm.contiguous(), oversample)
 
 
-# --- Initialization ---------------------------------------------------------------------
+# --- Initializer: range migration ------------------------------------------------------------
+
+
+def _raster_frame(positions, nu, nv):
+    """Origin, pitches and the orthonormal frame (u, v, u x v) of a row-major planar raster."""
+    grid = positions.reshape(nu, nv, 3)
+    step_u = (grid[-1, 0] - grid[0, 0]) / (nu - 1)
+    step_v = (grid[0, -1] - grid[0, 0]) / (nv - 1)
+    du, dv = float(step_u.norm()), float(step_v.norm())
+    eu, ev = step_u / du, step_v / dv
+    return grid[nu // 2, nv // 2], du, dv, torch.stack([eu, ev, torch.linalg.cross(eu, ev)], -1)
+
+
+def _chirp_samples(scan, dtype):
+    """ADC samples [A, S] back from the positive range bins (residual video phase undone)."""
+    cfg = scan.fmcw_config
+    data = scan.data
+    beat = torch.arange(cfg.num_range_bins, device=data.device, dtype=dtype) * (cfg.sample_rate_hz / cfg.n_fft)
+    unphased = data * torch.exp(1j * math.pi * beat.square() / cfg.slope_hz_s)
+    return torch.fft.ifft(unphased, n=cfg.n_fft, dim=-1)[..., : cfg.adc_samples] * cfg.adc_samples
+
+
+def _depth_planes(z, wavenumber, depth_samples):
+    """Depths at which the field is focused: the points' own planes when they are few and
+    regularly spaced, else an even grid with four samples per Nyquist interval of the
+    band |kz - K / 2| <= K_max / 2."""
+    planes = torch.unique(z)
+    if len(planes) < 3:
+        regular = True
+    else:
+        gaps = planes.diff()
+        regular = torch.allclose(gaps, gaps.mean().expand(len(gaps)), atol=1e-7, rtol=1e-4)
+    if len(planes) <= depth_samples and regular:
+        return planes
+    z_low, z_high = float(z.min()), float(z.max())
+    count = max(depth_samples, 1 + math.ceil((z_high - z_low) * float(wavenumber.max()) * 2 / math.pi))
+    return torch.linspace(z_low, z_high, count, device=z.device, dtype=z.dtype)
 
 
 @torch.no_grad()
@@ -350,83 +409,62 @@ def migration(scan, points, aperture_shape, *, depth_samples=96, padding=2, freq
     """Relative complex focusing strength of a planar raster scan at world-space points.
 
     Reference: dsplat/fmcw.py:361-454. The scan must be a complete row-major planar raster
-    and the points lie on one side of it. The positive range bins are zero-filled back to
-    chirp samples with the residual-video-phase correction, every ADC sample's aperture
-    field is propagated by the angular spectrum (K = 4 pi f / c, every propagating replica
-    of an undersampled aperture kept), and the focused volume is interpolated at the
-    points. A scalar Green model without obliquity or Fresnel factors: an initializer,
-    not a calibrated reflectivity. The frequency sum of every (depth, kx, ky) runs in one
-    CUDA kernel (dsg_migration_focus); frequency_chunk is accepted for the reference's
-    signature and has no effect.
+    and the points lie on one side of it. Positive range bins go back to chirp samples, the
+    aperture field of every ADC sample is propagated by the angular spectrum (K = 4 pi f / c,
+    every propagating replica of an undersampled aperture kept) and the focused volume is
+    interpolated at the points. A scalar Green model without obliquity or Fresnel factors:
+    an initializer, not a calibrated reflectivity. The frequency sum for every (depth, kx,
+    ky) is one CUDA kernel (dsg_migration_focus); frequency_chunk is accepted for the
+    reference's signature and has no effect.
     """
     from .kernels import _lib
 
     del frequency_chunk
     nu, nv = aperture_shape
-    raster = scan.scan_positions_m.reshape(nu, nv, 3)
-    center = raster[nu // 2, nv // 2]
-    step_u = (raster[-1, 0] - raster[0, 0]) / (nu - 1)
-    step_v = (raster[0, -1] - raster[0, 0]) / (nv - 1)
-    du, dv = float(step_u.norm()), float(step_v.norm())
-    eu, ev = step_u / du, step_v / dv
-    local = (points - center) @ torch.stack([eu, ev, torch.linalg.cross(eu, ev)], -1)
-    local[:, 2] = local[:, 2].abs()
-    z_low, z_high = local[:, 2].min(), local[:, 2].max()
-    if float(z_high - z_low) < 1e-6:
-        depth_samples = 1
     cfg = scan.fmcw_config
     device, dtype = points.device, points.dtype
-    # back to chirp samples: undo the residual video phase, inverse range FFT
-    beat_hz = torch.arange(cfg.num_range_bins, device=device, dtype=dtype) * (cfg.sample_rate_hz / cfg.n_fft)
-    video = scan.data * torch.exp(1j * math.pi * beat_hz.square() / cfg.slope_hz_s)
-    adc = torch.fft.ifft(video, n=cfg.n_fft, dim=-1)[..., : cfg.adc_samples] * cfg.adc_samples
+    origin, du, dv, frame = _raster_frame(scan.scan_positions_m, nu, nv)
+    local = (points - origin) @ frame
+    local[:, 2] = local[:, 2].abs()
+    z = local[:, 2]
+    flat = float(z.max() - z.min()) < 1e-6
+    # zero-padded aperture field per ADC sample, centred, and its 2-D spectrum
     pu, pv = nu * padding, nv * padding
-    field = adc.new_zeros((cfg.adc_samples, pu, pv))
-    ou, ov = pu // 2 - nu // 2, pv // 2 - nv // 2
-    field[:, ou : ou + nu, ov : ov + nv] = adc.reshape(nu, nv, -1).permute(2, 0, 1)
-    spectrum = torch.fft.fftshift(torch.fft.fft2(torch.fft.ifftshift(field, dim=(-2, -1))), dim=(-2, -1))
+    adc = _chirp_samples(scan, dtype)
+    field_ = adc.new_zeros((cfg.adc_samples, pu, pv))
+    su, sv = pu // 2 - nu // 2, pv // 2 - nv // 2
+    field_[:, su : su + nu, sv : sv + nv] = adc.reshape(nu, nv, -1).permute(2, 0, 1)
+    spectrum = torch.fft.fftshift(torch.fft.fft2(torch.fft.ifftshift(field_, dim=(-2, -1))), dim=(-2, -1))
+    spectrum = spectrum.to(torch.complex64)
     times = cfg.adc_start_time_s + torch.arange(cfg.adc_samples, device=device, dtype=dtype) / cfg.sample_rate_hz
-    wavenumber = 4 * math.pi * (cfg.fc_hz + cfg.slope_hz_s * times) / cfg.c0_m_s
+    wavenumber = (4 * math.pi / cfg.c0_m_s) * (cfg.fc_hz + cfg.slope_hz_s * times)
+    k_max = float(wavenumber.max())
     carrier = wavenumber.max() / 2
-    planes = torch.unique(local[:, 2])
-    uniform = len(planes) < 3 or torch.allclose(
-        planes.diff(), planes.diff().mean().expand(len(planes) - 1), atol=1e-7, rtol=1e-4
-    )
-    if len(planes) <= depth_samples and uniform:
-        depths = planes  # the points already lie on these regularly spaced planes
-    else:
-        # |kz - carrier| <= Kmax / 2: four samples per Nyquist interval in depth
-        count = max(depth_samples, 1 + math.ceil(float(z_high - z_low) * float(wavenumber.max()) * 2 / math.pi))
-        depths = torch.linspace(float(z_low), float(z_high), count, device=device, dtype=dtype)
-    # every propagating replica of the sampled aperture spectrum
-    copies_u = max(1, math.ceil(float(wavenumber.max()) * du / math.pi))
-    copies_v = max(1, math.ceil(float(wavenumber.max()) * dv / math.pi))
-    qu, qv = pu * copies_u, pv * copies_v
-    dx, dy = du / copies_u, dv / copies_v
+    depths = _depth_planes(z, wavenumber, 1 if flat else depth_samples)
+    # the sampled spectrum is periodic: keep every propagating replica
+    copies = (max(1, math.ceil(k_max * du / math.pi)), max(1, math.ceil(k_max * dv / math.pi)))
+    qu, qv = pu * copies[0], pv * copies[1]
+    dx, dy = du / copies[0], dv / copies[1]
     kx = 2 * math.pi * torch.fft.fftshift(torch.fft.fftfreq(qu, d=dx, device=device, dtype=dtype))
     ky = 2 * math.pi * torch.fft.fftshift(torch.fft.fftfreq(qv, d=dy, device=device, dtype=dtype))
-    spectrum_c = torch.view_as_real(spectrum.to(torch.complex64).contiguous()).contiguous()
-    depth32 = depths.to(torch.float32).contiguous()
     focused = torch.empty((len(depths), qu, qv, 2), dtype=torch.float32, device=device)
-    _lib.call(
-        "dsg_migration_focus", _lib.ptr(spectrum_c), cfg.adc_samples, pu, pv,
-        _lib.ptr(wavenumber.to(torch.float32).contiguous()), _lib.ptr(kx.to(torch.float32).contiguous()),
-        _lib.ptr(ky.to(torch.float32).contiguous()), qu, qv, _lib.ptr(depth32), len(depths), _lib.ptr(focused),
-        _lib.stream(device),
-    )  # fmt: skip
+    _lib.call("dsg_migration_focus", _lib.ptr(torch.view_as_real(spectrum.contiguous()).contiguous()),
+              cfg.adc_samples, pu, pv, _lib.ptr(wavenumber.float().contiguous()), _lib.ptr(kx.float().contiguous()),
+              _lib.ptr(ky.float().contiguous()), qu, qv, _lib.ptr(depths.float().contiguous()), len(depths),
+              _lib.ptr(focused), _lib.stream(device))  # fmt: skip
+    # crop the points' footprint (two cells of margin) from each focused plane
     pitch = local.new_tensor([dx, dy])
-    low = torch.floor(local[:, :2].min(0).values / pitch).long() - 2
-    high = torch.ceil(local[:, :2].max(0).values / pitch).long() + 2
-    a, b = int(low[0]) + qu // 2, int(high[0]) + qu // 2 + 1
-    c, d = int(low[1]) + qv // 2, int(high[1]) + qv // 2 + 1
-    planes_xy = torch.fft.fftshift(torch.fft.ifft2(torch.fft.ifftshift(torch.view_as_complex(focused), dim=(-2, -1))),
-                                   dim=(-2, -1))  # fmt: skip
-    # remove the carrier before interpolating (the band is then centred), restore it after
-    volume = planes_xy[:, a:b, c:d] * torch.exp(1j * carrier * depths)[:, None, None]
-    volume = volume * (copies_u * copies_v / cfg.adc_samples)
-    xy = 2 * (local[:, :2] - low * pitch) / ((high - low) * pitch) - 1
-    zz = 2 * (local[:, 2] - z_low) / (z_high - z_low) - 1 if len(depths) > 1 else torch.zeros_like(local[:, 2])
+    first = torch.floor(local[:, :2].amin(0) / pitch).long() - 2
+    last = torch.ceil(local[:, :2].amax(0) / pitch).long() + 2
+    (x0, y0), (x1, y1) = first.tolist(), last.tolist()
+    planes = torch.fft.fftshift(torch.fft.ifft2(torch.fft.ifftshift(torch.view_as_complex(focused), dim=(-2, -1))),
+                                dim=(-2, -1))  # fmt: skip
+    crop = planes[:, x0 + qu // 2 : x1 + qu // 2 + 1, y0 + qv // 2 : y1 + qv // 2 + 1]
+    # interpolate with the carrier removed (a centred band), then put it back
+    volume = crop * torch.exp(1j * carrier * depths)[:, None, None] * (copies[0] * copies[1] / cfg.adc_samples)
+    xy = 2 * (local[:, :2] - first * pitch) / ((last - first) * pitch) - 1
+    zz = 2 * (z - z.min()) / (z.max() - z.min()) - 1 if len(depths) > 1 else torch.zeros_like(z)
     where = torch.stack([xy[:, 1], xy[:, 0], zz], -1).reshape(1, 1, 1, -1, 3)
-    channels = torch.view_as_real(volume).permute(3, 0, 1, 2)[None]
+    channels = torch.view_as_real(volume).permute(3, 0, 1, 2).unsqueeze(0)
     sampled = F.grid_sample(channels, where, mode="bilinear", align_corners=True).reshape(2, -1)
-    return torch.complex(sampled[0], sampled[1]) * torch.exp(-1j * carrier * local[:, 2])
+    return torch.complex(sampled[0], sampled[1]) * torch.exp(-1j * carrier * z)

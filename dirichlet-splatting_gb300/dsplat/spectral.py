@@ -1,8 +1,10 @@
 """Dirichlet atoms on a spectral grid: the signal-level measurement model.
 
-An atom has a center [D] in bin units and a complex amplitude (its coefficient); its
-spectrum is the separable windowed Dirichlet kernel of every axis observed at every
-grid bin (reference: dsplat/spectral.py:16-120).
+An atom is a center [D] in bin units (one to three axes) with a complex amplitude, its
+coefficient. Its spectrum at every grid bin is the product over axes of the windowed
+Dirichlet kernel of that axis, evaluated by the CUDA spectral kernels
+(dsplat.kernels.spectral). Behaviour of the reference's dsplat/spectral.py:16-120; the
+grid's bin coordinates are built once per device and reused by every product.
 """
 
 from __future__ import annotations
@@ -13,6 +15,8 @@ from math import prod
 import torch
 
 from .kernels import spectral as kernel
+
+_BIN_TABLES: dict = {}
 
 
 @dataclass(frozen=True)
@@ -32,8 +36,14 @@ class SpectralGrid:
         return prod(self.shape)
 
     def bins(self, device="cuda"):
-        axes = [torch.arange(n, device=device, dtype=torch.float32) for n in self.shape]
-        return torch.stack(torch.meshgrid(*axes, indexing="ij"), -1).reshape(-1, len(axes))
+        """Coordinates [size, D] (float32) of every grid bin, in row-major order."""
+        key = (tuple(self.shape), torch.device(device))
+        table = _BIN_TABLES.get(key)
+        if table is None:
+            axes = [torch.arange(n, device=device, dtype=torch.float32) for n in self.shape]
+            table = torch.cartesian_prod(*axes).reshape(-1, len(self.shape))
+            _BIN_TABLES[key] = table
+        return table.clone()
 
 
 @dataclass(frozen=True)
@@ -53,70 +63,67 @@ class SpectralModel:
         return self.grid.size
 
     def prepare(self, specs):
-        """Nothing to precompute: every grid bin is observed."""
+        """Nothing to precompute: every bin is observed."""
         return self
 
+    def _bins(self, params):
+        return self.grid.bins(params["centers"].device)
+
     def design(self, params, rows):
-        centers = params["centers"]
-        return kernel.design(self.grid, centers, self.grid.bins(centers.device)[rows])
+        return kernel.design(self.grid, params["centers"], self._bins(params)[rows])
 
     def jacobian(self, params, rows, atoms, keys):
-        centers = params["centers"]
-        bins = self.grid.bins(centers.device)[rows]
-        return {"centers": kernel.design(self.grid, centers[atoms], bins, derivatives=True)[1]}
+        derivatives = kernel.design(self.grid, params["centers"][atoms], self._bins(params)[rows], derivatives=True)
+        return {"centers": derivatives[1]}
 
     def render(self, params, coefficients):
-        centers = params["centers"]
-        values = kernel.render(self.grid, centers, coefficients, self.grid.bins(centers.device))
-        return values.reshape(self.shape)
+        return kernel.render(self.grid, params["centers"], coefficients, self._bins(params)).reshape(self.shape)
 
     def jvp(self, params, coefficients, tangent, delta_coefficients):
-        centers = params["centers"]
-        value = kernel.jvp(
-            self.grid, centers, coefficients, tangent["centers"], delta_coefficients,
-            self.grid.bins(centers.device),
-        )  # fmt: skip
-        return value.reshape(self.shape)
+        change = kernel.jvp(self.grid, params["centers"], coefficients, tangent["centers"], delta_coefficients,
+                            self._bins(params))  # fmt: skip
+        return change.reshape(self.shape)
 
     def vjp(self, params, coefficients, upstream):
-        centers = params["centers"]
-        gc, gb = kernel.vjp(
-            self.grid, centers, coefficients, upstream.flatten(), self.grid.bins(centers.device)
-        )
-        return {"centers": gc}, gb
+        centers, weights = kernel.vjp(self.grid, params["centers"], coefficients, upstream.reshape(-1),
+                                      self._bins(params))  # fmt: skip
+        return {"centers": centers}, weights
 
     def correlate(self, params, residual, active=None):
-        """a^H r and |a|^2 of every atom; an FFT when the atoms are exactly the grid bins.
+        """a^H r and |a|^2 of every atom (active is ignored: every atom is scored).
 
-        active is accepted for the FMCW model's interface and ignored: every atom is scored.
+        Atoms sitting exactly on every grid bin in order (the candidate set of a full
+        search) are correlated as one FFT convolution; any other set streams dictionary
+        blocks of at most 2^24 elements.
         """
         centers = params["centers"]
-        bins = self.grid.bins(centers.device)
+        bins = self._bins(params)
+        flat = residual.reshape(-1)
         if centers.shape == bins.shape and torch.equal(centers, bins):
             atom = kernel.design(self.grid, torch.zeros_like(centers[:1]), bins).reshape(self.shape)
-            spectrum = torch.fft.fftn(residual.reshape(self.shape)) * torch.fft.fftn(atom).conj()
-            norm = atom.abs().square().sum().expand(len(centers))
-            return torch.fft.ifftn(spectrum).flatten(), norm
-        corr = residual.new_zeros(len(centers))
-        norm = corr.real.clone()
-        chunk = max(1, 2**24 // len(centers))  # bounds the streamed dictionary block
-        flat = residual.flatten()
-        for start in range(0, self.size, chunk):
-            a = self.design(params, slice(start, start + chunk))
-            corr += a.H @ flat[start : start + chunk]
+            product = torch.fft.fftn(residual.reshape(self.shape)) * torch.fft.fftn(atom).conj()
+            energy = atom.abs().square().sum()
+            return torch.fft.ifftn(product).reshape(-1), energy.expand(len(centers))
+        block = max(1, 2**24 // len(centers))
+        corr = flat.new_zeros(len(centers))
+        norm = flat.real.new_zeros(len(centers))
+        for start in range(0, self.size, block):
+            a = self.design(params, slice(start, start + block))
+            corr += a.mH @ flat[start : start + block]
             norm += a.abs().square().sum(0)
         return corr, norm
 
     def blocks(self, params, target, real, chunk):
-        flat = target.flatten()
+        """Least-squares blocks of chunk bins; real blocks stack (re, im) rows per bin."""
+        flat = target.reshape(-1)
         for start in range(0, self.size, chunk):
             rows = slice(start, start + chunk)
             a, y = self.design(params, rows), flat[rows]
             if real:
-                a = torch.view_as_real(a).permute(0, 2, 1).reshape(-1, a.shape[1])
+                a = torch.view_as_real(a).transpose(1, 2).reshape(-1, a.shape[1])
                 y = torch.view_as_real(y).reshape(-1)
             yield a, y
 
     def sample_rows(self, count, seed, device):
-        # Deterministic broad coverage; every row once count reaches the grid size.
+        """Evenly spread rows (deterministic; every row once count reaches the grid size)."""
         return torch.linspace(0, self.size - 1, min(count, self.size), device=device).long()
