@@ -1,0 +1,150 @@
+"""Dense Hermitian solves of the solver and its preconditioned conjugate gradients.
+
+Every system here is small (K x K with K the support size, at most a few thousand) and
+lives on the GPU; cuSOLVER (through torch.linalg) factors it. The numerically delicate
+part is the rank-deficient Gram of a support with a surfel no aperture sees, or two atoms
+at one position: its Cholesky factor does not exist, and the solve instead factors
+h + shift I in float64 with shift = (size * eps) * lambda_max(h), the level at which a
+pseudoinverse would truncate. The shift only moves the solution along near-null
+directions, which the prediction does not see. Semantics of the reference's
+dsplat/varpro.py:29-79 (power iteration start, shift schedule) and varpro.py:206-228 (PCG).
+
+GB300 choices: each data-dependent decision reads one small device tensor (a factor's
+status with its diagnostics); a float64 system that must be shifted is first solved from a
+float32 factor with float64 refinement (a float32 Cholesky of 2000^2 costs a seventh of the
+float64 one here); and PCG runs a fixed number of iterations with its stopping rule kept
+as a device-side flag, looking at it only every few iterations.
+"""
+
+from __future__ import annotations
+
+import torch
+
+POWER_STEPS = 24  # power iterations for the largest eigenvalue of a Gram
+SHIFT_RETRIES = 4
+# Cumulative shift multipliers of the retries: each retry adds nine times everything
+# added so far (1, 1 + 9, 10 + 81, 91 + 729).
+SHIFT_LADDER = (1, 10, 91, 820)[:SHIFT_RETRIES]
+PCG_CHECK_EVERY = 4  # iterations between host reads of the PCG stopping flag
+
+
+def _wide(h):
+    """h in float64 (complex128 when complex), as a fresh tensor."""
+    return h.to(torch.complex128 if h.is_complex() else torch.float64, copy=True)
+
+
+def largest_eigenvalue(h):
+    """Power-iteration estimate of the largest eigenvalue of a positive semidefinite h.
+
+    The start vector is the fixed golden-ratio sequence frac(0.618 i) + 0.5, so the
+    estimate is reproducible without a generator.
+    """
+    ramp = torch.arange(len(h), device=h.device, dtype=torch.float64)
+    v = (torch.remainder(ramp * 0.6180339887, 1) + 0.5).to(h.dtype)
+    length = v.norm()
+    for _ in range(POWER_STEPS):
+        v = h @ v
+        length = v.norm()
+        v = v / length.clamp(min=torch.finfo(length.dtype).tiny)
+    return length
+
+
+def shifted_cholesky(h, floor):
+    """Float64 Cholesky factor of h + shift I, or None when every retry fails.
+
+    shift = floor * lambda_max(h) at first; after a failure the diagonal gets nine times
+    the total shift so far, at most SHIFT_RETRIES attempts.
+    """
+    base = _wide(h)
+    unit = floor * largest_eigenvalue(base)
+    diagonal = base.diagonal().clone()
+    for multiple in SHIFT_LADDER:
+        base.diagonal().copy_(diagonal + multiple * unit)
+        factor, status = torch.linalg.cholesky_ex(base)
+        if int(status) == 0:
+            return factor
+    return None
+
+
+def refined_solve(h, rhs, iterations=3, tolerance=1e-13):
+    """x = h^-1 rhs for a float64 h from a float32 factor with float64 iterative refinement.
+
+    Returns None, and the caller factors in float64, when the float32 factor does not
+    exist or the normwise backward error |q - h x| / (|h|_F |x| + |q|) stays above
+    tolerance (systems whose condition number nears 1 / float32 epsilon). One device read
+    decides both.
+    """
+    low = torch.complex64 if h.is_complex() else torch.float32
+    factor, status = torch.linalg.cholesky_ex(h.to(low))
+    q = (rhs if rhs.ndim == 2 else rhs[:, None]).to(h.dtype)
+    x = torch.cholesky_solve(q.to(low), factor).to(h.dtype)
+    for _ in range(iterations):
+        x = x + torch.cholesky_solve((q - h @ x).to(low), factor).to(h.dtype)
+    scale = torch.linalg.matrix_norm(h) * x.norm() + q.norm()
+    error = (q - h @ x).norm() / scale.clamp(min=1e-300)
+    verdict = (status == 0) & (error <= tolerance)  # a failed factor leaves NaN in error
+    if not bool(verdict):
+        return None
+    return x if rhs.ndim == 2 else x[:, 0]
+
+
+def shifted_refined_solve(h, q, floor):
+    """(h + floor lambda_max(h) I)^-1 q at the first shift of shifted_cholesky, or None."""
+    base = _wide(h)
+    base.diagonal().add_(floor * largest_eigenvalue(base))
+    return refined_solve(base, q)
+
+
+def solve(h, rhs, refined=False):
+    """Hermitian solve; a singular h is shifted to where a pseudoinverse would truncate.
+
+    refined first tries the shifted system through refined_solve (float32 factor, float64
+    refinement), which gives its solution to float64 accuracy like the float64 factor.
+    A Gram whose columns are all zero has nothing to fit: the answer is zero.
+    """
+    q = rhs if rhs.ndim == 2 else rhs[:, None]
+    factor, status = torch.linalg.cholesky_ex(h)
+    if int(status) != 0:
+        floor = len(h) * torch.finfo(h.real.dtype).eps
+        if refined and h.is_cuda:
+            x = shifted_refined_solve(h, q, floor)
+            if x is not None:
+                return (x if rhs.ndim == 2 else x[:, 0]).to(rhs.dtype)
+        factor = shifted_cholesky(h, floor)
+        if factor is None:
+            return torch.zeros_like(rhs)
+    x = torch.cholesky_solve(q.to(factor.dtype), factor).to(q.dtype)
+    return x if rhs.ndim == 2 else x[:, 0]
+
+
+def pcg(operator, rhs, diagonal, *, iterations=32, tolerance=1e-3):
+    """Jacobi-preconditioned conjugate gradients from zero.
+
+    Stops (keeps x) at the first direction of nonpositive curvature, or after the update
+    that brings |r| to tolerance * |rhs| or below. The stop is a device flag: iterations
+    after it change nothing, and the host looks at the flag every PCG_CHECK_EVERY
+    iterations to skip the rest, so the loop issues no per-iteration device read.
+    """
+    x = torch.zeros_like(rhs)
+    goal = tolerance * rhs.norm()
+    r = rhs.clone()
+    z = r / diagonal
+    p = z.clone()
+    rz = r @ z
+    live = torch.ones((), dtype=torch.bool, device=rhs.device)
+    for done in range(iterations):
+        if done and done % PCG_CHECK_EVERY == 0 and not bool(live):
+            break
+        hp = operator(p)
+        curvature = p @ hp
+        live = live & (curvature > 0)
+        alpha = rz / curvature
+        x = torch.where(live, x + alpha * p, x)
+        r = torch.where(live, r - alpha * hp, r)
+        going = live & (r.norm() > goal)
+        z = r / diagonal
+        rz_next = r @ z
+        p = torch.where(going, z + (rz_next / rz) * p, p)
+        rz = torch.where(going, rz_next, rz)
+        live = going
+    return x

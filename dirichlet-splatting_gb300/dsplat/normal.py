@@ -1,0 +1,166 @@
+"""Streamed normal equations G = A^H A / M, q = A^H y / M of one support.
+
+The dictionary A (M observations x S atoms; 33.5 GB at 16 384 apertures x 2000 surfels)
+is never stored: rows are generated in blocks of whole apertures, projected onto the
+row basis of their range band, reduced into the Gram, and dropped. Two accumulators:
+
+  Fp32Syrk       the reference's arithmetic (dsplat/varpro.py:91-120): each real block
+                 adds its upper triangle in float32 (SSYRK), folded into a float64 total
+                 every FOLD blocks; complex blocks use complex GEMMs.
+  TensorCoreGram split-BF16x3 on tcgen05 (DSFWConfig.gram == "bf16x3", real
+                 coefficients): every projected row block is stored transposed as bf16
+                 hi + lo, in the fused design-projection kernel when the basis allows
+                 (no dictionary block ever reaches HBM), and one tcgen05 launch adds the
+                 whole Gram to the float64 total.
+
+The right-hand side of the fused path is the correlation of every atom with the data
+(dsg_surfel_correlate), which needs no dictionary rows either.
+"""
+
+from __future__ import annotations
+
+import torch
+
+from .kernels.cublas import syrk
+
+FOLD = 8  # float32 blocks summed before each float64 fold of the Gram
+
+
+def row_chunk(model, columns, config):
+    """Observation rows per streamed block: at most dictionary_elements / columns, whole apertures."""
+    limit = min(config.row_chunk, max(1, config.dictionary_elements // columns))
+    align = model.row_alignment
+    return max(align, limit - limit % align)
+
+
+def _block_ranges(model, chunk):
+    for start in range(0, model.size, chunk):
+        yield slice(start, min(start + chunk, model.size))
+
+
+def projected_rows(model, chunk):
+    """Real rows that model.blocks(..., real=True, chunk) yields, known before streaming."""
+    if not hasattr(model, "block_basis"):
+        return 2 * model.size
+    bins = model.shape[1]
+    total = 0
+    for rows in _block_ranges(model, chunk):
+        basis = model.block_basis(rows)
+        width = 2 * bins if basis is None else basis.interleaved.shape[0]
+        total += width * (-(-rows.stop // bins) - rows.start // bins)
+    return total
+
+
+def fused_rows(model, params, store, chunk):
+    """Store every projected real row block with the fused design-projection kernel.
+
+    Consecutive blocks sharing one basis go to the kernel as one aperture range. Returns
+    the kernel status tensor, or None (nothing stored) when the model or a block's basis
+    is outside what the kernel covers; the caller then streams explicit blocks.
+    """
+    from .kernels.gram import append_projected, fused_supported
+
+    if not hasattr(model, "block_basis"):
+        return None
+    config, positions = model.sensor
+    bins = model.shape[1]
+    runs = []  # [first aperture, stop aperture, basis]
+    for rows in _block_ranges(model, chunk):
+        basis = model.block_basis(rows)
+        if not fused_supported(config, basis):
+            return None
+        first, stop = rows.start // bins, rows.stop // bins
+        if runs and runs[-1][2] is basis and runs[-1][1] == first:
+            runs[-1][1] = stop
+        else:
+            runs.append([first, stop, basis])
+    status = torch.zeros(1, dtype=torch.int32, device=positions.device)
+    for first, stop, basis in runs:
+        append_projected(store, config, positions[first:stop], params, basis, model.fresnel_n, status)
+    return status
+
+
+def _symmetrize_upper(total, size):
+    """Full symmetric matrix from the upper triangle of total, divided by size."""
+    upper = torch.triu(total)
+    return (upper + torch.triu(total, 1).mT) / size
+
+
+class Fp32Syrk:
+    """Float32 SSYRK per block, folded into float64 every FOLD blocks."""
+
+    def __init__(self, count, device):
+        self.total = torch.zeros((count, count), dtype=torch.float64, device=device)
+        self.part = torch.zeros((count, count), dtype=torch.float32, device=device)
+        self.rhs = torch.zeros(count, dtype=torch.float64, device=device)
+        self.blocks = 0
+
+    def add(self, a, y):
+        a = a.contiguous()
+        syrk(a, self.part)
+        self.rhs += a.T @ y
+        self.blocks += 1
+        if self.blocks % FOLD == 0:
+            self.total += self.part
+            self.part.zero_()
+
+    def finish(self):
+        self.total += self.part
+        return self.total, self.rhs
+
+
+class TensorCoreGram:
+    """Split-BF16x3 rows stored for one tcgen05 Gram launch (real coefficients)."""
+
+    def __init__(self, model, count, chunk, device):
+        from .kernels.gram import GramRows
+
+        self.store = GramRows(count, projected_rows(model, chunk), device)
+        self.total = torch.zeros((count, count), dtype=torch.float64, device=device)
+        self.rhs = torch.zeros(count, dtype=torch.float64, device=device)
+
+    def add(self, a, y):
+        self.store.append(a)
+        self.rhs += a.T @ y
+
+    def finish(self, column_from=0):
+        from .kernels.gram import check
+
+        check(self.store.accumulate(self.total, column_from=column_from))
+        return self.total, self.rhs
+
+
+def normal_equations(model, params, target, config):
+    """(G, q) = (A^H A / M, A^H y / M) of params, streamed over projected row blocks.
+
+    Real coefficients return float32 real G and q (float64 accumulation inside);
+    complex coefficients return complex G and q accumulated in complex64.
+    """
+    count = len(params["centers"])
+    chunk = row_chunk(model, count, config)
+    if not config.real:
+        gram = target.new_zeros((count, count))
+        rhs = target.new_zeros(count)
+        for a, y in model.blocks(params, target, False, chunk):
+            gram.addmm_(a.mH, a)
+            rhs.addmv_(a.mH, y)
+        return (gram + gram.mH) / (2 * model.size), rhs / model.size
+    device = target.device
+    if getattr(config, "gram", "fp32") == "bf16x3":
+        acc = TensorCoreGram(model, count, chunk, device)
+        status = fused_rows(model, params, acc.store, chunk)
+        if status is None:
+            for a, y in model.blocks(params, target, True, chunk):
+                acc.add(a, y)
+        else:
+            from .kernels.gram import check
+
+            acc.rhs += model.correlate(params, target)[0].real.double()
+            check(status)
+        total, rhs = acc.finish()
+    else:
+        acc = Fp32Syrk(count, device)
+        for a, y in model.blocks(params, target, True, chunk):
+            acc.add(a, y)
+        total, rhs = acc.finish()
+    return _symmetrize_upper(total, model.size).float(), (rhs / model.size).float()

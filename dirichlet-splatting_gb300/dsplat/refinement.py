@@ -1,18 +1,33 @@
 """Local geometry refinement: dense reduced-VarPro LM and matrix-free joint Gauss-Newton.
 
-Both propose moves of every trainable atom and keep one only if its refitted
-objective is lower (varpro.accept). Steps are dimensionless; each
-ParameterConfig.scale sets its unit. Behaviour follows the reference's
-dsplat/refinement.py:20-227; the joint system's products are the CUDA JVP and
-adjoint (VJP) kernels.
+Both propose a move of every trainable atom and keep it only when its refitted
+objective is lower (varpro.accept), trying the full step, then shorter ones. Steps are
+dimensionless; ParameterConfig.scale gives each field its unit. Semantics of the
+reference's dsplat/refinement.py:20-227.
+
+joint: the unknowns are every trainable geometry component and every coefficient,
+scaled to unit steps; the Gauss-Newton matrix is never formed. A product with it is one
+forward-mode JVP and one adjoint VJP on the CUDA kernels, its Jacobi diagonal is
+estimated from Rademacher probes through the adjoint, and PCG (dsplat.linalg.pcg) runs
+with a device-side stopping flag. dense: the coefficients are eliminated exactly on
+sampled rows and the reduced Gauss-Newton system is formed and solved.
 """
 
 from __future__ import annotations
 
 import torch
 
+from .linalg import pcg, solve
 from .tracing import stage
-from .varpro import accept, fit_coefficients, pcg, screen_bar, solve
+from .varpro import accept, fit_coefficients, screen_bar
+
+BACKTRACK_JOINT = (1.0, 0.5, 0.25, 0.125)  # step fractions tried by the joint slide
+BACKTRACK_DENSE = (1.0, 0.5, 0.25)  # step fractions tried by the dense slide
+
+
+def trainable(params, specs):
+    """[(key, spec)] of the fields with at least one free component, in specs order."""
+    return [(key, spec) for key, spec in specs.items() if spec.any_free and key in params]
 
 
 def probe_signs(shape, seed, device):
@@ -22,8 +37,16 @@ def probe_signs(shape, seed, device):
         yield torch.randint(0, 2, shape, device=device, generator=generator)
 
 
-def trainable(params, specs):
-    return [(key, spec) for key, spec in specs.items() if spec.mask(params[key]).any()]
+def _as_matrix(value):
+    return value[:, None] if value.ndim == 1 else value
+
+
+def _free_width(spec, value):
+    """Number of free components per atom, from the configuration (no device read)."""
+    flags = spec.trainable
+    if isinstance(flags, (tuple, list)):
+        return sum(bool(flag) for flag in flags)
+    return _as_matrix(value).shape[1] if flags else 0
 
 
 # --- dense: reduced VarPro on sampled rows ---------------------------------------------------
@@ -31,49 +54,53 @@ def trainable(params, specs):
 
 @torch.no_grad()
 def reduced_system(model, params, target, specs, config, rows):
-    """Gauss-Newton normal matrix and gradient of the ridge-VarPro objective on some rows.
+    """Gauss-Newton matrix and gradient of the ridge-VarPro objective on the given rows.
 
-    Every coefficient is eliminated: J = dA b + A db with the exact coefficient
-    differential db, including the dA^H r term; unit-vector retractions and parameter
-    scales are chained before elimination.
+    With every coefficient eliminated, the Jacobian of the residual is
+    J = dA b + A db, db the exact differential of the least-squares coefficients
+    (its right-hand side carries the dA^H r term); the unit-vector retraction and the
+    parameter scales are chained in before the elimination.
     """
     a = model.design(params, rows)
-    y = target.flatten()[rows]
+    y = target.reshape(-1)[rows]
     m = len(a)
-    gram, rhs = a.H @ a / m, a.H @ y / m
+    gram, rhs = a.mH @ a / m, a.mH @ y / m
     b = fit_coefficients(gram, rhs, config)
     residual = a @ b.to(a.dtype) - y
     layout = trainable(params, specs)
-    atoms = torch.arange(len(b), device=a.device)
-    raw = model.jacobian(params, rows, atoms, [key for key, _ in layout])
-    da = torch.cat([spec.differential(raw[key], params[key]) for key, spec in layout], -1)
-    eye = torch.eye(len(b), dtype=b.dtype, device=a.device)
-    h = (gram.real if config.real else gram) + config.ridge * eye
-    j = (da * b[None, :, None]).reshape(m, -1)
-    cross = a.H @ j / m
-    columns = torch.arange(j.shape[1], device=a.device)
-    cross[atoms.repeat_interleave(da.shape[-1]), columns] += (
-        (da.conj() * residual[:, None, None]).sum(0).flatten() / m
-    )
+    count = len(b)
+    raw = model.jacobian(params, rows, torch.arange(count, device=a.device), [key for key, _ in layout])
+    da = torch.cat([spec.differential(raw[key], params[key]) for key, spec in layout], -1)  # [m, S, D]
+    width = da.shape[-1]
+    j = (da * b[None, :, None]).reshape(m, count * width)
+    cross = a.mH @ j / m
+    # atom s's own columns also get sum_rows conj(dA[:, s, d]) r / m (the dA^H r term)
+    own = torch.einsum("rsd,r->sd", da.conj(), residual) / m
+    torch.diagonal(cross.view(count, count, width), dim1=0, dim2=1).add_(own.mT)
+    h = gram.real if config.real else gram
+    if config.ridge:
+        h = h.clone()
+        h.diagonal().add_(config.ridge)
     db = -solve(h, cross.real if config.real else cross, refined=getattr(config, "batched", False))
     reduced = j + a @ db.to(a.dtype)
-    normal = (reduced.H @ reduced / m + config.ridge * db.H @ db).real
-    gradient = (reduced.H @ residual / m + config.ridge * db.H @ b).real
+    normal = (reduced.mH @ reduced / m + config.ridge * db.mH @ db).real
+    gradient = (reduced.mH @ residual / m + config.ridge * db.mH @ b).real
     return normal, gradient
 
 
-def _step_along(state, layout, delta, fraction):
-    """Parameters moved by fraction * scale * delta on their free components, projected."""
-    proposal = {key: value.clone() for key, value in state.params.items()}
-    offset = 0
+def _moved(state, layout, delta, fraction):
+    """Parameters shifted by fraction * scale * delta on their free components, projected."""
+    proposal = dict(state.params)
+    column = 0
     for key, spec in layout:
-        value = proposal[key]
-        matrix = value[:, None] if value.ndim == 1 else value.clone()
-        mask = spec.mask(value)
-        width = int(mask.sum())
-        matrix[:, mask] += fraction * spec.scale * delta[:, offset : offset + width]
-        proposal[key] = spec.project(matrix[:, 0] if value.ndim == 1 else matrix, state.params[key])
-        offset += width
+        value = state.params[key]
+        free = spec.mask(value)
+        width = _free_width(spec, value)
+        step = torch.zeros_like(_as_matrix(value))
+        step[:, free] = delta[:, column : column + width] * (fraction * spec.scale)
+        moved = _as_matrix(value) + step
+        proposal[key] = spec.project(moved[:, 0] if value.ndim == 1 else moved, value)
+        column += width
     return proposal
 
 
@@ -85,19 +112,20 @@ def dense_slide(state, config, screen=None):
     layout = trainable(state.params, state.parameters)
     rows = state.model.sample_rows(config.lm_rows, config.seed + state.iteration, state.target.device)
     accepted = 0
+    refined = getattr(config, "batched", False)
     for _ in range(config.lm_steps):
-        normal, gradient = reduced_system(state.model, state.params, state.target,
-                                          state.parameters, config, rows)  # fmt: skip
-        scale = normal.diag().clamp(min=normal.diag().max() * 1e-6 + 1e-30)
-        delta = solve(normal + config.damping * torch.diag(scale), -gradient, refined=getattr(config, "batched", False))
-        delta = delta.reshape(len(state.coefficients), -1)
-        length = delta.norm(dim=1, keepdim=True).clamp(min=1e-30)
-        delta *= (config.trust_radius / length).clamp(max=1)
-        if not torch.isfinite(delta).all():
+        normal, gradient = reduced_system(state.model, state.params, state.target, state.parameters, config, rows)
+        diag = normal.diagonal()
+        floor = diag.max() * 1e-6 + 1e-30
+        damped = normal + config.damping * torch.diag(diag.clamp(min=floor))
+        delta = solve(damped, -gradient, refined=refined).reshape(len(state.coefficients), -1)
+        radius = delta.norm(dim=1, keepdim=True).clamp(min=1e-30)
+        delta = delta * (config.trust_radius / radius).clamp(max=1)
+        if not bool(torch.isfinite(delta).all()):
             break
         bar = screen_bar(screen, state.params, config)
-        for fraction in (1.0, 0.5, 0.25):
-            trial = accept(state, _step_along(state, layout, delta, fraction), config, bar)
+        for fraction in BACKTRACK_DENSE:
+            trial = accept(state, _moved(state, layout, delta, fraction), config, bar)
             if trial is not None:
                 state, accepted = trial, accepted + 1
                 break
@@ -109,98 +137,115 @@ def dense_slide(state, config, screen=None):
 # --- joint: matrix-free Gauss-Newton over geometry and coefficients --------------------------
 
 
-def joint_system(model, params, coefficients, target, specs, config, seed):
-    """Scaled Gauss-Newton system of all trainable geometry and every coefficient.
+class _JointLayout:
+    """Packing of the joint unknowns: per trainable field, count x free-width geometry
+    entries (atom-major) in units of its scale; then the coefficients (re, im interleaved
+    when complex) in units of coefficient_scale."""
 
-    Returns matvec, gradient, a damped Jacobi diagonal and proposal(vector, fraction).
-    Products use the model's exact JVP and VJP; Rademacher probes only estimate the
-    diagonal. Coefficients are scaled by their magnitude, floored at a tenth of the
-    RMS magnitude.
+    def __init__(self, params, specs, b, complex_mode):
+        self.params, self.specs, self.b = params, specs, b
+        self.complex = complex_mode
+        self.count = len(b)
+        self.sections = []  # (key, free mask, slice)
+        start = 0
+        for key, spec in trainable(params, specs):
+            free = spec.mask(params[key])
+            stop = start + self.count * _free_width(spec, params[key])
+            self.sections.append((key, free, slice(start, stop)))
+            start = stop
+        self.geometry = start
+        self.size = start + (2 if complex_mode else 1) * self.count
+        amplitude = b.abs()
+        self.amplitude = amplitude
+        self.coefficient_scale = amplitude.clamp(min=amplitude.square().mean().sqrt() * 0.1 + 1e-20)
+
+    def coefficient_entries(self, values):
+        """Complex [count] per-coefficient values written into the packed coefficient slots."""
+        return torch.view_as_real(values).reshape(-1) if self.complex else values.real
+
+    def unpack(self, vector):
+        """(tangent of every field, coefficient change) of a packed vector."""
+        tangent = {key: torch.zeros_like(value) for key, value in self.params.items()}
+        for key, free, section in self.sections:
+            spec = self.specs[key]
+            target = _as_matrix(tangent[key])
+            target[:, free] = vector[section].reshape(self.count, -1) * spec.scale
+            tangent[key] = spec.tangent(tangent[key], self.params[key])
+        tail = vector[self.geometry :]
+        if self.complex:
+            return tangent, torch.complex(tail[0::2], tail[1::2]) * self.coefficient_scale
+        return tangent, (tail * self.coefficient_scale).to(self.b.dtype)
+
+    def pack_gradient(self, grads, coefficient):
+        """Packed vector of field gradients (tangent, masked, scaled) and the coefficient one."""
+        out = self.amplitude.new_zeros(self.size)
+        for key, free, section in self.sections:
+            spec = self.specs[key]
+            along = _as_matrix(spec.tangent(grads[key], self.params[key]))
+            out[section] = (along[:, free] * spec.scale).reshape(-1)
+        out[self.geometry :] = self.coefficient_entries(coefficient * self.coefficient_scale)
+        return out
+
+    def step_lengths(self, tangent):
+        """Per-atom length of a geometry tangent in units of each field's scale."""
+        total = self.amplitude.new_zeros(self.count)
+        for key, free, _ in self.sections:
+            total += (_as_matrix(tangent[key])[:, free] / self.specs[key].scale).square().sum(1)
+        return total.sqrt()
+
+
+def joint_system(model, params, coefficients, target, specs, config, seed):
+    """Scaled Gauss-Newton system of every trainable geometry component and coefficient.
+
+    Returns (matvec, gradient, damped Jacobi diagonal, proposal(vector, fraction)).
+    Products use the model's exact JVP and VJP; the Rademacher probes only estimate the
+    diagonal.
     """
     b = coefficients.to(target.dtype)
-    complex_mode = not config.real
-    count = len(b)
-    layout, offset = [], 0
-    for key, spec in trainable(params, specs):
-        mask = spec.mask(params[key])
-        width = count * int(mask.sum())
-        layout.append((key, mask, slice(offset, offset + width)))
-        offset += width
-    geometry = offset
-    size = geometry + (2 * count if complex_mode else count)
-    amplitude = b.abs()
-    coefficient_scale = amplitude.clamp(min=amplitude.square().mean().sqrt() * 0.1 + 1e-20)
+    layout = _JointLayout(params, specs, b, not config.real)
     power = target.abs().square().mean().clamp(min=1e-30)
     normalization = target.numel() * power
     ridge = config.ridge / power
-    ridge_diagonal = amplitude.new_zeros(size)
-    ridge_gradient = amplitude.new_zeros(size)
-    if complex_mode:
-        ridge_diagonal[geometry:] = (ridge * coefficient_scale.square()).repeat_interleave(2)
-        ridge_gradient[geometry:] = torch.view_as_real(b * (ridge * coefficient_scale)).flatten()
-    else:
-        ridge_diagonal[geometry:] = ridge * coefficient_scale.square()
-        ridge_gradient[geometry:] = ridge * coefficient_scale * b.real
-
-    def unpack(vector):
-        tangent = {key: torch.zeros_like(value) for key, value in params.items()}
-        for key, mask, section in layout:
-            value = tangent[key]
-            matrix = value[:, None] if value.ndim == 1 else value
-            matrix[:, mask] = vector[section].reshape(count, -1) * specs[key].scale
-            tangent[key] = specs[key].tangent(value, params[key])
-        tail = vector[geometry:]
-        if complex_mode:
-            return tangent, torch.complex(tail[0::2], tail[1::2]) * coefficient_scale
-        return tangent, (tail * coefficient_scale).to(b.dtype)
+    ridge_diagonal = layout.amplitude.new_zeros(layout.size)
+    ridge_gradient = layout.amplitude.new_zeros(layout.size)
+    scale = layout.coefficient_scale
+    ridge_diagonal[layout.geometry :] = (ridge * scale.square()).repeat_interleave(2 if layout.complex else 1)
+    ridge_gradient[layout.geometry :] = layout.coefficient_entries(b * (ridge * scale))
 
     def adjoint(upstream):
         grads, coefficient = model.vjp(params, b, upstream)
-        result = amplitude.new_zeros(size)
-        for key, mask, section in layout:
-            value = specs[key].tangent(grads[key], params[key])
-            matrix = value[:, None] if value.ndim == 1 else value
-            result[section] = (matrix[:, mask] * specs[key].scale).flatten()
-        tail = coefficient * coefficient_scale
-        result[geometry:] = torch.view_as_real(tail).flatten() if complex_mode else tail.real
-        return result
+        return layout.pack_gradient(grads, coefficient)
 
     gradient = adjoint(model.render(params, b) - target) / normalization + ridge_gradient
     draws = probe_signs((*target.shape, 2), seed, b.device)
     diagonal = torch.zeros_like(gradient)
     for _ in range(config.cg_probes):
-        signs = next(draws)
-        probe = torch.view_as_complex((2 * signs - 1).to(target.real.dtype))
+        probe = torch.view_as_complex((2 * next(draws) - 1).to(target.real.dtype))
         diagonal += adjoint(probe).square() / normalization
     diagonal = diagonal / config.cg_probes + ridge_diagonal
     diagonal = diagonal.clamp(min=diagonal.max().clamp(min=1e-30) * 1e-6)
     damping = config.damping * diagonal
+    shift = ridge_diagonal + damping
 
     def matvec(vector):
-        return adjoint(model.jvp(params, b, *unpack(vector))) / normalization + (ridge_diagonal + damping) * vector
+        return adjoint(model.jvp(params, b, *layout.unpack(vector))) / normalization + shift * vector
 
     def proposal(vector, fraction):
-        # One scale for every atom keeps the joint direction; the radial part of a
-        # unit-normal update is a null direction and must not shrink the step.
-        tangent, _ = unpack(vector)
-        lengths = amplitude.new_zeros(count)
-        for key, mask, _ in layout:
-            matrix = tangent[key][:, None] if tangent[key].ndim == 1 else tangent[key]
-            lengths += (matrix[:, mask] / specs[key].scale).square().sum(1)
-        scale = (config.trust_radius / lengths.sqrt().max().clamp(min=1e-30)).clamp(max=1)
-        return {
-            key: specs[key].project(value + tangent[key] * (scale * fraction), value)
-            for key, value in params.items()
-        }
+        # one step scale for every atom keeps the joint direction; a unit normal's radial
+        # part is a null direction and must not shrink the step
+        tangent, _ = layout.unpack(vector)
+        scale = (config.trust_radius / layout.step_lengths(tangent).max().clamp(min=1e-30)).clamp(max=1)
+        return {key: specs[key].project(value + tangent[key] * (scale * fraction), value)
+                for key, value in params.items()}  # fmt: skip
 
     return matvec, gradient, diagonal + damping, proposal
 
 
 @torch.no_grad()
 def joint_slide(state, config, screen=None):
-    """PCG steps of the joint system, built on joint_apertures sampled apertures.
+    """Joint Gauss-Newton steps, the system built on joint_apertures seeded apertures.
 
-    Sampling affects proposals only; acceptance uses every fitting observation.
+    The subset only shapes the proposal; acceptance refits on every observation.
     Returns the state and the number of accepted steps.
     """
     model, target = state.model, state.target
@@ -212,16 +257,15 @@ def joint_slide(state, config, screen=None):
         with stage("slide.system"):
             matvec, gradient, diagonal, proposal = joint_system(
                 model, state.params, state.coefficients, target, state.parameters, config,
-                config.seed + state.iteration + inner,
-            )  # fmt: skip
+                config.seed + state.iteration + inner)  # fmt: skip
         with stage("slide.pcg"):
-            delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations,
-                        tolerance=config.cg_tolerance)  # fmt: skip
-        if not (torch.isfinite(delta).all() and delta @ gradient < 0):
+            delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations, tolerance=config.cg_tolerance)
+        descent = torch.isfinite(delta).all() & (delta @ gradient < 0)
+        if not bool(descent):
             break
         with stage("slide.screen"):
             bar = screen_bar(screen, state.params, config)
-        for fraction in (1.0, 0.5, 0.25, 0.125):
+        for fraction in BACKTRACK_JOINT:
             with stage("slide.accept"):
                 trial = accept(state, proposal(delta, fraction), config, bar)
             if trial is not None:
