@@ -1,10 +1,19 @@
 """Fixed-budget support replacement.
 
-Both policies install a new support only if its refitted objective is lower.
-utility swaps the least useful atom for the best certificate candidate; merged pools
-many candidates with the whole support, ranks every atom by the cost of deleting it
-from one pooled fit and keeps the budget's cheapest-to-lose complement. Behaviour
-follows the reference's dsplat/replacement.py:27-270.
+Both policies install a new support only when its refitted objective is lower.
+
+utility  (one slot per step) swaps the least useful atom for the best certificate
+         candidate;
+merged   pools many candidates with the whole support, fits the pool once, ranks every
+         pooled atom by what deleting it would cost, deletes the cheapest until the
+         budget holds and lets surviving candidates take the freed slots.
+
+Semantics of the reference's dsplat/replacement.py:27-270. The pooled fit is organized
+around _PooledFit: the Gram of support + candidates is assembled from the state's own
+support block and one cross product of all pooled rows against the new columns (a
+tcgen05 launch in bf16x3 mode); the deletion order comes from backward elimination on its
+regularized inverse (batched mode: one CUDA kernel per deletion on the inverse Cholesky
+factor, which costs a quarter of forming the inverse).
 """
 
 from __future__ import annotations
@@ -15,78 +24,75 @@ import torch
 
 from .certificate import certificate
 from .kernels import search
+from .linalg import shifted_cholesky
+from .normal import TensorCoreGram, fused_rows, row_chunk
 from .parameters import periodic_delta
 from .tracing import stage
-from .varpro import (
-    Fit,
-    accept,
-    fit_coefficients,
-    rendered_loss,
-    row_chunk,
-    screen_bar,
-    shifted_cholesky,
-    varpro,
-)
+from .varpro import Fit, accept, fit_coefficients, rendered_loss, screen_bar, varpro
 
 
 def _feasible(state, pool, owner):
-    """The pool as feasible atoms; fields the pool lacks copy slot owner."""
-    count = len(pool["centers"])
-    result = {}
+    """The pool as feasible atoms; fields the pool lacks are copied from slot owner."""
+    size = len(pool["centers"])
+    atoms = {}
     for key, spec in state.parameters.items():
-        reference = state.params[key][owner].expand(count, *state.params[key].shape[1:])
-        result[key] = spec.project(pool.get(key, reference), reference)
-    return result
+        donor = state.params[key][owner].expand(size, *state.params[key].shape[1:])
+        atoms[key] = spec.project(pool.get(key, donor), donor)
+    return atoms
 
 
 # --- utility: one slot per step --------------------------------------------------------------
 
 
-def utility(gram, coefficients):
-    """Half relative amplitude, half unregularized projection efficiency of every atom.
+def _projection_efficiency(gram):
+    """1 / sqrt(max(G^-1_jj G_jj, 1)) per atom; G+ on a singular Gram.
 
-    Efficiency is 1 / sqrt(G^-1_jj G_jj). For a singular Gram a column is redundant
-    exactly when its coordinate takes part in the nullspace; the others use G+.
+    A singular Gram marks a column redundant (efficiency 0) exactly when its coordinate
+    takes part in the nullspace; zero columns are redundant too.
     """
-    chol, info = torch.linalg.cholesky_ex(gram)
-    diag = gram.diag().real
-    if int(info) == 0:
-        inverse_diag = torch.cholesky_inverse(chol).diag().real
-        efficiency = (1 / (inverse_diag * diag).clamp(min=1)).sqrt()
-    else:
-        values, vectors = torch.linalg.eigh(gram)
-        eps = torch.finfo(values.dtype).eps
-        active = values > values.abs().max() * len(values) * eps
-        inv = torch.where(active, values.clamp(min=torch.finfo(values.dtype).tiny).reciprocal(), 0)
-        inverse_diag = (vectors.abs().square() * inv[None]).sum(1)
-        null_weight = vectors[:, ~active].abs().square().sum(1)
-        efficiency = (1 / (inverse_diag * diag).clamp(min=1)).sqrt()
-        efficiency = torch.where(null_weight > len(values) * eps * 10, 0, efficiency)
-        efficiency = torch.where(diag > 0, efficiency, 0)
+    factor, status = torch.linalg.cholesky_ex(gram)
+    scale = gram.diagonal().real
+    if int(status) == 0:
+        inverse_diag = torch.cholesky_inverse(factor).diagonal().real
+        return (inverse_diag * scale).clamp(min=1).rsqrt()
+    values, vectors = torch.linalg.eigh(gram)
+    eps = torch.finfo(values.dtype).eps
+    kept = values > values.abs().max() * len(values) * eps
+    reciprocal = torch.where(kept, values.clamp(min=torch.finfo(values.dtype).tiny).reciprocal(), 0)
+    weight = vectors.abs().square()
+    inverse_diag = weight @ reciprocal
+    in_null = (weight * (~kept)).sum(1) > len(values) * eps * 10
+    efficiency = (inverse_diag * scale).clamp(min=1).rsqrt()
+    return torch.where(in_null | (scale <= 0), 0, efficiency)
+
+
+def utility(gram, coefficients):
+    """Half relative amplitude, half unregularized projection efficiency, per atom."""
     magnitude = coefficients.abs()
-    return 0.5 * magnitude / magnitude.max().clamp(min=1e-30) + 0.5 * efficiency
+    return 0.5 * magnitude / magnitude.max().clamp(min=1e-30) + 0.5 * _projection_efficiency(gram)
 
 
 @torch.no_grad()
 def replace_one(state, config, pool, screen=None):
-    """Try the best pool candidate in the least useful slot; the state and atoms replaced."""
+    """Try the best pool candidate in the least useful slot; (state, atoms replaced)."""
     owner = int(utility(state.gram, state.coefficients).argmin())
     candidate = _feasible(state, pool, owner)
-    residual = state.target - state.prediction
-    scores = certificate(state.model, candidate, residual, config.coefficients)
+    scores = certificate(state.model, candidate, state.target - state.prediction, config.coefficients)
     if config.min_separation > 0:
-        centers, period = state.params["centers"], state.parameters["centers"].period
+        support, period = state.params["centers"], state.parameters["centers"].period
         for start in range(0, len(scores), 256):
-            delta = periodic_delta(candidate["centers"][start : start + 256, None] - centers[None], period)
-            near = delta.norm(dim=-1).min(1).values < config.min_separation
-            scores[start : start + 256][near] = -torch.inf
-    scores[~torch.isfinite(scores)] = -torch.inf
-    index = int(scores.argmax())
-    if not scores[index] > 0:
+            gap = periodic_delta(candidate["centers"][start : start + 256, None] - support[None], period)
+            too_close = gap.norm(dim=-1).amin(1) < config.min_separation
+            scores[start : start + 256].masked_fill_(too_close, -torch.inf)
+    scores = torch.where(torch.isfinite(scores), scores, -torch.inf)
+    best = scores.argmax()
+    pick, positive = torch.stack((best.double(), (scores[best] > 0).double())).tolist()
+    if not positive:
         return state, 0
+    pick = int(pick)
     proposal = {key: value.clone() for key, value in state.params.items()}
     for key in proposal:
-        proposal[key][owner] = candidate[key][index]
+        proposal[key][owner] = candidate[key][pick]
     accepted = accept(state, proposal, config, screen_bar(screen, state.params, config))
     return (state, 0) if accepted is None else (accepted, 1)
 
@@ -95,7 +101,7 @@ def replace_one(state, config, pool, screen=None):
 
 
 def regularized_inverse(h, floor):
-    """Inverse of h + floor lambda_max(h) I in double precision, or None."""
+    """(h + floor lambda_max(h) I)^-1 in float64, or None."""
     with stage("inverse.cholesky"):
         factor = shifted_cholesky(h, floor)
     if factor is None:
@@ -105,11 +111,7 @@ def regularized_inverse(h, floor):
 
 
 def regularized_inverse_factor(h, floor):
-    """X = L^-1 with L the factor of regularized_inverse's shifted system (inverse = X^H X).
-
-    The batched replacement eliminates from X: a triangular inverse (trtri) costs a quarter
-    of forming the inverse (potri) at float64 on this GPU.
-    """
+    """X = L^-1 of the factor of regularized_inverse's shifted system (inverse = X^H X)."""
     with stage("inverse.cholesky"):
         factor = shifted_cholesky(h, floor)
     if factor is None:
@@ -119,16 +121,15 @@ def regularized_inverse_factor(h, floor):
 
 
 def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, on_device=False, factored=False):
-    """Remove count unknowns one at a time from the least squares with this inverse.
+    """Indices of count unknowns removed one at a time from a least-squares fit, in order.
 
-    With W the inverse of the current system and b = W q, deleting unknown j and
-    refitting raises the objective by |b_j|^2 / W_jj; each step deletes the cheapest
-    and continues with W - w w^H / W_jj (w = W[:, j]), kept as rank-one corrections.
-    At most limit of the unknowns marked in limited are removed. Returns the removed
-    indices in order. on_device runs the loop as one CUDA kernel per step
-    (dsg_backward_elimination) instead of about ten PyTorch launches; the arithmetic is
-    the same up to the order of the float64 sums. factored means inverse is the factor X
-    of regularized_inverse_factor (the inverse being X^H X).
+    With W the inverse of the current normal matrix and b = W q, removing unknown j and
+    refitting raises the objective by |b_j|^2 / W_jj. Each step removes the cheapest
+    unknown, then updates b and the diagonal by the rank-one downdate
+    W <- W - w w^H / W_jj (w = W[:, j]), kept as a list of scaled columns. At most limit
+    of the unknowns flagged in limited may go. on_device runs one CUDA kernel per step
+    (the same arithmetic up to the order of float64 sums); factored means inverse holds
+    X with W = X^H X.
     """
     if factored:
         if on_device and inverse.is_cuda:
@@ -136,200 +137,211 @@ def backward_elimination(inverse, rhs, count, limited=None, limit=0, *, on_devic
         inverse = inverse.mH @ inverse
     if on_device and inverse.is_cuda:
         return search.backward_elimination(inverse, rhs, count, limited, limit)
-    size = len(inverse)
+    n = len(inverse)
+    device = inverse.device
     b = inverse @ rhs.to(inverse.dtype)
-    diagonal = inverse.diagonal().real.clone()
-    alive = torch.ones(size, device=inverse.device, dtype=torch.bool)
-    updates = inverse.new_zeros((size, count))
-    removed = torch.zeros(count, device=inverse.device, dtype=torch.long)
-    spent = torch.zeros((), device=inverse.device, dtype=torch.long)
-    tiny = torch.finfo(diagonal.dtype).tiny
-    # Indexing with device tensors (index_select / index_fill_) keeps every step on the
-    # device: no value is read back, so the loop can also be captured in a CUDA graph.
-    for step in range(count):
-        cost = b.abs().square() / diagonal.clamp(min=tiny)
-        blocked = ~alive if limited is None else ~alive | (limited & (spent >= limit))
-        index = cost.masked_fill(blocked, torch.inf).argmin().view(1)
-        column = inverse.index_select(1, index)[:, 0]
-        if step:
-            column = column - updates[:, :step] @ updates.index_select(0, index)[0, :step].conj()
-        pivot = column.index_select(0, index).real.clamp(min=tiny)
-        b = b - column * (b.index_select(0, index) / pivot)
-        scaled = column / pivot.sqrt()
-        updates[:, step] = scaled
-        diagonal = diagonal - scaled.abs().square()
-        alive.index_fill_(0, index, False)
-        diagonal.index_fill_(0, index, 1.0)  # a removed unknown stays masked; this keeps its cost finite
-        b.index_fill_(0, index, 0)
-        removed[step : step + 1] = index
+    diag = inverse.diagonal().real.clone()
+    tiny = torch.finfo(diag.dtype).tiny
+    downdates = inverse.new_zeros((n, count))  # scaled columns w / sqrt(W_jj) of every removal
+    gone = torch.zeros(n, dtype=torch.bool, device=device)
+    order = torch.zeros(count, dtype=torch.long, device=device)
+    used = torch.zeros((), dtype=torch.long, device=device)
+    # every index below stays a device tensor (index_select / index_fill_): no value is read back
+    for k in range(count):
+        blocked = gone if limited is None else gone | (limited & (used >= limit))
+        j = (b.abs().square() / diag.clamp(min=tiny)).masked_fill(blocked, torch.inf).argmin().reshape(1)
+        w = inverse.index_select(1, j).squeeze(1)
+        if k:
+            w = w - downdates[:, :k] @ downdates.index_select(0, j).squeeze(0)[:k].conj()
+        pivot = w.index_select(0, j).real.clamp(min=tiny)
+        b = b - w * (b.index_select(0, j) / pivot)
+        column = w / pivot.sqrt()
+        downdates[:, k] = column
+        diag = diag - column.abs().square()
+        gone.index_fill_(0, j, True)
+        diag.index_fill_(0, j, 1.0)  # keeps the masked cost of a removed unknown finite
+        b.index_fill_(0, j, 0)
+        order[k : k + 1] = j
         if limited is not None:
-            spent = spent + limited.index_select(0, index)[0]
-    return removed
+            used = used + limited.index_select(0, j).squeeze(0)
+    return order
 
 
 def _distinct(scores, points, occupied, period, separation, width):
-    """Best-scoring candidates colliding neither with the support nor with each other.
+    """Up to width best-scoring candidates colliding neither with occupied nor each other.
 
-    A collision is a distance below separation, or exactly zero (an atom pooled twice
-    would make the pooled system singular for no gain).
+    A collision is a distance below separation, or exactly zero (one atom pooled twice
+    would make the pooled system singular for nothing). Candidates are taken best first
+    in blocks of 1024; inside a block a candidate yields only to a better kept one.
     """
 
-    def distance(a, b):
+    def distances(a, b):
         return periodic_delta(a[:, None] - b[None], period).norm(dim=-1)
 
-    order = scores.argsort(descending=True, stable=True)
-    order = order[torch.isfinite(scores[order])]
-    kept, found = [], 0
-    for start in range(0, len(order), 1024):
-        if found >= width:
+    def clear(gap):
+        return (gap >= separation) & (gap > 0)
+
+    ranked = scores.argsort(descending=True, stable=True)
+    ranked = ranked[torch.isfinite(scores[ranked])]
+    kept, total = [], 0
+    for start in range(0, len(ranked), 1024):
+        if total >= width:
             break
-        ids = order[start : start + 1024]
+        ids = ranked[start : start + 1024]
         block = points[ids]
-        near = distance(block, occupied).min(1).values
-        free = (near >= separation) & (near > 0)
-        for previous in kept:
-            near = distance(block, points[previous]).min(1).values
-            free &= (near >= separation) & (near > 0)
-        inside = distance(block, block)
-        clash = ((inside < separation) | (inside == 0)).triu(1)
-        if bool(clash[free][:, free].any()):
-            # Greedy by score: a candidate yields only to a kept better one.
+        free = clear(distances(block, occupied).amin(1))
+        for earlier in kept:
+            free &= clear(distances(block, points[earlier]).amin(1))
+        conflict = (~clear(distances(block, block))).triu(1)
+        if bool(conflict[free][:, free].any()):
             for i in free.nonzero().flatten().tolist():
-                if bool((clash[:i, i] & free[:i]).any()):
+                if bool((conflict[:i, i] & free[:i]).any()):
                     free[i] = False
         kept.append(ids[free])
-        found += int(free.sum())
-    return torch.cat(kept)[:width] if kept else order[:0]
+        total += int(free.sum())
+    return torch.cat(kept)[:width] if kept else ranked[:0]
+
+
+def _cross_on_tensor_cores(model, pool, target, support, chunk):
+    """(cross [total, added] = A^T A[:, support:], right = A[:, support:]^T y), tcgen05 Gram."""
+    total = len(pool["centers"])
+    gram = TensorCoreGram(model, total, chunk, target.device)
+    status = fused_rows(model, pool, gram.store, chunk)
+    if status is None:
+        right = torch.zeros(total - support, dtype=torch.float64, device=target.device)
+        for a, y in model.blocks(pool, target, True, chunk):
+            gram.store.append(a)
+            right += a[:, support:].T @ y
+    else:
+        from .kernels.gram import check
+
+        right = model.correlate({key: value[support:] for key, value in pool.items()}, target)[0].real.double()
+        check(status)
+    products, _ = gram.finish(column_from=support)
+    new = products[support:, support:]
+    cross = torch.cat((products[:support, support:], torch.triu(new) + torch.triu(new, 1).T))
+    return cross.float(), right.float()
 
 
 def pooled_statistics(state, pool, config):
-    """Gram and right-hand side over the support followed by the pooled new atoms.
+    """Gram and right-hand side of the support followed by the pooled new atoms.
 
-    Only the new columns are streamed; the support block is the state's. With
-    DSFWConfig.gram == "bf16x3" (real coefficients) the cross products of all pooled
-    rows against the new columns are one tcgen05 launch over the stored split rows.
+    Only the new columns are streamed; the support block is the state's.
     """
-    model, count = state.model, len(state.coefficients)
-    total, added = len(pool["centers"]), len(pool["centers"]) - count
-    gram = state.gram.new_empty((total, total))
-    rhs = state.rhs.new_empty(total)
-    gram[:count, :count], rhs[:count] = state.gram, state.rhs
+    model, support = state.model, len(state.coefficients)
+    total = len(pool["centers"])
     chunk = row_chunk(model, total, config)
     if config.real and getattr(config, "gram", "fp32") == "bf16x3":
-        cross, right = _pooled_cross_mixed(model, pool, state.target, count, added, chunk, config)
+        cross, right = _cross_on_tensor_cores(model, pool, state.target, support, chunk)
     else:
-        cross = state.gram.new_zeros((total, added))
-        right = state.rhs.new_zeros(added)
+        cross = state.gram.new_zeros((total, total - support))
+        right = state.rhs.new_zeros(total - support)
         for a, y in model.blocks(pool, state.target, config.real, chunk):
-            new = a[:, count:]
-            cross.addmm_(a.H, new)
-            right.addmv_(new.H, y)
-    cross /= model.size
-    gram[:, count:], gram[count:, :] = cross, cross.H
-    gram[count:, count:] = (cross[count:] + cross[count:].H) * 0.5
-    rhs[count:] = right / model.size
+            fresh = a[:, support:]
+            cross.addmm_(a.mH, fresh)
+            right.addmv_(fresh.mH, y)
+    cross = cross / model.size
+    gram = state.gram.new_empty((total, total))
+    gram[:support, :support] = state.gram
+    gram[:, support:] = cross
+    gram[support:, :] = cross.mH
+    gram[support:, support:] = (cross[support:] + cross[support:].mH) * 0.5
+    rhs = torch.cat((state.rhs, right / model.size))
     return gram, rhs
 
 
-def _pooled_cross_mixed(model, pool, target, count, added, chunk, config):
-    """cross [total, added] = A^T A[:, count:] and right = A[:, count:]^T y on the tensor cores."""
-    from .kernels.gram import GramRows, check
-    from .varpro import fused_rows, projected_rows
+def _all_free(spec):
+    flags = spec.trainable
+    return all(bool(f) for f in flags) if isinstance(flags, (tuple, list)) else bool(flags)
 
-    total = count + added
-    device = target.device
-    store = GramRows(total, projected_rows(model, chunk), device)
-    fused = fused_rows(model, pool, store, chunk)
-    if fused is not None:
-        new = {key: value[count:] for key, value in pool.items()}
-        right = model.correlate(new, target)[0].real.double()
-        check(fused)
-    else:
-        right = torch.zeros(added, dtype=torch.float64, device=device)
-        for a, y in model.blocks(pool, target, True, chunk):
-            store.append(a)
-            right += a[:, count:].T @ y
-    products = torch.zeros((total, total), dtype=torch.float64, device=device)
-    check(store.accumulate(products, column_from=count))
-    cross = torch.empty((total, added), dtype=torch.float64, device=device)
-    cross[:count] = products[:count, count:]
-    block = products[count:, count:]
-    cross[count:] = torch.triu(block) + torch.triu(block, 1).T
-    return cross.to(torch.float32), right.to(torch.float32)
+
+class _PooledFit:
+    """One regularized fit of support + candidates and the deletions it ranks."""
+
+    def __init__(self, state, pool, config):
+        self.state, self.pool, self.config = state, pool, config
+        self.support = len(state.coefficients)
+        with stage("replace.pooled"):
+            self.gram, self.rhs = pooled_statistics(state, pool, config)
+        h = self.gram.real if config.real else self.gram
+        if config.ridge:
+            h = h.clone()
+            h.diagonal().add_(config.ridge)
+        self.q = self.rhs.real if config.real else self.rhs
+        self.batched = getattr(config, "batched", False)
+        self.factored = self.batched and h.is_cuda
+        floor = len(h) * torch.finfo(h.real.dtype).eps
+        with stage("replace.inverse"):
+            self.inverse = (regularized_inverse_factor if self.factored else regularized_inverse)(h, floor)
+        self.is_old = torch.arange(len(self.q), device=self.q.device) < self.support
+
+    def survivors(self, deletions, limit):
+        """(slot -> pooled index map, owners: old slots that left) after the deletions."""
+        with stage("replace.elimination"):
+            removed = backward_elimination(self.inverse, self.q, deletions, None if limit is None else self.is_old,
+                                           limit or 0, on_device=self.batched, factored=self.factored)  # fmt: skip
+        dropped = torch.zeros(len(self.q), dtype=torch.bool, device=self.q.device)
+        dropped[removed] = True
+        owners = dropped[: self.support].nonzero().flatten()
+        slots = torch.arange(self.support, device=self.q.device)
+        if len(owners):
+            slots[owners] = (~dropped[self.support :]).nonzero().flatten() + self.support
+        return slots, owners
+
+    def trial(self, slots, owners):
+        """Support of the surviving atoms (new atoms take their slot's frozen fields) and its fit."""
+        state = self.state
+        atoms = {key: value[slots] for key, value in self.pool.items()}
+        # new atoms copied slot 0's frozen fields when pooled; they take the ones of the
+        # slot they fill, and then their pooled columns no longer apply
+        moved = False
+        for key, spec in state.parameters.items():
+            if _all_free(spec):
+                continue
+            fixed = spec.project(atoms[key][owners], state.params[key][owners])
+            moved = moved or not torch.equal(fixed, atoms[key][owners])
+            atoms[key][owners] = fixed
+        if moved:
+            with stage("replace.refit"):
+                return atoms, varpro(state.model, atoms, state.target, self.config)
+        gram = self.gram[slots[:, None], slots[None, :]]
+        rhs = self.rhs[slots]
+        coefficients = fit_coefficients(gram, rhs, self.config)
+        prediction, objective = rendered_loss(state.model, atoms, coefficients, state.target, self.config.ridge)
+        return atoms, Fit(coefficients, prediction, objective, gram, rhs)
 
 
 @torch.no_grad()
 def merge_support(state, config, pool, scores=None):
     """Pool the best candidates with the support, fit once, prune back to the budget.
 
-    One regularized pooled fit ranks old and new atoms by the cost of deleting them;
-    the cheapest leave until the budget is met and surviving new atoms take the slots
-    of old atoms that left. The result needs a lower rendered objective; a rejected
-    support is retried with half as many old atoms allowed to leave. Returns the state
-    and the number of atoms replaced.
+    The pooled fit ranks old and new atoms by the cost of deleting them; the cheapest
+    leave until the budget is met, and surviving new atoms take the slots of old atoms
+    that left. The result must lower the rendered objective; a rejected support is
+    retried allowing half as many old atoms to leave. Returns (state, atoms replaced).
     """
-    centers = state.params["centers"]
-    count = len(centers)
+    support = state.params["centers"]
     candidate = _feasible(state, pool, 0)
     if scores is None:
-        residual = state.target - state.prediction
-        scores = certificate(state.model, candidate, residual, config.coefficients)
+        scores = certificate(state.model, candidate, state.target - state.prediction, config.coefficients)
     with stage("replace.distinct"):
         period = state.parameters["centers"].period
-        if getattr(config, "batched", False):
-            chosen = search.distinct(scores, candidate["centers"], centers, period,
-                                     config.min_separation, config.batch)  # fmt: skip
-        else:
-            chosen = _distinct(scores, candidate["centers"], centers, period, config.min_separation,
-                               config.batch)  # fmt: skip
+        pick = search.distinct if getattr(config, "batched", False) else _distinct
+        chosen = pick(scores, candidate["centers"], support, period, config.min_separation, config.batch)
     if not len(chosen):
         return state, 0
-    pool = {key: torch.cat((value, candidate[key][chosen])) for key, value in state.params.items()}
-    with stage("replace.pooled"):
-        gram, rhs = pooled_statistics(state, pool, config)
-    real = config.real
-    eye = torch.eye(len(gram), dtype=gram.dtype, device=gram.device)
-    h = (gram.real if real else gram) + config.ridge * eye
-    factored = getattr(config, "batched", False) and h.is_cuda
-    with stage("replace.inverse"):
-        floor = len(h) * torch.finfo(h.real.dtype).eps
-        inverse = regularized_inverse_factor(h, floor) if factored else regularized_inverse(h, floor)
-    if inverse is None:
+    pooled = {key: torch.cat((value, candidate[key][chosen])) for key, value in state.params.items()}
+    fit = _PooledFit(state, pooled, config)
+    if fit.inverse is None:
         return state, 0
-    q = rhs.real if real else rhs
-    old = torch.arange(len(q), device=q.device) < count
     limit = None
     while True:
-        with stage("replace.elimination"):
-            removed = backward_elimination(inverse, q, len(chosen), None if limit is None else old,
-                                           limit or 0, on_device=getattr(config, "batched", False),
-                                           factored=factored)  # fmt: skip
-        gone = torch.zeros(len(q), device=q.device, dtype=torch.bool)
-        gone[removed] = True
-        owners = gone[:count].nonzero().flatten()
+        slots, owners = fit.survivors(len(chosen), limit)
         if not len(owners):
             return state, 0
-        ids = torch.arange(count, device=q.device)
-        ids[owners] = (~gone[count:]).nonzero().flatten() + count
-        trial = {key: value[ids] for key, value in pool.items()}
-        # New atoms copied slot 0's frozen components; they take those of the slot they
-        # fill, and then their pooled columns no longer apply.
-        moved = False
-        for key, spec in state.parameters.items():
-            if not spec.mask(trial[key]).all():
-                fixed = spec.project(trial[key][owners], state.params[key][owners])
-                moved = moved or not torch.equal(fixed, trial[key][owners])
-                trial[key][owners] = fixed
-        if moved:
-            with stage("replace.refit"):
-                fit = varpro(state.model, trial, state.target, config)
-        else:
-            trial_gram, trial_rhs = gram[ids[:, None], ids[None, :]], rhs[ids]
-            b = fit_coefficients(trial_gram, trial_rhs, config)
-            fit = Fit(b, *rendered_loss(state.model, trial, b, state.target, config.ridge),
-                      trial_gram, trial_rhs)  # fmt: skip
-        if fit.objective < state.objective:
-            return replace(state, params=trial, **fit._asdict()), len(owners)
+        atoms, result = fit.trial(slots, owners)
+        if result.objective < state.objective:
+            return replace(state, params=atoms, **result._asdict()), len(owners)
         limit = len(owners) // 2
         if limit < 1:
             return state, 0

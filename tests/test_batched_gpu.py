@@ -149,7 +149,8 @@ def test_fused_ascent_iterations_match_the_pytorch_iterations(fmcw, mode, with_n
     the same accepted steps, centers within a thousandth of their step scale, normals within
     1e-5, values, gradients and BFGS inverses within 1e-4."""
     from dsplat import ParameterConfig
-    from dsplat.certificate import CertificateSearchConfig, _closures, _controls, _fused_iteration, _iteration
+    from dsplat.ascent import _closures, _fused_iteration, _iteration
+    from dsplat.certificate import CertificateSearchConfig, _controls
 
     model, params, _ = fmcw
     residual = model.scan.data

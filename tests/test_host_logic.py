@@ -251,7 +251,7 @@ def test_fused_ascent_takes_only_surfel_candidates():
     and areas, and at most 16 backtracking fractions; anything else keeps the PyTorch loop."""
     from types import SimpleNamespace
 
-    from dsplat.certificate import _fusable
+    from dsplat.ascent import _fusable
 
     class Tensorish:
         is_cuda = True
