@@ -1,10 +1,17 @@
-"""Spatial candidate search: hierarchical 3D grids and continuous certificate refinement.
+"""Spatial candidate search: hierarchical 3-D grids and continuous certificate refinement.
 
-Each step, before replacement, builds a fresh candidate set inside the box of the
-centers' bounds: a range-gated coarse grid plus cached peaks, finer cubes around
-separated peaks, quasi-Newton refinement on a subset of apertures, then on all of
-them. Trainable unit normals use a sphere bank and joint refinement; frozen fields
-copy slot 0. Behaviour follows the reference's dsplat/spatial.py:26-178.
+Every step, before replacement, builds a fresh candidate pool inside the box of the
+centers' bounds:
+
+  1. a coarse grid over the box (finer and shifted after failed steps), range-gated by
+     the measured profiles, plus the peaks kept from the previous step;
+  2. per finer level, a cube of offsets around every separated peak of the last level;
+  3. quasi-Newton certificate ascent of the separated peaks on an aperture subset, then
+     of the best few on every aperture.
+
+Positions are scored with their best normal from a sphere bank (FFT-interpolated range
+table, one CUDA launch per chunk) when normals are trainable; fields the search does not
+move copy slot 0. Semantics of the reference's dsplat/spatial.py:26-178.
 """
 
 from __future__ import annotations
@@ -23,6 +30,9 @@ from .certificate import (
     select_peaks,
 )
 from .tracing import stage
+
+GRID_SHIFT = (0.37, 0.61, 0.23)  # cell fractions of the coarse grid's shift after failures
+REFINE_SEED = 1000003  # seed offset of the refinement's aperture subset
 
 
 @dataclass(frozen=True)
@@ -46,119 +56,155 @@ class SpatialSearchConfig:
     continuous: CertificateSearchConfig = field(default_factory=CertificateSearchConfig)
 
 
-def _points_per_box(lower, upper, pitch):
-    return prod(1 + ceil(float(b - a) / pitch) for a, b in zip(lower, upper, strict=True))
+def _grid_size(lower, upper, pitch):
+    """Points candidate_grid(lower, upper, pitch) would make."""
+    return prod(1 + ceil(float(hi - lo) / pitch) for lo, hi in zip(lower, upper, strict=True))
+
+
+def _coarsened(lower, upper, pitch, budget):
+    """pitch grown by 10 % steps until the grid fits in budget points."""
+    while _grid_size(lower, upper, pitch) > budget:
+        pitch *= 1.1
+    return pitch
+
+
+def _take(atoms, index):
+    return {key: value[index] for key, value in atoms.items()}
+
+
+def _free_axes(spec, width=3):
+    """Per-axis trainable flags of a field, on the host."""
+    flags = spec.trainable
+    return [bool(f) for f in flags] if isinstance(flags, (tuple, list)) else [bool(flags)] * width
+
+
+class _Proposer:
+    """One step's search: the sampled apertures, the residual, and how positions are scored."""
+
+    def __init__(self, state, config, search):
+        self.state, self.config, self.search = state, config, search
+        self.spec = state.parameters["centers"]
+        self.normal_spec = state.parameters["normals"]
+        normals_free = self.normal_spec.any_free
+        self.refine_normals = self.normal_spec if normals_free and search.joint_normals else None
+        self.mode = config.coefficients
+        self.residual = state.target - state.prediction
+        self.ids, self.model = state.model.sample_apertures(search.proposal_apertures,
+                                                            config.seed + state.iteration)  # fmt: skip
+        self.sub_residual = self.residual[self.ids]
+        self.banked = normals_free and search.normal_candidates > 0
+        oversample = search.fft_oversample
+        self.table = self.model.range_table(self.sub_residual, oversample) if self.banked and oversample else None
+
+    def atoms(self, points, normals=None):
+        """Feasible atoms at points (fields copied from slot 0), optionally with normals."""
+        size = len(points)
+        result = {key: value[:1].expand(size, *value.shape[1:]).clone() for key, value in self.state.params.items()}
+        result["centers"] = self.spec.project(points, result["centers"])
+        if normals is not None:
+            result["normals"] = self.normal_spec.project(normals, result["normals"])
+        return result
+
+    def score(self, candidates):
+        """Certificates on the sampled apertures; with a bank, the candidates take their best normal."""
+        if not self.banked:
+            return certificate(self.model, candidates, self.sub_residual, self.mode)
+        oriented, scores = orient_candidates(self.model, candidates, self.sub_residual, self.search.normal_candidates,
+                                             self.mode, self.table)  # fmt: skip
+        candidates["normals"] = oriented["normals"]
+        return scores
+
+    def coarse_candidates(self):
+        """Range-gated coarse grid over the box plus the cached peaks of the last step."""
+        state, search, spec = self.state, self.search, self.spec
+        centers = state.params["centers"]
+        failures = state.search_failures
+        free = _free_axes(spec)
+        box = torch.stack((centers.new_tensor(spec.lower).expand(3), centers.new_tensor(spec.upper).expand(3)))
+        pinned = [axis for axis in range(3) if not free[axis]]
+        if pinned:
+            box[:, pinned] = centers[0, pinned]
+        lower, upper = box.tolist()
+        spacing = _coarsened(lower, upper, search.coarse_spacing / (1 + min(failures, 2)), search.max_candidates)
+        points = candidate_grid(lower, upper, spacing, device=centers.device)
+        if failures:
+            shift = points.new_tensor(GRID_SHIFT) * (spacing * ((failures % 3) + 1) / 3)
+            points = spec.project(points + shift, points)
+        if failures < search.ungated_after:
+            loosen = 1 + failures
+            hit = self.model.range_gate(points, state.target[self.ids], relative_power=search.range_power / loosen,
+                                        margin_cells=search.range_margin_cells * loosen,
+                                        min_fraction=search.range_fraction)  # fmt: skip
+            if bool(hit.any()):  # an empty gate never stops the search
+                points = points[hit]
+        carried = 0
+        if state.peak_cache is not None:
+            carried = min(len(state.peak_cache["centers"]), search.max_candidates - len(points))
+            points = torch.cat((points, state.peak_cache["centers"][:carried]))
+        candidates = self.atoms(points)
+        if carried:
+            tail = candidates["normals"][-carried:]
+            candidates["normals"][-carried:] = self.normal_spec.project(state.peak_cache["normals"][:carried], tail)
+        return candidates
+
+    def level_candidates(self, peaks, radius, pitch):
+        """A cube of offsets (radius, pitch) around each peak; frozen axes get no offsets."""
+        free = _free_axes(self.spec)
+        low = [-radius if f else 0.0 for f in free]
+        high = [radius if f else 0.0 for f in free]
+        pitch = _coarsened(low, high, pitch, self.search.max_candidates)
+        offsets = candidate_grid(low, high, pitch, device=peaks["centers"].device)
+        # the best-ranked peaks keep priority inside the per-level budget
+        peaks = {key: value[: max(1, self.search.max_candidates // len(offsets))] for key, value in peaks.items()}
+        points = (peaks["centers"][:, None, :] + offsets[None]).reshape(-1, 3)
+        return self.atoms(points, peaks["normals"].repeat_interleave(len(offsets), dim=0))
 
 
 @torch.no_grad()
 def propose(state, config, search):
     """Refined candidates, their scores best first, and the peaks kept for the next step.
 
-    After failed steps (state.search_failures) the coarse grid gets finer and shifts by
-    a fraction of a cell, more peaks are kept and the range gate loosens.
+    After failed steps (state.search_failures) the coarse grid gets finer and shifts by a
+    fraction of a cell, more peaks are kept and the range gate loosens.
     """
-    centers = state.params["centers"]
-    spec, normal_spec = state.parameters["centers"], state.parameters["normals"]
-    free_normals = bool(normal_spec.mask(state.params["normals"]).any())
-    refine_normals = normal_spec if free_normals and search.joint_normals else None
-    failures, mode = state.search_failures, config.coefficients
-    residual = state.target - state.prediction
-    ids, model = state.model.sample_apertures(search.proposal_apertures, config.seed + state.iteration)
-    r = residual[ids]
-    banked = free_normals and search.normal_candidates
-    table = model.range_table(r, search.fft_oversample) if banked and search.fft_oversample else None
+    finder = _Proposer(state, config, search)
+    ascent_config = search.continuous
+    wanted = min(ascent_config.peaks * (1 + state.search_failures), 4 * ascent_config.peaks)
+    separation = ascent_config.separation
+    batched = getattr(config, "batched", False)
 
-    def score(candidates):
-        if banked:
-            oriented, scores = orient_candidates(model, candidates, r, search.normal_candidates,
-                                                 mode, table)  # fmt: skip
-            candidates["normals"] = oriented["normals"]
-            return scores
-        return certificate(model, candidates, r, mode)
-
-    def atoms(points, normals=None):
-        """Feasible atoms at these points; other fields copy slot 0."""
-        result = {key: value[:1].expand(len(points), *value.shape[1:]).clone()
-                  for key, value in state.params.items()}  # fmt: skip
-        result["centers"] = spec.project(points, result["centers"])
-        if normals is not None:
-            result["normals"] = normal_spec.project(normals, result["normals"])
-        return result
-
-    peaks = min(search.continuous.peaks * (1 + failures), 4 * search.continuous.peaks)
-    separation = search.continuous.separation
-    lower = centers.new_tensor(spec.lower).expand(3).clone()
-    upper = centers.new_tensor(spec.upper).expand(3).clone()
-    frozen = ~spec.mask(centers)
-    lower[frozen] = upper[frozen] = centers[0, frozen]
-
-    spacing = search.coarse_spacing / (1 + min(failures, 2))
-    while _points_per_box(lower, upper, spacing) > search.max_candidates:
-        spacing *= 1.1
-    points = candidate_grid(lower.tolist(), upper.tolist(), spacing)
-    if failures:
-        shift = points.new_tensor([0.37, 0.61, 0.23]) * spacing * ((failures % 3) + 1) / 3
-        points = spec.project(points + shift, points)
-    if failures < search.ungated_after:
-        keep = model.range_gate(
-            points, state.target[ids], relative_power=search.range_power / (1 + failures),
-            margin_cells=search.range_margin_cells * (1 + failures),
-            min_fraction=search.range_fraction,
-        )  # fmt: skip
-        if keep.any():  # an empty measurement gate never stops the search
-            points = points[keep]
-    cached = 0
-    if state.peak_cache is not None:
-        cached = min(len(state.peak_cache["centers"]), search.max_candidates - len(points))
-        points = torch.cat((points, state.peak_cache["centers"][:cached]))
-    candidates = atoms(points)
-    if cached:
-        normals = state.peak_cache["normals"][:cached]
-        candidates["normals"][-cached:] = normal_spec.project(normals, candidates["normals"][-cached:])
-
+    candidates = finder.coarse_candidates()
     with stage("propose.coarse"):
-        scores = score(candidates)
-        selected = select_peaks(scores, candidates["centers"], peaks, separation)
-        candidates = {key: value[selected] for key, value in candidates.items()}
+        scores = finder.score(candidates)
+        kept = select_peaks(scores, candidates["centers"], wanted, separation)
+        candidates = _take(candidates, kept)
     for radius, pitch in search.levels:
-        offset_lower = [-radius if active else 0 for active in ~frozen]
-        offset_upper = [radius if active else 0 for active in ~frozen]
-        while _points_per_box(offset_lower, offset_upper, pitch) > search.max_candidates:
-            pitch *= 1.1
-        offsets = candidate_grid(offset_lower, offset_upper, pitch)
-        # Highest-ranked regions keep priority within the per-level budget.
-        candidates = {key: value[: max(1, search.max_candidates // len(offsets))]
-                      for key, value in candidates.items()}  # fmt: skip
-        points = (candidates["centers"][:, None] + offsets[None]).reshape(-1, 3)
-        candidates = atoms(points, candidates["normals"].repeat_interleave(len(offsets), dim=0))
+        candidates = finder.level_candidates(candidates, radius, pitch)
         with stage("propose.level"):
-            scores = score(candidates)
-            selected = select_peaks(scores, candidates["centers"], peaks, min(separation, radius / 2))
-            candidates = {key: value[selected] for key, value in candidates.items()}
-    # FFT-interpolated scores only propose; the refinement rescores exactly.
-    initial = scores[selected] if table is None else None
+            scores = finder.score(candidates)
+            kept = select_peaks(scores, candidates["centers"], wanted, min(separation, radius / 2))
+            candidates = _take(candidates, kept)
+    # FFT-interpolated scores only propose; exact ones may seed the refinement
+    model, residual = finder.model, finder.sub_residual
+    initial = scores[kept] if finder.table is None else None
     if search.refine_apertures > search.proposal_apertures:
-        refine_ids, model = state.model.sample_apertures(
-            search.refine_apertures, config.seed + state.iteration + 1000003
-        )
-        r, initial = residual[refine_ids], None
+        refine_ids, model = state.model.sample_apertures(search.refine_apertures,
+                                                         config.seed + state.iteration + REFINE_SEED)  # fmt: skip
+        residual, initial = finder.residual[refine_ids], None
     with stage("propose.refine"):
         params, scores = search_certificate(
-            model, r, candidates, spec, replace(search.continuous, peaks=peaks, separation=0), mode,
-            normal_spec=refine_normals, initial_scores=initial,
-            full_model=state.model, full_residual=residual, batched=getattr(config, "batched", False),
-        )  # fmt: skip
+            model, residual, candidates, finder.spec, replace(ascent_config, peaks=wanted, separation=0),
+            finder.mode, normal_spec=finder.refine_normals, initial_scores=initial, full_model=state.model,
+            full_residual=finder.residual, batched=batched)  # fmt: skip
     if search.full_iterations:
-        full = select_peaks(scores, params["centers"], search.full_peaks, min(separation, spec.scale / 2))
+        finalists = select_peaks(scores, params["centers"], search.full_peaks, min(separation, finder.spec.scale / 2))
         with stage("propose.full"):
             refined, refined_scores = search_certificate(
-                state.model, residual, {key: value[full] for key, value in params.items()}, spec,
-                replace(search.continuous, peaks=search.full_peaks, iterations=search.full_iterations,
-                        separation=0),
-                mode, normal_spec=refine_normals, initial_scores=scores[full],
-                batched=getattr(config, "batched", False),
-            )  # fmt: skip
-        # The screened finalists stay in the pool beside the fully refined ones.
+                state.model, finder.residual, _take(params, finalists), finder.spec,
+                replace(ascent_config, peaks=search.full_peaks, iterations=search.full_iterations, separation=0),
+                finder.mode, normal_spec=finder.refine_normals, initial_scores=scores[finalists],
+                batched=batched)  # fmt: skip
+        # the screened finalists stay in the pool beside the fully refined ones
         scores = torch.cat((refined_scores, scores))
         order = scores.argsort(descending=True, stable=True)
         params = {key: torch.cat((value, params[key]))[order] for key, value in refined.items()}
