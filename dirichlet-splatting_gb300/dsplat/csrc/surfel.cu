@@ -8,6 +8,7 @@
 // bins, and its numerator class is fixed per pair. The 32 lanes first compute the
 // geometry of 32 (or 128) pairs in parallel into shared memory, then every quarter
 // sweeps its pairs' bins reading the geometry by broadcast.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <atomic>
@@ -1281,9 +1282,10 @@ int dsg_surfel_jacobian(const DsgChirp* chirp, const float* positions, int32_t a
 // library holds until the process exits.
 //
 // In host code the array's name is only a stand-in for the symbol; its device address
-// is looked up once per device with cudaGetSymbolAddress, with that device current, on
-// the first call made on that device. That first call may also load this module onto
-// the device, so it should come before any stream capture on that device.
+// is looked up with cudaGetSymbolAddress, with that device current, on the first call
+// made on that device (and again after the device's context changed, e.g. after a
+// cudaDeviceReset). That first call may also load this module onto the device, so it
+// should come before any stream capture on that device.
 //
 // Every call on a device shares the one array and leaves its partials there. Nothing in
 // it needs to start at zero: the partial kernel writes every (surfel, chunk) slot that
@@ -1295,26 +1297,67 @@ namespace {
 static __device__ __align__(256) float g_vjp_scratch[DSG_VJP_SCRATCH_MAX_BYTES / sizeof(float)];
 
 constexpr int kScratchDevices = 64;
-std::atomic<void*> g_vjp_scratch_address[kScratchDevices];
+
+// The scratch address is valid for one CUDA context: a cudaDeviceReset, or a caller that
+// makes another (non-primary) context current, loads the module anew. Each device slot
+// therefore remembers the unique id (cuCtxGetId) of the context it was looked up in, and
+// a call from any other context looks the address up again.
+struct ScratchSlot {
+  unsigned long long context_id = 0;
+  void* address = nullptr;
+};
+ScratchSlot g_vjp_scratch_slots[kScratchDevices];
 std::mutex g_vjp_scratch_mutex;
+
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrent g_ctx_get_current = nullptr;
+CtxGetId g_ctx_get_id = nullptr;
+std::once_flag g_ctx_entry_once;
+
+void resolve_context_entry_points() {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess && fn != nullptr)
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrent>(fn);
+  fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess && fn != nullptr)
+    g_ctx_get_id = reinterpret_cast<CtxGetId>(fn);
+  cudaGetLastError();
+}
+
+// Unique id of the calling thread's current context; 0 when none is current.
+unsigned long long current_context_id() {
+  std::call_once(g_ctx_entry_once, resolve_context_entry_points);
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  CUcontext context = nullptr;
+  if (g_ctx_get_current(&context) != CUDA_SUCCESS || context == nullptr) return 0;
+  unsigned long long id = 0;
+  if (g_ctx_get_id(context, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 int vjp_scratch_address(void** out) {
   int device = -1;
   if (cudaGetDevice(&device) != cudaSuccess) return DSG_ERR_LAUNCH;
   if (device < 0 || device >= kScratchDevices) return DSG_ERR_UNSUPPORTED;
-  void* address = g_vjp_scratch_address[device].load(std::memory_order_acquire);
-  if (address == nullptr) {
-    std::lock_guard<std::mutex> lock(g_vjp_scratch_mutex);
-    address = g_vjp_scratch_address[device].load(std::memory_order_acquire);
-    if (address == nullptr) {
-      const cudaError_t e = cudaGetSymbolAddress(&address, g_vjp_scratch);
-      if (e != cudaSuccess || address == nullptr) {
-        cudaGetLastError();
-        return DSG_ERR_LAUNCH;
-      }
-      g_vjp_scratch_address[device].store(address, std::memory_order_release);
-    }
+  std::lock_guard<std::mutex> lock(g_vjp_scratch_mutex);
+  ScratchSlot& slot = g_vjp_scratch_slots[device];
+  const unsigned long long id = current_context_id();
+  if (id != 0 && id == slot.context_id && slot.address != nullptr) {
+    *out = slot.address;
+    return DSG_OK;
   }
+  void* address = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&address, g_vjp_scratch);  // makes the primary context current
+  if (e != cudaSuccess || address == nullptr) {
+    cudaGetLastError();
+    return DSG_ERR_LAUNCH;
+  }
+  slot.context_id = current_context_id();  // 0 (look up again next time) if ids are unavailable
+  slot.address = address;
   *out = address;
   return DSG_OK;
 }

@@ -112,7 +112,9 @@ int dsg_surfel_vjp(const DsgChirp* chirp, const float* positions, int32_t apertu
  * dsg_surfel_reduce_workspace_bytes(chirp, apertures, surfels, 8) exceeds that bound
  * (with the 152-SM grid sizing that is above about 131k surfels). The first call on a
  * device looks up the scratch address there (and may load the module), so make it
- * before any stream capture on that device. Calls share the scratch: two calls whose
+ * before any stream capture on that device; the address is remembered per device and
+ * CUDA context, so a call after cudaDeviceReset, or from another context, looks it up
+ * again (and is again a first call). Calls share the scratch: two calls whose
  * kernels overlap on the GPU race and give wrong gradients; order them on one stream.
  * Allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine. */
 int dsg_surfel_vjp_fixed_scratch(const DsgChirp* chirp, const float* positions,
