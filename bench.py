@@ -318,7 +318,10 @@ def run_ours(args, world, rank, local):
         "fit_after_timed_steps": _fit_figures(after_value, truth),
         "fit_final": _fit_figures(state, truth),
         "steps_1_to_final": {"steps": len(fit_ms), "value": round(len(fit_ms) / (sum(fit_ms) / 1e3), 4),
-                             "ms_per_step": round(sum(fit_ms) / len(fit_ms), 3)},  # fmt: skip
+                             "ms_per_step": round(sum(fit_ms) / len(fit_ms), 3),
+                             "step_ms": [round(t, 1) for t in fit_ms],
+                             "replaced": [e.get("replaced") for e in state.history[1:]],
+                             "lm_accepted": [e.get("lm_accepted") for e in state.history[1:]]},  # fmt: skip
     }
     mixed_gram = work.get("dsg_gram_bf16x3")
     if mixed and not args.no_plain:
@@ -336,7 +339,8 @@ def run_ours(args, world, rank, local):
         within = all(g <= 0.05 for g in gaps.values())
         result["plain_fp32"] = {"value": round(plain_value, 4), "ms_per_step": round(plain_s * 1e3 / args.steps, 3),
                                 "steps_1_to_final": {"steps": len(plain_ms),
-                                                     "value": round(len(plain_ms) / (sum(plain_ms) / 1e3), 4)},
+                                                     "value": round(len(plain_ms) / (sum(plain_ms) / 1e3), 4),
+                                                     "step_ms": [round(t, 1) for t in plain_ms]},
                                 "fit_final": final}  # fmt: skip
         result["speedup_vs_plain_fp32"] = round(value / plain_value, 3)
         result["speedup_vs_plain_fp32_steps_1_to_final"] = round(

@@ -448,10 +448,12 @@ def migration(scan, points, aperture_shape, *, depth_samples=96, padding=2, freq
     kx = 2 * math.pi * torch.fft.fftshift(torch.fft.fftfreq(qu, d=dx, device=device, dtype=dtype))
     ky = 2 * math.pi * torch.fft.fftshift(torch.fft.fftfreq(qv, d=dy, device=device, dtype=dtype))
     focused = torch.empty((len(depths), qu, qv, 2), dtype=torch.float32, device=device)
-    _lib.call("dsg_migration_focus", _lib.ptr(torch.view_as_real(spectrum.contiguous()).contiguous()),
-              cfg.adc_samples, pu, pv, _lib.ptr(wavenumber.float().contiguous()), _lib.ptr(kx.float().contiguous()),
-              _lib.ptr(ky.float().contiguous()), qu, qv, _lib.ptr(depths.float().contiguous()), len(depths),
-              _lib.ptr(focused), _lib.stream(device))  # fmt: skip
+    # every buffer the kernel reads stays referenced here until the launch is queued
+    inputs = [torch.view_as_real(spectrum.contiguous()).contiguous(), wavenumber.float().contiguous(),
+              kx.float().contiguous(), ky.float().contiguous(), depths.float().contiguous()]  # fmt: skip
+    field_spectrum, k32, kx32, ky32, depth32 = inputs
+    _lib.call("dsg_migration_focus", _lib.ptr(field_spectrum), cfg.adc_samples, pu, pv, _lib.ptr(k32), _lib.ptr(kx32),
+              _lib.ptr(ky32), qu, qv, _lib.ptr(depth32), len(depths), _lib.ptr(focused), _lib.stream(device))  # fmt: skip
     # crop the points' footprint (two cells of margin) from each focused plane
     pitch = local.new_tensor([dx, dy])
     first = torch.floor(local[:, :2].amin(0) / pitch).long() - 2

@@ -57,13 +57,14 @@ def synthesize(aperture_positions, surfel_centers, surfel_normals, surfel_amplit
     from .kernels import _lib
 
     device = surfel_centers.device
-    as64 = dict(dtype=torch.float64)
-    positions = aperture_positions.to(device=device, **as64).contiguous()
+    # every buffer the kernel reads stays referenced here until the launch is queued
+    positions = aperture_positions.to(device=device, dtype=torch.float64).contiguous()
+    centers = surfel_centers.to(torch.float64).contiguous()
+    normals = surfel_normals.to(torch.float64).contiguous()
     amplitudes = torch.view_as_real(surfel_amplitudes.to(torch.complex128).reshape(-1).contiguous())
-    adc = torch.empty((len(positions), config.adc_samples, 2), device=device, **as64)
+    adc = torch.empty((len(positions), config.adc_samples, 2), device=device, dtype=torch.float64)
     _lib.call("dsg_synthesize_adc", _lib.chirp(config, fresnel_n), float(config.sample_rate_hz), _lib.ptr(positions),
-              len(positions), _lib.ptr(surfel_centers.to(**as64).contiguous()),
-              _lib.ptr(surfel_normals.to(**as64).contiguous()), _lib.ptr(amplitudes), len(surfel_centers),
+              len(positions), _lib.ptr(centers), _lib.ptr(normals), _lib.ptr(amplitudes), len(centers),
               _lib.ptr(adc), _lib.stream(device))  # fmt: skip
     bins = torch.fft.fft(torch.view_as_complex(adc), n=config.n_fft)[:, : config.num_range_bins]
     return Scan((bins / config.adc_samples).to(torch.complex64), aperture_positions, config)
