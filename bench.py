@@ -161,6 +161,42 @@ def median_distance(params, truth, radius=0.03, depth=0.35):
     return float(((c - center).norm(dim=1) - radius).abs().median())
 
 
+def run_accuracy(args):
+    """Final NMSE and centre-to-surface distance of both arms over several scenes.
+
+    One fit is a chaotic sequence of discrete decisions (which candidates enter, which
+    slides pass), so two arithmetics that agree to rounding still reach different final
+    states. This mode runs the 100-step fit of the plain FP32 arm and of the mixed+batched
+    arm on args.accuracy seeded scenes (sphere cap and start drawn from the seed) and
+    reports each pair and the means, to compare the arms' spread with their difference.
+    """
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from dsplat import DSFWConfig, SpatialSearchConfig, initialize, step
+
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    search = SpatialSearchConfig()
+    arms = {"plain_fp32": DSFWConfig(iterations=args.iterations, batch=256),
+            "mixed_batched": DSFWConfig(iterations=args.iterations, batch=256, gram="bf16x3", batched=True)}
+    runs = []
+    for seed in range(args.accuracy):
+        model, target, start, parameters, truth = build_problem(device, seed=seed)
+        record = {"seed": seed}
+        for name, config in arms.items():
+            state = initialize(model, target, start, config, parameters=parameters)
+            for _ in range(config.iterations):
+                state = step(state, config, search)
+            record[name] = _fit_figures(state, truth)
+        runs.append(record)
+        print(json.dumps(record), flush=True)
+    means = {name: {key: statistics.fmean(r[name][key] for r in runs)
+                    for key in ("nmse", "median_center_to_surface_m")} for name in arms}  # fmt: skip
+    gaps = {key: _gap(means["mixed_batched"][key], means["plain_fp32"][key]) for key in means["plain_fp32"]}
+    print(json.dumps({"accuracy": runs, "means": means, "relative_gap_of_means": gaps}), flush=True)
+
+
 def _timed_steps(state, config, search, count, flush, device):
     """Run count steps, each timed with CUDA events on the launching stream after an L2 flush."""
     from dsplat import step
@@ -581,6 +617,9 @@ def run_kernels(args):
     record("dsg_surfel_jvp", ms, A * S * K, 24)
     ms = _event_time(lambda: kernel.vjp(config, positions, centers, normals, weights, upstream, 0.0), it, wu, flush)
     record("dsg_surfel_vjp", ms, A * S * K, 20)
+    if args.only == "splat":  # the three splat kernels alone (the ncu captures of render / JVP / VJP)
+        print(json.dumps({"case": args.case, "apertures": A, "surfels": S, "bins": K, "kernels": rows}), flush=True)
+        return
     sub = positions[: min(A, 768)].contiguous()
     cand = centers.repeat(max(1, 8192 // S), 1)[:8192].contiguous()
     cand_n = normals.repeat(max(1, 8192 // S), 1)[:8192].contiguous()
@@ -672,9 +711,14 @@ def main():
     parser.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison run")
     parser.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead")
     parser.add_argument("--case", choices=["small", "medium", "full"], default="full")
+    parser.add_argument("--only", choices=["all", "splat"], default="all", help="with --kernels: which kernels")
+    parser.add_argument("--accuracy", type=int, default=0, help="final-accuracy study of both arms on N seeds")
     args = parser.parse_args()
     if args.kernels:
         run_kernels(args)
+        return
+    if args.accuracy:
+        run_accuracy(args)
         return
     world, rank, local = _distributed()
     if args.impl == "reference":
