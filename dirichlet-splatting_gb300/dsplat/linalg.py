@@ -117,14 +117,18 @@ def solve(h, rhs, refined=False):
     return x if rhs.ndim == 2 else x[:, 0]
 
 
-def pcg(operator, rhs, diagonal, *, iterations=32, tolerance=1e-3):
+def pcg(operator, rhs, diagonal, *, iterations=32, tolerance=1e-3, capture=False):
     """Jacobi-preconditioned conjugate gradients from zero.
 
     Stops (keeps x) at the first direction of nonpositive curvature, or after the update
     that brings |r| to tolerance * |rhs| or below. The stop is a device flag: iterations
-    after it change nothing, and the host looks at the flag every PCG_CHECK_EVERY
-    iterations to skip the rest, so the loop issues no per-iteration device read.
+    after it change nothing. Eagerly the host looks at the flag every PCG_CHECK_EVERY
+    iterations to skip the rest; with capture (CUDA tensors, and an operator that reads
+    no device value) the first iteration runs eagerly and the others replay it from a
+    CUDA graph, all iterations, with no device read at all.
     """
+    if capture and rhs.is_cuda and iterations > 1:
+        return _pcg_graphed(operator, rhs, diagonal, iterations, tolerance)
     x = torch.zeros_like(rhs)
     goal = tolerance * rhs.norm()
     r = rhs.clone()
@@ -148,3 +152,54 @@ def pcg(operator, rhs, diagonal, *, iterations=32, tolerance=1e-3):
         rz = torch.where(going, rz_next, rz)
         live = going
     return x
+
+
+def _pcg_graphed(operator, rhs, diagonal, iterations, tolerance):
+    """pcg with every iteration after the first replayed from one captured CUDA graph.
+
+    The iterates live in static buffers that one iteration updates in place; the graph is
+    captured per call (the operator's tensors belong to one Gauss-Newton system).
+    """
+    from .kernels import _lib
+
+    goal = tolerance * rhs.norm()
+    x = torch.zeros_like(rhs)
+    r = rhs.clone()
+    p = r / diagonal
+    rz = (r @ p).reshape(())
+    live = torch.ones((), dtype=torch.bool, device=rhs.device)
+
+    def iteration():
+        hp = operator(p)
+        curvature = p @ hp
+        moving = live & (curvature > 0)
+        alpha = rz / curvature
+        x.copy_(torch.where(moving, x + alpha * p, x))
+        r_next = torch.where(moving, r - alpha * hp, r)
+        going = moving & (r_next.norm() > goal)
+        z = r_next / diagonal
+        rz_next = r_next @ z
+        p.copy_(torch.where(going, z + (rz_next / rz) * p, p))
+        rz.copy_(torch.where(going, rz_next, rz))
+        r.copy_(r_next)
+        live.copy_(going)
+
+    device = rhs.device
+    side = torch.cuda.Stream(device)
+    side.wait_stream(torch.cuda.current_stream(device))
+    timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be recorded inside a capture
+    try:
+        with torch.cuda.stream(side):
+            iteration()  # the first iteration, which is also the capture's warm-up
+        torch.cuda.current_stream(device).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        before = _lib.library().dsg_launch_count()
+        with torch.cuda.graph(graph):
+            iteration()
+        per_replay = _lib.library().dsg_launch_count() - before
+        for _ in range(iterations - 1):
+            graph.replay()
+        _lib.REPLAYED_LAUNCHES += per_replay * (iterations - 1)
+    finally:
+        _lib.TIMERS = timers
+    return x.clone()

@@ -57,6 +57,17 @@ class ParameterConfig:
         """Boolean [components] mask of the free components of a row of value."""
         return _constant("free", self.trainable, value, value.shape[1] if value.ndim == 2 else 1)
 
+    def free_index(self, value):
+        """Long [free components] indices of the free components (gathers without a device read)."""
+        width = value.shape[1] if value.ndim == 2 else 1
+        flags = self.trainable if isinstance(self.trainable, (tuple, list)) else (self.trainable,) * width
+        key = ("index", tuple(bool(f) for f in flags), value.device, width)
+        found = _CONSTANTS.get(key)
+        if found is None:
+            found = torch.tensor([i for i in range(width) if flags[i]], dtype=torch.long, device=value.device)
+            _CONSTANTS[key] = found
+        return found
+
     def project(self, proposed, reference):
         """The feasible point nearest proposed; frozen components come from reference."""
         x, restore = _rows(proposed)

@@ -146,10 +146,10 @@ class _JointLayout:
         self.params, self.specs, self.b = params, specs, b
         self.complex = complex_mode
         self.count = len(b)
-        self.sections = []  # (key, free mask, slice)
+        self.sections = []  # (key, free component indices, slice)
         start = 0
         for key, spec in trainable(params, specs):
-            free = spec.mask(params[key])
+            free = spec.free_index(params[key])
             stop = start + self.count * _free_width(spec, params[key])
             self.sections.append((key, free, slice(start, stop)))
             start = stop
@@ -169,7 +169,7 @@ class _JointLayout:
         for key, free, section in self.sections:
             spec = self.specs[key]
             target = _as_matrix(tangent[key])
-            target[:, free] = vector[section].reshape(self.count, -1) * spec.scale
+            target.index_copy_(1, free, vector[section].reshape(self.count, -1) * spec.scale)
             tangent[key] = spec.tangent(tangent[key], self.params[key])
         tail = vector[self.geometry :]
         if self.complex:
@@ -182,7 +182,7 @@ class _JointLayout:
         for key, free, section in self.sections:
             spec = self.specs[key]
             along = _as_matrix(spec.tangent(grads[key], self.params[key]))
-            out[section] = (along[:, free] * spec.scale).reshape(-1)
+            out[section] = (along.index_select(1, free) * spec.scale).reshape(-1)
         out[self.geometry :] = self.coefficient_entries(coefficient * self.coefficient_scale)
         return out
 
@@ -190,7 +190,7 @@ class _JointLayout:
         """Per-atom length of a geometry tangent in units of each field's scale."""
         total = self.amplitude.new_zeros(self.count)
         for key, free, _ in self.sections:
-            total += (_as_matrix(tangent[key])[:, free] / self.specs[key].scale).square().sum(1)
+            total += (_as_matrix(tangent[key]).index_select(1, free) / self.specs[key].scale).square().sum(1)
         return total.sqrt()
 
 
@@ -259,7 +259,8 @@ def joint_slide(state, config, screen=None):
                 model, state.params, state.coefficients, target, state.parameters, config,
                 config.seed + state.iteration + inner)  # fmt: skip
         with stage("slide.pcg"):
-            delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations, tolerance=config.cg_tolerance)
+            delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations, tolerance=config.cg_tolerance,
+                        capture=getattr(config, "batched", False))  # fmt: skip
         descent = torch.isfinite(delta).all() & (delta @ gradient < 0)
         if not bool(descent):
             break

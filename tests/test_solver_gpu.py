@@ -171,6 +171,24 @@ def test_joint_system_is_symmetric_and_pcg_matches_a_dense_solve(spectral):
     close(solution, torch.linalg.solve(dense, -gradient.double()), 1e-3)
 
 
+@pytest.mark.parametrize("iterations,tolerance", [(16, 1e-3), (40, 1e-9)])
+def test_graph_replayed_pcg_matches_the_eager_loop(fmcw, iterations, tolerance):
+    """The batched slide's PCG (first iteration eager, the rest replayed from a captured CUDA
+    graph with the stop rule as a device flag) against the eager loop on the same FMCW
+    joint system: same iterates up to rounding, also when the stop rule fires early."""
+    from dsplat import DSFWConfig
+    from dsplat.refinement import joint_system
+    from dsplat.varpro import pcg
+
+    model, params, b = fmcw
+    trial = {**params, "centers": params["centers"] + 2e-4}
+    matvec, gradient, diagonal, _ = joint_system(model, trial, b, model.scan.data, fmcw_specs(), DSFWConfig(), 0)
+    eager = pcg(matvec, -gradient, diagonal, iterations=iterations, tolerance=tolerance)
+    replayed = pcg(matvec, -gradient, diagonal, iterations=iterations, tolerance=tolerance, capture=True)
+    assert bool(torch.isfinite(replayed).all())
+    close(replayed, eager, 1e-4)
+
+
 def test_fmcw_joint_system_is_symmetric(fmcw):
     from dsplat import DSFWConfig
     from dsplat.refinement import joint_system
