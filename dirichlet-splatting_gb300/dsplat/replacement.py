@@ -28,7 +28,7 @@ from .linalg import shifted_cholesky
 from .normal import TensorCoreGram, fused_rows, row_chunk
 from .parameters import periodic_delta
 from .tracing import stage
-from .varpro import Fit, accept, fit_coefficients, rendered_loss, screen_bar, varpro
+from .varpro import Fit, accept, refined_coefficients, rendered_loss, screen_bar, varpro
 
 
 def _feasible(state, pool, owner):
@@ -306,7 +306,7 @@ class _PooledFit:
                 return atoms, varpro(state.model, atoms, state.target, self.config)
         gram = self.gram[slots[:, None], slots[None, :]]
         rhs = self.rhs[slots]
-        coefficients = fit_coefficients(gram, rhs, self.config)
+        coefficients = refined_coefficients(state.model, atoms, state.target, gram, rhs, self.config)
         prediction, objective = rendered_loss(state.model, atoms, coefficients, state.target, self.config.ridge)
         return atoms, Fit(coefficients, prediction, objective, gram, rhs)
 
