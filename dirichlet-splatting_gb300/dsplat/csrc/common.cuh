@@ -25,6 +25,8 @@
 
 // Host-side count of kernel launches made by the library (defined in misc.cu).
 void dsg_count_launches(int kernels);
+// Launch-shape knob (DSG_TUNE_*) set through dsg_tuning_set; 0 means automatic.
+int dsg_tuning_value(int knob);
 
 namespace dsg {
 

@@ -70,6 +70,7 @@ __global__ void range_response_kernel(double low, double high, int count, int bi
 
 std::mutex g_mutex;
 std::atomic<unsigned long long> g_launches{0};
+std::atomic<int> g_tuning[DSG_TUNE_COUNT] = {};
 cublasHandle_t g_handles[64] = {};
 
 }  // namespace
@@ -77,9 +78,24 @@ cublasHandle_t g_handles[64] = {};
 // Every launch site of the library adds its kernel count here (host side).
 void dsg_count_launches(int kernels) { g_launches.fetch_add((unsigned long long)kernels); }
 
+// Launch-shape knob for the launchers of this library; 0 means "choose automatically".
+int dsg_tuning_value(int knob) { return knob >= 0 && knob < DSG_TUNE_COUNT ? g_tuning[knob].load() : 0; }
+
 extern "C" {
 
 uint64_t dsg_launch_count(void) { return g_launches.load(); }
+
+int dsg_tuning_set(int32_t knob, int32_t value) {
+  if (knob < 0 || knob >= DSG_TUNE_COUNT || value < 0) return DSG_ERR_ARGUMENT;
+  static const int kMax[DSG_TUNE_COUNT] = {32, 8, 8};
+  if (value > kMax[knob]) return DSG_ERR_ARGUMENT;
+  g_tuning[knob].store(value);
+  return DSG_OK;
+}
+
+int32_t dsg_tuning_get(int32_t knob) {
+  return knob >= 0 && knob < DSG_TUNE_COUNT ? g_tuning[knob].load() : -1;
+}
 
 const char* dsg_version(void) { return "dsplat-gb300 0.1.0 (sm_103a)"; }
 

@@ -416,8 +416,10 @@ template <int P>
 int launch_project(const Consts& c, const CUtensorMap& mh, const CUtensorMap& ml, const float* pos,
                    int A, const float* cen, const float* nrm, const float* areas, int S, int rank2,
                    void* hi, void* lo, int64_t ld, int64_t col0, int* status, cudaStream_t st) {
-  const int stages = plan_stages(c.K, c.N, P, rank2);
-  if (stages == 0) return DSG_ERR_UNSUPPORTED;
+  const int deepest = plan_stages(c.K, c.N, P, rank2);
+  if (deepest == 0) return DSG_ERR_UNSUPPORTED;
+  const int tuned = dsg_tuning_value(DSG_TUNE_PROJECT_STAGES);
+  const int stages = tuned >= 2 && tuned < deepest ? tuned : deepest;
   const size_t smem = (size_t)make_plan(c.K, c.N, P, rank2, stages).total;
   auto kern = design_project_kernel<P>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

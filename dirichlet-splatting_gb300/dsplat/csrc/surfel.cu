@@ -765,7 +765,7 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* rec = smem + ((tbl_n + 3) & ~3) + warp * 32 * kOrientRec;
-  const int s = blockIdx.x * kOrientWarps + warp;
+  const int s = blockIdx.x * (int)(blockDim.x >> 5) + warp;  // blockDim: 1..kOrientWarps warps
   if (s >= C) return;  // warp-uniform; no block barrier follows
   const float cx = __ldg(cen + 3 * s), cy = __ldg(cen + 3 * s + 1), cz = __ldg(cen + 3 * s + 2);
   const float own[3] = {__ldg(nrm + 3 * s), __ldg(nrm + 3 * s + 1), __ldg(nrm + 3 * s + 2)};
@@ -874,7 +874,11 @@ using namespace dsg;
 
 namespace {
 
-constexpr int kTargetCtas = 152 * 6;
+// CTAs the segment / chunk splits aim for: 152 SMs x (DSG_TUNE_SPLAT_CTAS_PER_SM, default 6).
+int target_ctas() {
+  const int per_sm = dsg_tuning_value(DSG_TUNE_SPLAT_CTAS_PER_SM);
+  return 152 * (per_sm > 0 ? per_sm : 6);
+}
 
 bool chirp_ok(const DsgChirp* c) {
   if (!c) return false;
@@ -887,7 +891,7 @@ bool chirp_ok(const DsgChirp* c) {
 
 int render_segments(const DsgChirp* c, int A, int S) {
   const int tiles = (A + 15) / 16;
-  int seg = (kTargetCtas + tiles - 1) / tiles;
+  int seg = (target_ctas() + tiles - 1) / tiles;
   const int max_seg = (S + 31) / 32;
   if (seg > max_seg) seg = max_seg;
   if (seg < 1) seg = 1;
@@ -897,7 +901,7 @@ int render_segments(const DsgChirp* c, int A, int S) {
 
 int reduce_chunks(int A, int S) {
   const int tiles = (S + 15) / 16;
-  int ch = (kTargetCtas + tiles - 1) / tiles;
+  int ch = (target_ctas() + tiles - 1) / tiles;
   const int max_ch = (A + 7) / 8;
   if (ch > max_ch) ch = max_ch;
   if (ch < 1) ch = 1;
@@ -1047,14 +1051,16 @@ struct OrientLaunch {
   cudaStream_t st;
   template <int P>
   int run() {
-    const size_t smem = (((c.N + c.K + 3) & ~3) + kOrientWarps * 32 * kOrientRec) * sizeof(float);
-    const dim3 grid((C + kOrientWarps - 1) / kOrientWarps);
+    const int tuned = dsg_tuning_value(DSG_TUNE_ORIENT_WARPS);
+    const int warps = tuned > 0 && tuned <= kOrientWarps ? tuned : kOrientWarps;
+    const size_t smem = (((c.N + c.K + 3) & ~3) + warps * 32 * kOrientRec) * sizeof(float);
+    const dim3 grid((C + warps - 1) / warps);
     if (c.fresnel_n > 1.0f)
-      orientations_kernel<P, true><<<grid, kOrientWarps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
-                                                                          res, table, ntab, ov, out);
+      orientations_kernel<P, true><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res, table,
+                                                                   ntab, ov, out);
     else
-      orientations_kernel<P, false><<<grid, kOrientWarps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb,
-                                                                           res, table, ntab, ov, out);
+      orientations_kernel<P, false><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res, table,
+                                                                    ntab, ov, out);
     dsg_count_launches(1);
     return launch_status();
   }

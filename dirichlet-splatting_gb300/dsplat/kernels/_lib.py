@@ -72,6 +72,8 @@ SIGNATURES = {
     "dsg_version": (ctypes.c_char_p, []),
     "dsg_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "dsg_launch_count": (ctypes.c_uint64, []),
+    "dsg_tuning_set": (ctypes.c_int, [I32, I32]),
+    "dsg_tuning_get": (I32, [I32]),
     "dsg_surfel_render_workspace_bytes": (SZ, [CP, I32, I32]),
     "dsg_surfel_render": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, SZ, P]),
     "dsg_surfel_jvp": (ctypes.c_int, [CP, P, I32, P, P, P, P, P, P, I32, P, P, SZ, P]),

@@ -70,10 +70,12 @@ class GramRows:
         )  # fmt: skip
         self.rows += m
 
-    def accumulate(self, total, column_from=0):
+    def accumulate(self, total, column_from=0, splits=None):
         """total [S, S] float64 += upper tiles of the stored rows' Gram (unused tail is zeroed).
 
-        column_from > 0 computes only the tiles that hold columns >= column_from.
+        column_from > 0 computes only the tiles that hold columns >= column_from. splits
+        overrides the K-split count (default: the autotuner's value for this shape, else
+        k_splits).
         """
         if self.rows < self.k_pad:
             self.hi[:, self.rows :].zero_()
@@ -89,10 +91,14 @@ class GramRows:
         # logical FP32 flops of the needed symmetric block (a SYRK count)
         added = self.columns - int(column_from)
         _lib.add_work("dsg_gram_bf16x3", float(self.rows) * added * (2 * int(column_from) + added + 1))
+        if splits is None:
+            from .. import autotune
+
+            automatic = k_splits(self.n_pad, k_pad, column_from)
+            splits = autotune.gram_splits(automatic, autotune.gram_key(self.n_pad, k_pad, column_from, total.device))
         call(
             "dsg_gram_bf16x3", ptr(hi), ptr(lo), self.columns, self.n_pad, k_pad, int(column_from),
-            k_splits(self.n_pad, k_pad, column_from), ptr(total), total.shape[1], ptr(status),
-            _lib.stream(total.device),
+            int(splits), ptr(total), total.shape[1], ptr(status), _lib.stream(total.device),
         )  # fmt: skip
         return status
 
@@ -134,6 +140,10 @@ def append_projected(store, config, positions, params, basis, fresnel_n, status)
     centers = params["centers"].to(torch.float32).contiguous()
     normals = params["normals"].to(torch.float32).contiguous()
     areas = params["areas"].to(torch.float32).contiguous()
+    from .. import autotune
+
+    autotune.apply("project", surfels=len(params["centers"]), bins=config.num_range_bins, pad=config.pad_factor,
+                   rank2=rank2, device=positions.device)  # fmt: skip
     # logical FP32 flops of the projection U [rank2, 2K] . v over every aperture-surfel pair
     lib.add_work("dsg_design_project_bf16x3",
                  float(len(positions)) * len(centers) * 2 * (2 * config.num_range_bins) * rank2)  # fmt: skip

@@ -29,6 +29,14 @@ def _work(name, units):
     _lib.add_work(name, float(units) * FLOPS_PER_UNIT[name])
 
 
+def _tuned(family, config, apertures, surfels, device):
+    """Set the library's launch-shape knob of family for this shape (dsplat.autotune)."""
+    from .. import autotune
+
+    autotune.apply(family, apertures=apertures, surfels=surfels, bins=config.num_range_bins, pad=config.pad_factor,
+                   device=device)  # fmt: skip
+
+
 def _outputs(centers, *shape, dtype=torch.float32):
     return torch.empty(shape, dtype=dtype, device=centers.device)
 
@@ -39,6 +47,7 @@ def _profiles(config, positions, centers, normals, weights, fresnel_n):
     weights = weights.contiguous()
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
+    _tuned("splat", config, apertures, count, centers.device)
     out = _outputs(centers, apertures, config.num_range_bins, 2)
     nbytes = _lib.query("dsg_surfel_render_workspace_bytes", chirp, apertures, count)
     work, nbytes = _lib.workspace(nbytes, centers.device)
@@ -56,6 +65,7 @@ def vjp(config, positions, centers, normals, weights, upstream, fresnel_n):
     w, u = real_view(weights), real_view(upstream)
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
+    _tuned("splat", config, apertures, count, centers.device)
     gc, gn, gw = (_outputs(centers, count, 3), _outputs(centers, count, 3),
                   _outputs(centers, count, 2))  # fmt: skip
     nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 8)
@@ -77,6 +87,7 @@ def jvp(config, positions, centers, normals, weights, delta_centers, delta_norma
     w, dw = real_view(weights), real_view(delta_weights)
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
+    _tuned("splat", config, apertures, count, centers.device)
     out = _outputs(centers, apertures, config.num_range_bins, 2)
     nbytes = _lib.query("dsg_surfel_render_workspace_bytes", chirp, apertures, count)
     work, nbytes = _lib.workspace(nbytes, centers.device)
@@ -160,6 +171,7 @@ def correlate(config, positions, centers, normals, residual, fresnel_n, active=N
     r = real_view(residual)
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
+    _tuned("splat", config, apertures, count, centers.device)
     corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
     nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3)
     work, nbytes = _lib.workspace(nbytes, centers.device)
@@ -190,6 +202,7 @@ def correlate_orientations(config, positions, centers, normals, bank, residual, 
     positions, centers, normals, bank = f32(positions), f32(centers), f32(normals), f32(bank)
     chirp = _lib.chirp(config, fresnel_n)
     count = len(centers)
+    _tuned("orient", config, len(positions), 0, centers.device)
     out = _outputs(centers, count, len(bank) + 1, 3)
     if table is None:
         r, rt, nt, oversample = real_view(residual), None, None, 1
@@ -212,6 +225,7 @@ def correlate_gradient(config, positions, centers, normals, residual, fresnel_n,
     width = 6 if include_normals else 3
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
+    _tuned("splat", config, apertures, count, centers.device)
     corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
     dcorr, dnorm = _outputs(centers, count, width, 2), _outputs(centers, count, width)
     nbytes = _lib.query(

@@ -66,6 +66,25 @@ const char* dsg_error_string(int code);
 /* Kernels launched by this library since it was loaded (a host-side counter). */
 uint64_t dsg_launch_count(void);
 
+/* Launch-shape knobs, set by the autotuner (dsplat/autotune.py); no counterpart in the
+ * reference, whose kernels have fixed Slang tile constants (dsplat/kernels/__init__.py:17-21,
+ * kernels/surfel.py:42-55: PAD and TILE). 0 restores the automatic choice.
+ *   DSG_TUNE_SPLAT_CTAS_PER_SM  splat render / JVP / correlation reductions: target CTAs per
+ *                               SM when splitting surfels into segments or apertures into
+ *                               chunks (automatic: 6; 1..32)
+ *   DSG_TUNE_PROJECT_STAGES     dsg_design_project_bf16x3 pipeline stages (automatic: the
+ *                               deepest ring that fits shared memory; 2..4, capped at that)
+ *   DSG_TUNE_ORIENT_WARPS       dsg_surfel_correlate_orientations warps per CTA (automatic:
+ *                               8; 1..8)
+ * Knobs are process-wide; set them between launches, not while another thread launches. */
+#define DSG_TUNE_SPLAT_CTAS_PER_SM 0
+#define DSG_TUNE_PROJECT_STAGES 1
+#define DSG_TUNE_ORIENT_WARPS 2
+#define DSG_TUNE_COUNT 3
+int dsg_tuning_set(int32_t knob, int32_t value);
+/* Current value of a knob (0: automatic), or -1 for an unknown knob. */
+int32_t dsg_tuning_get(int32_t knob);
+
 /* ---- FMCW surfels: range profiles and derivatives ------------------------------- */
 
 /* Workspace of dsg_surfel_render / dsg_surfel_jvp (segment partials), in bytes. */

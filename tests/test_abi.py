@@ -121,6 +121,7 @@ def _prototypes():
     """{name: (return type, [parameter declarations])} of every entry point in the header."""
     text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
     text = re.sub(r"typedef struct\s*\{.*?\}\s*\w+\s*;", "", text, flags=re.S)
+    text = re.sub(r"^\s*#.*$", "", text, flags=re.M)  # preprocessor lines (knob constants)
     found = {}
     for match in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(dsg_\w+)\s*\(([^)]*)\)\s*;", text):
         params = [p.strip() for p in match.group(3).split(",") if p.strip() and p.strip() != "void"]
@@ -154,6 +155,7 @@ def test_bindings_match_the_header_prototypes():
                 assert kind is ctypes.c_int32, (name, position, declaration)
         expected = {"int": ctypes.c_int, "size_t": ctypes.c_size_t, "const char*": ctypes.c_char_p,
                     "const char *": ctypes.c_char_p, "int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64,
+                    "int32_t": ctypes.c_int32,
                     "void": None}  # fmt: skip
         assert ret in expected, (name, ret)
         assert restype is expected[ret], (name, ret, restype)
