@@ -263,6 +263,15 @@ def run_ours(args, world, rank, local):
     state = initialize(model, target, start, config, parameters=parameters)
     torch.cuda.synchronize(device)
     init_s = time.perf_counter() - init_begin
+    tuned = None
+    if not args.no_autotune:
+        # launch shapes from the autotuner, chosen on this workload's shapes (untimed)
+        from dsplat import autotune
+
+        chirp, positions = state.model.sensor
+        basis = state.model.block_basis(slice(0, min(2048, len(positions)) * chirp.num_range_bins))
+        chosen = autotune.tune_workload(chirp, positions, state.params, state.target - state.prediction, basis)
+        tuned = {family: value for family, (value, _) in chosen.items()}
     state, warm_ms = _timed_steps(state, config, search, args.warmup, flush, device)
     saved = state  # DSFWState is immutable: steps build new states and never write tensors in place
 
@@ -348,6 +357,7 @@ def run_ours(args, world, rank, local):
         "tensor_roofline": None if roofline and roofline["bound"] == "tensor" else _tensor_roofline(totals, timers, work),
         "kernel_ms": {k: round(v, 3) for k, v in sorted(totals.items(), key=lambda kv: -kv[1])},
         "stage_ms": stages,
+        "autotuned_launch_shapes": tuned,
         "timing": {"value_steps": f"{args.warmup + 1}..{args.warmup + args.steps}", "instrumented": False,
                    "kernel_ms_from": "a separate instrumented pass over the same steps",
                    "initialize_s": round(init_s, 3)},  # fmt: skip
@@ -713,6 +723,7 @@ def main():
     parser.add_argument("--case", choices=["small", "medium", "full"], default="full")
     parser.add_argument("--only", choices=["all", "splat"], default="all", help="with --kernels: which kernels")
     parser.add_argument("--accuracy", type=int, default=0, help="final-accuracy study of both arms on N seeds")
+    parser.add_argument("--no-autotune", action="store_true", help="keep every launch shape automatic")
     args = parser.parse_args()
     if args.kernels:
         run_kernels(args)
