@@ -379,10 +379,10 @@ def run_ours(args, world, rank, local):
         plain_value = world * args.steps / plain_s
         final = _fit_figures(other, truth)
         mine = result["fit_final"]
-        gaps = {"nmse": _gap(mine["nmse"], final["nmse"]),
-                "median_center_to_surface_m": _gap(mine["median_center_to_surface_m"],
-                                                   final["median_center_to_surface_m"])}  # fmt: skip
-        within = all(g <= 0.05 for g in gaps.values())
+        keys = ("nmse", "median_center_to_surface_m")
+        # signed: (mixed - plain) / plain; a negative gap is a better mixed fit
+        gaps = {key: (mine[key] - final[key]) / max(abs(final[key]), 1e-300) for key in keys}
+        within = all(gap <= 0.05 for gap in gaps.values())
         result["plain_fp32"] = {"value": round(plain_value, 4), "ms_per_step": round(plain_s * 1e3 / args.steps, 3),
                                 "steps_1_to_final": {"steps": len(plain_ms),
                                                      "value": round(len(plain_ms) / (sum(plain_ms) / 1e3), 4),
@@ -391,9 +391,10 @@ def run_ours(args, world, rank, local):
         result["speedup_vs_plain_fp32"] = round(value / plain_value, 3)
         result["speedup_vs_plain_fp32_steps_1_to_final"] = round(
             result["steps_1_to_final"]["value"] / result["plain_fp32"]["steps_1_to_final"]["value"], 3)
-        result["accuracy_vs_plain"] = {"relative_gap": {k: round(v, 4) for k, v in gaps.items()},
-                                       "within_5pct": bool(within),
-                                       "meets_metric": bool(within)}  # fmt: skip
+        result["accuracy_vs_plain"] = {"signed_relative_gap": {k: round(v, 4) for k, v in gaps.items()},
+                                       "not_worse_than_plain_by_5pct": bool(within),
+                                       "meets_metric": bool(within),
+                                       "note": "one seed; the fit is chaotic, see --accuracy for the seed study"}  # fmt: skip
     if mixed_gram:
         from dsplat.varpro import projected_rows, row_chunk
 

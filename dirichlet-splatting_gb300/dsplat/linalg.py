@@ -95,6 +95,41 @@ def shifted_refined_solve(h, q, floor):
     return refined_solve(base, q)
 
 
+def factored_solver(h, refined=False):
+    """solve(h, .) as a function of the right-hand side, with h factored once.
+
+    The first call decides the factorization exactly as solve does (float32 / float64
+    Cholesky, the shifted refined solve, or the shifted float64 factor); later calls reuse
+    it, so a refinement loop costs one factorization.
+    """
+    factor, status = torch.linalg.cholesky_ex(h)
+    if int(status) == 0:
+        return lambda rhs: _apply_factor(factor, rhs)
+    floor = len(h) * torch.finfo(h.real.dtype).eps
+    if refined and h.is_cuda:
+        shifted = _wide(h)
+        shifted.diagonal().add_(floor * largest_eigenvalue(shifted))
+
+        def refined_call(rhs):
+            q = rhs if rhs.ndim == 2 else rhs[:, None]
+            x = refined_solve(shifted, q)
+            if x is None:
+                return solve(h, rhs, refined=False)
+            return (x if rhs.ndim == 2 else x[:, 0]).to(rhs.dtype)
+
+        return refined_call
+    wide_factor = shifted_cholesky(h, floor)
+    if wide_factor is None:
+        return torch.zeros_like
+    return lambda rhs: _apply_factor(wide_factor, rhs)
+
+
+def _apply_factor(factor, rhs):
+    q = rhs if rhs.ndim == 2 else rhs[:, None]
+    x = torch.cholesky_solve(q.to(factor.dtype), factor).to(q.dtype)
+    return x if rhs.ndim == 2 else x[:, 0]
+
+
 def solve(h, rhs, refined=False):
     """Hermitian solve; a singular h is shifted to where a pseudoinverse would truncate.
 

@@ -20,6 +20,7 @@ from .kernels.reduce import energy
 from .linalg import (  # noqa: F401  (names of the reference's varpro module)
     POWER_STEPS,
     SHIFT_RETRIES,
+    factored_solver,
     largest_eigenvalue,
     pcg,
     refined_solve,
@@ -73,15 +74,20 @@ def refined_coefficients(model, params, target, gram, rhs, config):
     iterative refinement with the approximate Gram as the preconditioner, converging to
     the coefficients of the exact least-squares problem.
     """
-    b = fit_coefficients(gram, rhs, config)
     if not _refines(config):
-        return b
+        return fit_coefficients(gram, rhs, config)
+    h, q = gram.real, rhs.real
+    if config.ridge:
+        h = h.clone()
+        h.diagonal().add_(config.ridge)
+    solve_with = factored_solver(h, refined=getattr(config, "batched", False))
+    b = solve_with(q)
     for _ in range(RESIDUAL_REFINEMENTS):
         residual = target - model.render(params, b)
         g = model.correlate(params, residual)[0].real / model.size
         if config.ridge:
             g = g - config.ridge * b
-        b = b + fit_coefficients(gram, g.to(rhs.dtype), config).to(b.dtype)
+        b = b + solve_with(g.to(q.dtype)).to(b.dtype)
     return b
 
 
