@@ -10,9 +10,13 @@
 // One CTA owns one 128 x 128 tile of the upper triangle and a contiguous range of
 // 64-element K stages: warp 0 issues TMA loads into a 3-stage shared-memory ring,
 // warp 1 issues 12 tcgen05.mma (M=128, N=128, K=16) per stage into a TMEM
-// accumulator, and warps 2-5 read the accumulator (tcgen05.ld) and add it to the
-// FP64 output with atomics. Every mbarrier wait is bounded: a wait that runs out sets
-// the status word, drains the TMA copies it issued, frees TMEM and returns.
+// accumulator, and warps 2-5 read the accumulator (tcgen05.ld), transpose each 32 x 32
+// block through shared memory and store it with the lanes along the columns: with one
+// K split the block is added to the FP64 output directly (one writer per element), with
+// several each split writes its FP32 tile to a slab and gram_reduce_kernel adds the
+// splits in ascending order, so the result is bitwise reproducible. Every mbarrier wait
+// is bounded: a wait that runs out sets the status word, drains the TMA copies it
+// issued, frees TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -39,7 +43,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     gram_bf16x3_kernel(const __grid_constant__ CUtensorMap map_hi,
                        const __grid_constant__ CUtensorMap map_lo, int tiles_per_side,
                        int tile_from, int stages_total, int k_splits, double* __restrict__ out,
-                       int n, int ldo, int* __restrict__ status) {
+                       int n, int ldo, float* __restrict__ slab, int* __restrict__ status) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -141,23 +145,31 @@ __global__ void __launch_bounds__(THREADS, 1)
         umma_commit(&empty[s]);
       }
       if (ok) umma_commit(done);
-    } else if (warp >= 2) {  // epilogue: TMEM -> FP64 output
+    } else if (warp >= 2) {  // epilogue: TMEM -> transpose in shared memory -> FP64 output / slab
       const bool ok = mbar_wait(done, 0, abort);
       tc_fence_after();
       if (ok) {
-        const int q = warp & 3;
-        const int gi = ti * BM + 32 * q + lane;
+        const int q = warp & 3;  // TMEM lanes 32 q .. 32 q + 31 (the warp's accessible quarter)
+        // the stage ring is idle once every MMA finished: reuse it, 32 x 33 floats per warp
+        float* block = reinterpret_cast<float*>(smem) + q * 32 * 33;
+        const int row0 = 32 * q;
         for (int c0 = 0; c0 < BN; c0 += 32) {
           uint32_t v[32];
-          tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
-          if (gi < n) {
-            double* row = out + (size_t)gi * ldo;
+          tmem_ld32(tmem + ((uint32_t)row0 << 16) + (uint32_t)c0, v);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const int gj = tj * BN + c0 + j;
-              if (gj < n) atomicAdd(row + gj, (double)__uint_as_float(v[j]));
+          for (int j = 0; j < 32; ++j) block[lane * 33 + j] = __uint_as_float(v[j]);  // row lane, column j
+          __syncwarp();
+          const int gj = tj * BN + c0 + lane;
+          if (k_splits == 1) {
+            for (int r = 0; r < 32; ++r) {
+              const int gi = ti * BM + row0 + r;
+              if (gi < n && gj < n) out[(size_t)gi * ldo + gj] += (double)block[r * 33 + lane];
             }
+          } else {
+            float* tile = slab + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * (BM * BN);
+            for (int r = 0; r < 32; ++r) tile[(row0 + r) * BN + c0 + lane] = block[r * 33 + lane];
           }
+          __syncwarp();
         }
       } else {
         *abort = 1;
@@ -172,6 +184,38 @@ __global__ void __launch_bounds__(THREADS, 1)
                  "r"(TMEM_COLS));
   }
   if (threadIdx.x == 0 && *abort) atomicExch(status, 1);
+}
+
+// out[tile] += sum over splits s = 0, 1, ... of slab[s][tile], in that order, in FP64.
+// Grid (tiles, BM / 8): a CTA adds 8 rows of one tile, a thread per column.
+__global__ void __launch_bounds__(BN) gram_reduce_kernel(const float* __restrict__ slab, int tiles, int k_splits,
+                                                         int tiles_per_side, int tile_from, double* __restrict__ out,
+                                                         int n, int ldo) {
+  const int pair = blockIdx.x;
+  const int band = tiles_per_side - tile_from;
+  int ti, tj;
+  if (pair < tile_from * band) {
+    ti = pair / band;
+    tj = tile_from + pair % band;
+  } else {
+    int rem = pair - tile_from * band, per_row = band;
+    ti = tile_from;
+    while (rem >= per_row) {
+      rem -= per_row;
+      ++ti;
+      --per_row;
+    }
+    tj = ti + rem;
+  }
+  const int c = threadIdx.x;
+  const int gj = tj * BN + c;
+  for (int r = blockIdx.y * 8; r < blockIdx.y * 8 + 8; ++r) {
+    const int gi = ti * BM + r;
+    double sum = 0.0;
+    for (int split = 0; split < k_splits; ++split)
+      sum += (double)slab[((size_t)split * tiles + pair) * (BM * BN) + r * BN + c];
+    if (gi < n && gj < n) out[(size_t)gi * ldo + gj] += sum;
+  }
 }
 
 // rows [m, n] FP32 -> hi/lo [.., ld] bf16 transposed, at column offset col0.
@@ -244,9 +288,24 @@ int dsg_split_transpose_bf16(const float* rows, int64_t m, int32_t n, int64_t co
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 
+// Tiles of the upper triangle whose column tile is at least column_from's.
+static int gram_pairs(int n_pad, int column_from) {
+  const int tiles = n_pad / BM, tile_from = column_from / BN, band = tiles - tile_from;
+  return tile_from * band + band * (band + 1) / 2;
+}
+
+size_t dsg_gram_bf16x3_workspace_bytes(int32_t n_pad, int64_t k_pad, int32_t column_from, int32_t k_splits) {
+  if (n_pad <= 0 || n_pad % BM != 0 || k_pad <= 0 || column_from < 0 || column_from > n_pad || k_splits < 1)
+    return 0;
+  const int64_t stages = k_pad / BK;
+  const int splits = (int)(k_splits > stages ? stages : k_splits);
+  if (splits <= 1) return 0;
+  return (size_t)splits * gram_pairs(n_pad, column_from) * BM * BN * sizeof(float);
+}
+
 int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, int64_t k_pad,
-                    int32_t column_from, int32_t k_splits, double* out, int32_t ldo,
-                    int32_t* status, void* stream) {
+                    int32_t column_from, int32_t k_splits, double* out, int32_t ldo, void* workspace,
+                    size_t workspace_bytes, int32_t* status, void* stream) {
   if (n < 0 || n_pad < n || n_pad % BM != 0 || k_pad < 0 || k_pad % BK != 0 || ldo < n ||
       column_from < 0 || column_from > n)
     return DSG_ERR_ARGUMENT;
@@ -260,18 +319,26 @@ int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, in
     return DSG_ERR_ARGUMENT;
   const int tiles = n_pad / BM;
   const int tile_from = column_from / BN;
-  const int band = tiles - tile_from;
-  const int pairs = tile_from * band + band * (band + 1) / 2;
+  const int pairs = gram_pairs(n_pad, column_from);
   const int stages = (int)(k_pad / BK);
   if (k_splits > stages) k_splits = stages;
+  const size_t need = dsg_gram_bf16x3_workspace_bytes(n_pad, k_pad, column_from, k_splits);
+  if (need > 0 && (workspace == nullptr || workspace_bytes < need)) return DSG_ERR_WORKSPACE;
   const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
   if (cudaFuncSetAttribute(gram_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return DSG_ERR_LAUNCH;
   dim3 grid(pairs, k_splits);
-  gram_bf16x3_kernel<<<grid, THREADS, smem, (cudaStream_t)stream>>>(
-      map_hi, map_lo, tiles, tile_from, stages, k_splits, out, n, ldo, status);
+  cudaStream_t st = (cudaStream_t)stream;
+  float* slab = reinterpret_cast<float*>(workspace);
+  gram_bf16x3_kernel<<<grid, THREADS, smem, st>>>(map_hi, map_lo, tiles, tile_from, stages, k_splits, out, n, ldo,
+                                                  slab, status);
   dsg_count_launches(1);
+  if (cudaGetLastError() != cudaSuccess) return DSG_ERR_LAUNCH;
+  if (k_splits > 1) {
+    gram_reduce_kernel<<<dim3(pairs, BM / 8), BN, 0, st>>>(slab, pairs, k_splits, tiles, tile_from, out, n, ldo);
+    dsg_count_launches(1);
+  }
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
 }
 

@@ -123,7 +123,8 @@ SIGNATURES = {
         [CP, P, I32, P, P, P, I32, P, P, I32, P, P, I64, I64, P, P],
     ),
     "dsg_split_transpose_bf16": (ctypes.c_int, [P, I64, I32, I64, P, P, I64, P]),
-    "dsg_gram_bf16x3": (ctypes.c_int, [P, P, I32, I32, I64, I32, I32, P, I32, P, P]),
+    "dsg_gram_bf16x3_workspace_bytes": (SZ, [I32, I64, I32, I32]),
+    "dsg_gram_bf16x3": (ctypes.c_int, [P, P, I32, I32, I64, I32, I32, P, I32, P, SZ, P, P]),
 }
 
 _lock = threading.Lock()

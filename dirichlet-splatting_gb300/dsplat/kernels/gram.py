@@ -2,8 +2,9 @@
 
 GramRows collects projected real design rows [m, S] block by block, each stored
 transposed and split into bf16 hi + lo (dsg_split_transpose_bf16); accumulate() then
-adds PT PT^T to a float64 [S, S] total in one tcgen05 launch (dsg_gram_bf16x3), so the
-whole streamed normal-equation Gram is one dense contraction. The plain path is
+adds PT PT^T to a float64 [S, S] total in one tcgen05 launch (dsg_gram_bf16x3, plus an
+ordered sum of its K-split parts), so the whole streamed normal-equation Gram is one dense
+contraction, bitwise reproducible. The plain path is
 cublas.syrk (FP32 SSYRK), as in the reference's dsplat/varpro.py:108-118.
 """
 
@@ -96,9 +97,11 @@ class GramRows:
 
             automatic = k_splits(self.n_pad, k_pad, column_from)
             splits = autotune.gram_splits(automatic, autotune.gram_key(self.n_pad, k_pad, column_from, total.device))
+        nbytes = _lib.query("dsg_gram_bf16x3_workspace_bytes", self.n_pad, k_pad, int(column_from), int(splits))
+        work, nbytes = _lib.workspace(nbytes, total.device)
         call(
             "dsg_gram_bf16x3", ptr(hi), ptr(lo), self.columns, self.n_pad, k_pad, int(column_from),
-            int(splits), ptr(total), total.shape[1], ptr(status), _lib.stream(total.device),
+            int(splits), ptr(total), total.shape[1], ptr(work), nbytes, ptr(status), _lib.stream(total.device),
         )  # fmt: skip
         return status
 

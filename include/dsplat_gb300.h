@@ -351,17 +351,22 @@ int dsg_design_project_bf16x3(const DsgChirp* chirp, const float* positions, int
 int dsg_split_transpose_bf16(const float* rows, int64_t m, int32_t n, int64_t column_offset,
                              void* hi, void* lo, int64_t ld, void* stream);
 
+/* Workspace of dsg_gram_bf16x3 in bytes: one FP32 128 x 128 slab per (tile, K split)
+ * when k_splits > 1 (after capping k_splits at k_pad / 64), else 0. */
+size_t dsg_gram_bf16x3_workspace_bytes(int32_t n_pad, int64_t k_pad, int32_t column_from, int32_t k_splits);
+
 /* Mixed precision: out[n, n] (float64, row-major, leading dimension ldo) += the upper
  * 128 x 128 tiles of PT PT^T, PT = hi + lo of shape [n_pad, k_pad] bf16 (n_pad a multiple
  * of 128, k_pad of 64, zero padded), on the tcgen05 tensor cores in split-BF16x3 with FP32
- * accumulation; k_splits CTAs share each tile's reduction and add their parts atomically.
+ * accumulation; k_splits CTAs share each tile's reduction, write their FP32 parts to the
+ * workspace, and a second kernel adds the parts in split order (bitwise reproducible).
  * Only tiles whose columns reach column_from or beyond are computed (0: the whole upper
  * triangle; the pooled cross-Gram of dsplat/replacement.py:178-199 needs the new columns).
  * status (one int32, zero before the call) becomes 1 if a bounded wait ran out.
  * Replaces dsplat/kernels/cublas.py:31-44 (cublasSsyrk_v2) on the mixed path. */
 int dsg_gram_bf16x3(const void* hi, const void* lo, int32_t n, int32_t n_pad, int64_t k_pad,
-                    int32_t column_from, int32_t k_splits, double* out, int32_t ldo,
-                    int32_t* status, void* stream);
+                    int32_t column_from, int32_t k_splits, double* out, int32_t ldo, void* workspace,
+                    size_t workspace_bytes, int32_t* status, void* stream);
 
 /* ADC-domain synthesis of an FMCW scan in float64 (reference: dsplat/groundtruth.py:58-90
  * synthesize, :40-55 _echoes): adc[a, n] = sum_s amplitudes_s * (echo of surfel s at

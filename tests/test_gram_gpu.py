@@ -31,6 +31,30 @@ def test_split_bf16x3_gram_matches_float64(m, n):
         assert float(total[200:, :128].abs().max()) == 0.0
 
 
+@pytest.mark.parametrize("splits", [1, 3, 8])
+def test_k_split_gram_is_bitwise_reproducible_and_split_independent(splits):
+    """The K-split parts are added in split order by a second kernel (no atomics): two runs
+    give identical bits, and every split count agrees with one split to the FP32 rounding
+    of the partial tiles."""
+    from dsplat.kernels.gram import GramRows
+
+    generator = torch.Generator().manual_seed(11)
+    rows = (torch.randn(40000, 700, generator=generator) * (1 + torch.rand(700, generator=generator))).cuda()
+    store = GramRows(700, len(rows), "cuda")
+    store.append(rows)
+    results = []
+    for count in (splits, splits, 1):
+        total = torch.zeros((700, 700), dtype=torch.float64, device="cuda")
+        assert int(store.accumulate(total, splits=count).item()) == 0
+        results.append(total)
+    assert torch.equal(results[0], results[1])
+    expected = rows.double().T @ rows.double()
+    upper = torch.triu(torch.ones(700, 700, dtype=torch.bool, device="cuda"))
+    for total in results:
+        assert float((total - expected)[upper].abs().max() / expected.abs().max()) < 3e-5
+    assert float((results[0] - results[2])[upper].abs().max() / expected.abs().max()) < 1e-6
+
+
 def test_bf16x3_is_far_more_accurate_than_one_bf16_pass():
     from dsplat.kernels.gram import GramRows
 
