@@ -13,6 +13,8 @@
 #include <math.h>
 #include <atomic>
 #include <mutex>
+#include <algorithm>
+#include <vector>
 #include "common.cuh"
 
 namespace dsg {
@@ -26,14 +28,14 @@ __device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
 // Range profiles: out[seg][a][k] = sum over the segment's surfels of w c D(k - k0).
 // Reference: dsplat/kernels/surfel.slang:87-142 (render_bins), :61-85 (pair_geometry).
 // ------------------------------------------------------------------------------------
+// One CTA's share of the profiles: apertures [16 tile, 16 tile + 16) over the surfels
+// [s_begin, s_end), written to out[seg][a][k]. smem: the tan table, then the warps' records.
 template <int BPL, int P>
-__global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __restrict__ pos,
-                                                     int A, const float* __restrict__ cen,
-                                                     const float* __restrict__ nrm,
-                                                     const float2* __restrict__ w, int S,
-                                                     int seg_len, float2* __restrict__ out) {
+__device__ __forceinline__ void render_tile(const Consts& c, const float* __restrict__ pos, int A,
+                                            const float* __restrict__ cen, const float* __restrict__ nrm,
+                                            const float2* __restrict__ w, int s_begin, int s_end, int tile,
+                                            int seg, float2* __restrict__ out, float* smem) {
   constexpr int REC = 2 + 2 * P;
-  extern __shared__ float smem[];
   const int tbl_n = c.N + 8 * BPL;
   const int tbl_pad = (tbl_n + 3) & ~3;
   float* tbl = smem;
@@ -43,7 +45,7 @@ __global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __re
   for (int i = threadIdx.x; i < tbl_n; i += blockDim.x) tbl[i] = tan_entry(i, c.N, false);
   __syncthreads();
 
-  const int a_base = (blockIdx.x * kWarps + warp) * 4;
+  const int a_base = (tile * kWarps + warp) * 4;
   float apx[4], apy[4], apz[4];
   bool aok[4];
 #pragma unroll
@@ -60,8 +62,6 @@ __global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __re
   for (int i = 0; i < BPL; ++i) acc[i] = make_float2(0.f, 0.f);
   float2 gsum = make_float2(0.f, 0.f);
 
-  const int s_begin = blockIdx.y * seg_len;
-  const int s_end = min(S, s_begin + seg_len);
   for (int s0 = s_begin; s0 < s_end; s0 += 32) {
     const int s = s0 + lane;
     const bool sv = s < s_end;
@@ -123,9 +123,60 @@ __global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __re
   }
   const int a = a_base + qd;
   if (a < A) {
-    float2* o = out + ((size_t)blockIdx.y * A + a) * c.K;
+    float2* o = out + ((size_t)seg * A + a) * c.K;
 #pragma unroll
     for (int i = 0; i < BPL; ++i) o[lp + 8 * i] = make_float2(acc[i].x - gsum.y, acc[i].y + gsum.x);
+  }
+}
+
+template <int BPL, int P>
+__global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __restrict__ pos,
+                                                     int A, const float* __restrict__ cen,
+                                                     const float* __restrict__ nrm,
+                                                     const float2* __restrict__ w, int S,
+                                                     int seg_len, float2* __restrict__ out) {
+  extern __shared__ float smem[];
+  const int s_begin = blockIdx.y * seg_len;
+  render_tile<BPL, P>(c, pos, A, cen, nrm, w, s_begin, min(S, s_begin + seg_len), blockIdx.x, blockIdx.y, out,
+                      smem);
+}
+
+// ------------------------------------------------------------------------------------
+// Profiles of many scenes in one persistent launch (no counterpart in the reference,
+// which renders one scene per call): the work items are (scene, 16-aperture tile), the
+// largest scenes' tiles first, and every CTA takes the next item from a device counter
+// until none is left; a tile covers all of its scene's surfels, so nothing needs a second
+// pass. Scenes may differ in apertures, surfels and chirp (range bins 128 or 256, pad 2).
+// ------------------------------------------------------------------------------------
+struct SceneWork {
+  Consts c;
+  const float* pos;
+  const float* cen;
+  const float* nrm;
+  const float2* w;
+  float2* out;
+  int A, S;
+};
+
+__global__ void __launch_bounds__(128) render_scenes_kernel(const SceneWork* __restrict__ scenes,
+                                                            const int2* __restrict__ items, int count,
+                                                            int* __restrict__ next, int* __restrict__ status) {
+  extern __shared__ float smem[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= count) return;  // the same value in every thread of the CTA
+    const int2 work = items[item];
+    const SceneWork& d = scenes[work.x];
+    if (d.c.P == 2 && d.c.K == 128)
+      render_tile<16, 2>(d.c, d.pos, d.A, d.cen, d.nrm, d.w, 0, d.S, work.y, 0, d.out, smem);
+    else if (d.c.P == 2 && d.c.K == 256)
+      render_tile<32, 2>(d.c, d.pos, d.A, d.cen, d.nrm, d.w, 0, d.S, work.y, 0, d.out, smem);
+    else if (threadIdx.x == 0)
+      atomicExch(status, 1);  // the host validates the chirps; this is a second line of defence
+    __syncthreads();  // the table and s_item are rewritten for the next item
   }
 }
 
@@ -1121,6 +1172,83 @@ int dsg_surfel_jvp(const DsgChirp* chirp, const float* positions, int32_t apertu
               reinterpret_cast<float2*>(out), reinterpret_cast<float2*>(workspace),
               render_segments(chirp, apertures, surfels), st};
   return dispatch_kp(chirp->num_bins, chirp->pad, L);
+}
+
+// Workspace of dsg_surfel_render_scenes: the device scene table, the work items and the
+// queue counter, each 256-byte aligned.
+static size_t scenes_layout(const DsgRenderScene* scenes, int32_t count, size_t* items_at, size_t* counter_at,
+                            int* items) {
+  int total = 0;
+  for (int i = 0; i < count; ++i) total += (scenes[i].apertures + 15) / 16;
+  const size_t table = ((size_t)count * sizeof(SceneWork) + 255) & ~(size_t)255;
+  const size_t list = ((size_t)total * sizeof(int2) + 255) & ~(size_t)255;
+  *items_at = table;
+  *counter_at = table + list;
+  *items = total;
+  return table + list + 256;
+}
+
+size_t dsg_surfel_render_scenes_workspace_bytes(const DsgRenderScene* scenes, int32_t count) {
+  if (!scenes || count <= 0) return 0;
+  size_t items_at, counter_at;
+  int items;
+  return scenes_layout(scenes, count, &items_at, &counter_at, &items);
+}
+
+int dsg_surfel_render_scenes(const DsgRenderScene* scenes, int32_t count, void* workspace, size_t workspace_bytes,
+                             int32_t* status, void* stream) {
+  if (count < 0 || (count > 0 && !scenes)) return DSG_ERR_ARGUMENT;
+  if (count == 0) return DSG_OK;
+  if (!status) return DSG_ERR_ARGUMENT;
+  for (int i = 0; i < count; ++i) {
+    const DsgRenderScene& d = scenes[i];
+    if (!chirp_ok(&d.chirp) || d.chirp.pad != 2 || (d.chirp.num_bins != 128 && d.chirp.num_bins != 256))
+      return DSG_ERR_UNSUPPORTED;
+    if (d.apertures < 0 || d.surfels < 0) return DSG_ERR_ARGUMENT;
+    if (d.apertures > 0 && (!d.positions || !d.out)) return DSG_ERR_ARGUMENT;
+    if (d.apertures > 0 && d.surfels > 0 && (!d.centers || !d.normals || !d.weights)) return DSG_ERR_ARGUMENT;
+  }
+  size_t items_at, counter_at;
+  int total;
+  const size_t need = scenes_layout(scenes, count, &items_at, &counter_at, &total);
+  if (!workspace || workspace_bytes < need) return DSG_ERR_WORKSPACE;
+  if (total == 0) return DSG_OK;
+  // host staging: scene table, items (largest scenes first), counter = 0
+  std::vector<uint8_t> staging(need, 0);
+  SceneWork* table = reinterpret_cast<SceneWork*>(staging.data());
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) {
+    const DsgRenderScene& d = scenes[i];
+    table[i] = SceneWork{make_consts(d.chirp), d.positions, d.centers, d.normals,
+                         reinterpret_cast<const float2*>(d.weights), reinterpret_cast<float2*>(d.out), d.apertures,
+                         d.surfels};
+    order[i] = i;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return (double)scenes[x].surfels * scenes[x].chirp.num_bins > (double)scenes[y].surfels * scenes[y].chirp.num_bins;
+  });
+  int2* list = reinterpret_cast<int2*>(staging.data() + items_at);
+  int k = 0;
+  for (int i : order)
+    for (int t = 0; t < (scenes[i].apertures + 15) / 16; ++t) list[k++] = make_int2(i, t);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(workspace, staging.data(), need, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return launch_status();
+  // shared memory of the widest chirp (256 bins): the table and four warps' records
+  const size_t smem = (table_floats(512, 256) + kWarps * 32 * 4 * (2 + 2 * 2)) * sizeof(float);
+  if (cudaFuncSetAttribute(render_scenes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return launch_status();
+  int per_sm = 0, sms = 152, device = 0;
+  if (cudaGetDevice(&device) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_scenes_kernel, 128, smem);
+  const int grid = std::min(total, std::max(1, per_sm) * sms);
+  uint8_t* base = reinterpret_cast<uint8_t*>(workspace);
+  render_scenes_kernel<<<grid, 128, smem, st>>>(reinterpret_cast<const SceneWork*>(base),
+                                                reinterpret_cast<const int2*>(base + items_at), total,
+                                                reinterpret_cast<int*>(base + counter_at), status);
+  dsg_count_launches(1);
+  return launch_status();
 }
 
 size_t dsg_surfel_reduce_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels,

@@ -37,6 +37,19 @@ class Chirp(ctypes.Structure):
     ]
 
 
+class RenderScene(ctypes.Structure):
+    _fields_ = [
+        ("chirp", Chirp),
+        ("positions", ctypes.c_void_p),
+        ("apertures", ctypes.c_int32),
+        ("centers", ctypes.c_void_p),
+        ("normals", ctypes.c_void_p),
+        ("weights", ctypes.c_void_p),
+        ("surfels", ctypes.c_int32),
+        ("out", ctypes.c_void_p),
+    ]
+
+
 class Grid(ctypes.Structure):
     _fields_ = [
         ("dim", ctypes.c_int32),
@@ -64,6 +77,7 @@ class AscentSpec(ctypes.Structure):
 
 
 CP = ctypes.POINTER(Chirp)
+RSP = ctypes.POINTER(RenderScene)
 AP = ctypes.POINTER(AscentSpec)
 GP = ctypes.POINTER(Grid)
 
@@ -76,6 +90,8 @@ SIGNATURES = {
     "dsg_tuning_get": (I32, [I32]),
     "dsg_surfel_render_workspace_bytes": (SZ, [CP, I32, I32]),
     "dsg_surfel_render": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, SZ, P]),
+    "dsg_surfel_render_scenes_workspace_bytes": (SZ, [RSP, I32]),
+    "dsg_surfel_render_scenes": (ctypes.c_int, [RSP, I32, P, SZ, P, P]),
     "dsg_surfel_jvp": (ctypes.c_int, [CP, P, I32, P, P, P, P, P, P, I32, P, P, SZ, P]),
     "dsg_surfel_reduce_workspace_bytes": (SZ, [CP, I32, I32, I32]),
     "dsg_surfel_vjp": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, P, P, P, SZ, P]),

@@ -100,6 +100,40 @@ def jvp(config, positions, centers, normals, weights, delta_centers, delta_norma
     return torch.view_as_complex(out)
 
 
+def render_scenes(scenes):
+    """Profiles of many scenes in one persistent launch (dsg_surfel_render_scenes).
+
+    scenes: sequence of (config, positions [A, 3], centers [S, 3], normals [S, 3], weights
+    [S] complex, fresnel_n) on one device; every config needs pad 2 and 128 or 256 range
+    bins. Returns the profiles [A, K] complex64 of each scene, in order.
+    """
+    if not scenes:
+        return []
+    device = scenes[0][1].device
+    keep, outputs = [], []  # every buffer the kernel reads stays referenced until the launch is queued
+    table = (_lib.RenderScene * len(scenes))()
+    for slot, (config, positions, centers, normals, weights, fresnel_n) in zip(table, scenes, strict=True):
+        pos, cen, nrm, w = f32(positions), f32(centers), f32(normals), real_view(weights)
+        out = torch.empty((len(pos), config.num_range_bins, 2), dtype=torch.float32, device=device)
+        keep += [pos, cen, nrm, w]
+        outputs.append(out)
+        slot.chirp = _lib.chirp(config, fresnel_n)
+        slot.positions, slot.apertures = pos.data_ptr() if len(pos) else None, len(pos)
+        slot.centers = cen.data_ptr() if len(cen) else None
+        slot.normals = nrm.data_ptr() if len(nrm) else None
+        slot.weights = w.data_ptr() if len(w) else None
+        slot.surfels, slot.out = len(cen), out.data_ptr() if len(pos) else None
+        _work("dsg_surfel_render", len(pos) * len(cen) * config.num_range_bins)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    nbytes = _lib.query("dsg_surfel_render_scenes_workspace_bytes", table, len(scenes))
+    work, nbytes = _lib.workspace(nbytes, device)
+    call("dsg_surfel_render_scenes", table, len(scenes), ptr(work), nbytes, ptr(status), _lib.stream(device))
+    if int(status.item()) != 0:
+        raise _lib.DsplatKernelError("dsg_surfel_render_scenes: a scene descriptor was rejected on the device")
+    del keep
+    return [torch.view_as_complex(out) for out in outputs]
+
+
 class _Render(torch.autograd.Function):
     """Profiles forward; the backward is the hand-written adjoint kernel (dsg_surfel_vjp)."""
 

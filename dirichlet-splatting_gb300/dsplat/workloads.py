@@ -121,3 +121,42 @@ def star_tones(side=256, count=80, span=0.3, snr_db=20.0, seed=0, device="cuda")
                           torch.randn(side, side, generator=generator, dtype=torch.float64))  # fmt: skip
     target = target + sigma * noise
     return target.to(torch.complex64).to(device), truth.float().to(device)
+
+
+def uneven_scenes(count=64, seed=0, device="cuda"):
+    """count FMCW scenes of uneven size (the batched many-scene workload), seeded.
+
+    Each scene draws: array side from {32, 64, 96, 128} at 2.5 mm pitch; 128 or 256 ADC
+    samples (pad 2, so 128 or 256 range bins); 200 to 4000 surfels area-uniform on the front
+    (n_z < 0) half of an ellipsoid with semi-axes 15-40 mm centred at depth 0.30-0.45 m, with
+    outward normals and reflectivity one. Returns a list of dicts with the FMCWConfig, the
+    positions, the true surfels (centers, normals, areas) and their amplitudes.
+    """
+    from .fmcw import FMCWConfig
+
+    generator = torch.Generator().manual_seed(seed)
+    scenes = []
+    for _ in range(count):
+        side = (32, 64, 96, 128)[int(torch.randint(0, 4, (1,), generator=generator))]
+        samples = (128, 256)[int(torch.randint(0, 2, (1,), generator=generator))]
+        surfels = int(torch.randint(200, 4001, (1,), generator=generator))
+        axes = 0.015 + 0.025 * torch.rand(3, generator=generator, dtype=torch.float64)
+        depth = 0.30 + 0.15 * float(torch.rand(1, generator=generator, dtype=torch.float64))
+        # area-uniform on the unit sphere's front half, then stretched onto the ellipsoid
+        z = torch.rand(surfels, generator=generator, dtype=torch.float64)
+        phi = 2 * math.pi * torch.rand(surfels, generator=generator, dtype=torch.float64)
+        ring = (1 - z.square()).clamp(min=0).sqrt()
+        unit = torch.stack((ring * phi.cos(), ring * phi.sin(), -z), -1)
+        centers = torch.tensor([0.0, 0.0, depth], dtype=torch.float64) + axes * unit
+        normals = torch.nn.functional.normalize(unit / axes, dim=1)  # ellipsoid normal ~ gradient of x^2/a^2
+        mean_axis = float(axes.mean())
+        area = 2 * math.pi * mean_axis * mean_axis / surfels
+        scenes.append({
+            "config": FMCWConfig(adc_samples=samples),
+            "positions": planar_array(side, 0.0025, device=device),
+            "centers": centers.float().to(device),
+            "normals": normals.float().to(device),
+            "areas": torch.full((surfels,), area, device=device),
+            "amplitudes": torch.full((surfels,), math.sqrt(area), dtype=torch.complex64, device=device),
+        })  # fmt: skip
+    return scenes

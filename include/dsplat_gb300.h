@@ -87,6 +87,34 @@ int32_t dsg_tuning_get(int32_t knob);
 
 /* ---- FMCW surfels: range profiles and derivatives ------------------------------- */
 
+/* One scene of dsg_surfel_render_scenes: its chirp, sensor positions [apertures, 3],
+ * surfels (centers, normals [surfels, 3], weights [surfels] complex interleaved) and its
+ * output profiles [apertures, num_bins] complex interleaved (all device pointers). */
+typedef struct {
+  DsgChirp chirp;
+  const float* positions;
+  int32_t apertures;
+  const float* centers;
+  const float* normals;
+  const float* weights;
+  int32_t surfels;
+  float* out;
+} DsgRenderScene;
+
+/* Workspace of dsg_surfel_render_scenes (the device scene table, work list and queue counter). */
+size_t dsg_surfel_render_scenes_workspace_bytes(const DsgRenderScene* scenes, int32_t count);
+
+/* Range profiles of many scenes (a HOST array of count descriptors) in one persistent
+ * launch; no counterpart in the reference, which renders one scene per call
+ * (dsplat/kernels/surfel.py:167-196). Work items are (scene, 16-aperture tile), the scenes
+ * with the most surfel-bins first; CTAs take items from a device counter until none is left
+ * (no waits). Scenes may differ in apertures, surfels and chirp; each chirp needs pad 2
+ * and 128 or 256 range bins (DSG_ERR_UNSUPPORTED otherwise). status (one int32, zero before
+ * the call) becomes 1 if the device met a descriptor it cannot render. The descriptors and
+ * the work list are copied to the workspace with one host-to-device copy on stream. */
+int dsg_surfel_render_scenes(const DsgRenderScene* scenes, int32_t count, void* workspace, size_t workspace_bytes,
+                             int32_t* status, void* stream);
+
 /* Workspace of dsg_surfel_render / dsg_surfel_jvp (segment partials), in bytes. */
 size_t dsg_surfel_render_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels);
 
