@@ -132,6 +132,11 @@ def _fused_iteration(model, residual, power, controls, specs, config, mode, frac
     the active-set correlation of the smaller fractions, dsg_ascent_select, the
     correlation gradient and dsg_ascent_update replace the PyTorch algebra of
     _iteration (the same arithmetic, up to the order of float sums).
+
+    stuck (uint8 per candidate) marks candidates that rejected every fraction: their state
+    did not change, so the same trials fail again in every later iteration (the kernels
+    are deterministic); they are kept out of the active set, which removes most of the
+    backtracking work once the ascent converges, without changing any result.
     """
     from .kernels import surfel as kernel
 
@@ -141,20 +146,21 @@ def _fused_iteration(model, residual, power, controls, specs, config, mode, frac
     spec = search.ascent_spec(specs)
     move_normals = "normals" in specs
 
-    def iterate(params, value, grad, inverse):
+    def iterate(params, value, grad, inverse, stuck):
         centers, normals, areas = params["centers"], params["normals"], params["areas"]
         direction = search.direction(inverse, grad, normals, controls[1], config.trust_radius)
         trial_centers, trial_normals = search.trials(centers, normals, direction, controls, fractions)
         corr, norm = kernel.correlate(chirp, positions, trial_centers[0], trial_normals[0], shaped, model.fresnel_n)
         improved, position, pending, batch_centers, batch_normals = search.ascent_partition(
-            corr, norm, areas, power, real_mode, value, trial_centers, trial_normals)  # fmt: skip
+            corr, norm, areas, power, real_mode, value, trial_centers, trial_normals, stuck)  # fmt: skip
         corr2 = norm2 = None
         if len(fractions) > 1:
             corr2, norm2 = kernel.correlate(chirp, positions, batch_centers, batch_normals, shaped, model.fresnel_n,
                                             active=(pending, len(value)))  # fmt: skip
         new_centers, new_normals, accepted = search.ascent_select(
             corr2, norm2, areas, power, real_mode, value, improved, position, trial_centers, trial_normals,
-            centers, normals, move_normals)  # fmt: skip
+            centers, normals, move_normals, stuck)  # fmt: skip
+        stuck.copy_(stuck | (accepted == 0).to(torch.uint8))
         c, n, dc, dn = kernel.correlate_gradient(chirp, positions, new_centers, new_normals, shaped, model.fresnel_n,
                                                  move_normals)  # fmt: skip
         search.ascent_update(spec, c, n, dc, dn, areas, power, real_mode, new_centers, new_normals, accepted,
@@ -185,6 +191,7 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
         inputs["residual"].copy_(residual)
         inputs["controls"].copy_(controls)
         inputs["power"].copy_(power)
+        inputs["stuck"].zero_()
         for k, v in params.items():
             state[0][k].copy_(v)
         state[1].copy_(value)
@@ -196,7 +203,8 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
         _lib.REPLAYED_LAUNCHES += per_replay * config.iterations
     else:
         inputs = {"positions": positions.clone(), "residual": residual.contiguous().clone(),
-                  "controls": controls.contiguous().clone(), "power": power.clone()}  # fmt: skip
+                  "controls": controls.contiguous().clone(), "power": power.clone(),
+                  "stuck": torch.zeros(len(value), dtype=torch.uint8, device=value.device)}  # fmt: skip
         state = ({k: v.float().contiguous().clone() for k, v in params.items()}, value.float().contiguous().clone(),
                  grad.float().contiguous().clone(), inverse.float().contiguous().clone())  # fmt: skip
         static_model = replace(model, scan=replace(model.scan, scan_positions_m=inputs["positions"]))
@@ -209,12 +217,12 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
         try:
             with stage("ascent.capture"):
                 with torch.cuda.stream(side):
-                    iterate(*state)
+                    iterate(*state, inputs["stuck"])
                 torch.cuda.current_stream(device).wait_stream(side)
                 graph = torch.cuda.CUDAGraph()
                 before = _lib.library().dsg_launch_count()
                 with torch.cuda.graph(graph):
-                    iterate(*state)
+                    iterate(*state, inputs["stuck"])
                 per_replay = _lib.library().dsg_launch_count() - before
             with stage("ascent.replay"):
                 for _ in range(config.iterations - 1):

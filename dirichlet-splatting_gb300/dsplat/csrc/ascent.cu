@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(kPartitionThreads)
     partition_kernel(const float2* __restrict__ corr, const float* __restrict__ norm,
                      const float* __restrict__ areas, const double* __restrict__ power, int real_mode,
                      const float* __restrict__ value, int count, const float* __restrict__ trial_centers,
-                     const float* __restrict__ trial_normals, int fraction_count, uint8_t* __restrict__ improved,
-                     int32_t* __restrict__ position, int32_t* __restrict__ pending,
+                     const float* __restrict__ trial_normals, int fraction_count, const uint8_t* __restrict__ stuck,
+                     uint8_t* __restrict__ improved, int32_t* __restrict__ position, int32_t* __restrict__ pending,
                      float* __restrict__ batch_centers, float* __restrict__ batch_normals) {
   constexpr int kWarps = kPartitionThreads / 32;
   __shared__ int warp_count[kWarps];
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kPartitionThreads)
     const float v = certificate_value(corr[i], norm[i], areas[i], p, real_mode != 0);
     const bool up = isfinite(v) && v > value[i];
     improved[i] = up ? 1 : 0;
-    waiting_here += up ? 0 : 1;
+    waiting_here += up || (stuck != nullptr && stuck[i]) ? 0 : 1;
   }
   for (int offset = 16; offset > 0; offset >>= 1) waiting_here += __shfl_xor_sync(0xffffffffu, waiting_here, offset);
   if (lane == 0) warp_count[warp] = waiting_here;
@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(kPartitionThreads)
   for (int start = 0; start < count; start += kPartitionThreads) {
     const int i = start + t;
     const bool live = i < count;
-    const bool waiting = live && improved[i] == 0;  // written by this thread above
+    // written by this thread above; a stuck candidate waits for nothing (no fraction is scored)
+    const bool waiting = live && improved[i] == 0 && !(stuck != nullptr && stuck[i]);
     const unsigned ballot = __ballot_sync(0xffffffffu, waiting);
     __syncthreads();  // every thread has read the previous chunk's counts
     if (lane == 0) warp_count[warp] = __popc(ballot);
@@ -115,13 +116,15 @@ __global__ void select_kernel(const float2* __restrict__ corr, const float* __re
                               const float* __restrict__ value, int count, const uint8_t* __restrict__ improved,
                               const int32_t* __restrict__ position, const float* __restrict__ trial_centers,
                               const float* __restrict__ trial_normals, int fraction_count,
-                              const float* __restrict__ centers, const float* __restrict__ normals, int move_normals,
-                              float* __restrict__ new_centers, float* __restrict__ new_normals,
-                              uint8_t* __restrict__ accepted) {
+                              const uint8_t* __restrict__ stuck, const float* __restrict__ centers,
+                              const float* __restrict__ normals, int move_normals, float* __restrict__ new_centers,
+                              float* __restrict__ new_normals, uint8_t* __restrict__ accepted) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   int chosen = -1;
-  if (improved[i]) {
+  if (stuck != nullptr && stuck[i]) {
+    chosen = -1;  // rejected every fraction from this same state before: it rejects them again
+  } else if (improved[i]) {
     chosen = 0;
   } else if (fraction_count > 1) {
     const int slot = position[i];
@@ -272,7 +275,7 @@ extern "C" {
 
 int dsg_ascent_partition(const float* corr, const float* norm, const float* areas, const double* power,
                          int32_t real_mode, const float* value, int32_t count, const float* trial_centers,
-                         const float* trial_normals, int32_t fraction_count, uint8_t* improved,
+                         const float* trial_normals, int32_t fraction_count, const uint8_t* stuck, uint8_t* improved,
                          int32_t* position, int32_t* pending, float* batch_centers, float* batch_normals,
                          void* stream) {
   if (count < 0 || fraction_count < 1 || fraction_count > kMaxFractions) return DSG_ERR_ARGUMENT;
@@ -282,7 +285,7 @@ int dsg_ascent_partition(const float* corr, const float* norm, const float* area
     return DSG_ERR_ARGUMENT;
   partition_kernel<<<1, kPartitionThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(corr), norm, areas, power, real_mode, value, count, trial_centers,
-      trial_normals, fraction_count, improved, position, pending, batch_centers, batch_normals);
+      trial_normals, fraction_count, stuck, improved, position, pending, batch_centers, batch_normals);
   dsg_count_launches(1);
   return status();
 }
@@ -290,8 +293,9 @@ int dsg_ascent_partition(const float* corr, const float* norm, const float* area
 int dsg_ascent_select(const float* corr, const float* norm, const float* areas, const double* power,
                       int32_t real_mode, const float* value, int32_t count, const uint8_t* improved,
                       const int32_t* position, const float* trial_centers, const float* trial_normals,
-                      int32_t fraction_count, const float* centers, const float* normals, int32_t move_normals,
-                      float* new_centers, float* new_normals, uint8_t* accepted, void* stream) {
+                      int32_t fraction_count, const uint8_t* stuck, const float* centers, const float* normals,
+                      int32_t move_normals, float* new_centers, float* new_normals, uint8_t* accepted,
+                      void* stream) {
   if (count < 0 || fraction_count < 1 || fraction_count > kMaxFractions) return DSG_ERR_ARGUMENT;
   if (count == 0) return DSG_OK;
   if (!areas || !power || !value || !improved || !position || !trial_centers || !trial_normals || !centers ||
@@ -299,7 +303,7 @@ int dsg_ascent_select(const float* corr, const float* norm, const float* areas, 
     return DSG_ERR_ARGUMENT;
   select_kernel<<<(count + kThreads - 1) / kThreads, kThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(corr), norm, areas, power, real_mode, value, count, improved, position,
-      trial_centers, trial_normals, fraction_count, centers, normals, move_normals, new_centers, new_normals,
+      trial_centers, trial_normals, fraction_count, stuck, centers, normals, move_normals, new_centers, new_normals,
       accepted);
   dsg_count_launches(1);
   return status();

@@ -126,8 +126,8 @@ SIGNATURES = {
     "dsg_direction": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P]),
     "dsg_trial": (ctypes.c_int, [P, P, P, P, I32, I32, F32, P, P, P]),
     "dsg_trials": (ctypes.c_int, [P, P, P, P, I32, I32, P, I32, P, P, P]),
-    "dsg_ascent_partition": (ctypes.c_int, [P, P, P, P, I32, P, I32, P, P, I32, P, P, P, P, P, P]),
-    "dsg_ascent_select": (ctypes.c_int, [P, P, P, P, I32, P, I32, P, P, P, P, I32, P, P, I32, P, P, P, P]),
+    "dsg_ascent_partition": (ctypes.c_int, [P, P, P, P, I32, P, I32, P, P, I32, P, P, P, P, P, P, P]),
+    "dsg_ascent_select": (ctypes.c_int, [P, P, P, P, I32, P, I32, P, P, P, P, I32, P, P, P, I32, P, P, P, P]),
     "dsg_ascent_update": (ctypes.c_int, [AP, P, P, P, P, P, P, I32, I32, P, P, P, P, P, P, P, P, P]),
     "dsg_energy_workspace_bytes": (SZ, [I64]),
     "dsg_energy": (ctypes.c_int, [P, P, I64, P, P, SZ, P]),

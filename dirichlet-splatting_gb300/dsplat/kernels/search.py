@@ -113,11 +113,13 @@ def ascent_spec(specs):
     return spec
 
 
-def ascent_partition(corr, norm, areas, power, real_mode, value, trial_centers, trial_normals):
+def ascent_partition(corr, norm, areas, power, real_mode, value, trial_centers, trial_normals, stuck=None):
     """Full-step improvement flags, slots of the stable pending-first partition, the pending
-    count (device) and the batch rows of the smaller fractions at those slots."""
+    count (device) and the batch rows of the smaller fractions at those slots; candidates
+    flagged in stuck (uint8) are never pending."""
     fractions, count = trial_centers.shape[:2]
     device = value.device
+    areas = f32(areas)
     improved = torch.empty(count, dtype=torch.uint8, device=device)
     position = torch.empty(count, dtype=torch.int32, device=device)
     pending = torch.empty(1, dtype=torch.int32, device=device)
@@ -125,24 +127,25 @@ def ascent_partition(corr, norm, areas, power, real_mode, value, trial_centers, 
     batch_centers = torch.empty((rows, 3), dtype=torch.float32, device=device)
     batch_normals = torch.empty((rows, 3), dtype=torch.float32, device=device)
     call(
-        "dsg_ascent_partition", ptr(torch.view_as_real(corr)), ptr(norm), ptr(f32(areas)), ptr(power), int(real_mode),
-        ptr(value), count, ptr(trial_centers), ptr(trial_normals), fractions, ptr(improved), ptr(position),
-        ptr(pending), ptr(batch_centers) if rows else None, ptr(batch_normals) if rows else None,
+        "dsg_ascent_partition", ptr(torch.view_as_real(corr)), ptr(norm), ptr(areas), ptr(power), int(real_mode),
+        ptr(value), count, ptr(trial_centers), ptr(trial_normals), fractions, ptr(stuck), ptr(improved),
+        ptr(position), ptr(pending), ptr(batch_centers) if rows else None, ptr(batch_normals) if rows else None,
         _lib.stream(device),
     )  # fmt: skip
     return improved, position, pending, batch_centers, batch_normals
 
 
 def ascent_select(corr, norm, areas, power, real_mode, value, improved, position, trial_centers, trial_normals,
-                  centers, normals, move_normals):  # fmt: skip
+                  centers, normals, move_normals, stuck=None):  # fmt: skip
     """New centers and normals (the first improving fraction, else unchanged) and accepted."""
     fractions, count = trial_centers.shape[:2]
+    areas = f32(areas)
     new_centers, new_normals = torch.empty_like(centers), torch.empty_like(normals)
     accepted = torch.empty(count, dtype=torch.uint8, device=value.device)
     call(
-        "dsg_ascent_select", None if corr is None else ptr(torch.view_as_real(corr)), ptr(norm), ptr(f32(areas)),
+        "dsg_ascent_select", None if corr is None else ptr(torch.view_as_real(corr)), ptr(norm), ptr(areas),
         ptr(power), int(real_mode), ptr(value), count, ptr(improved), ptr(position), ptr(trial_centers),
-        ptr(trial_normals), fractions, ptr(centers), ptr(normals), int(move_normals), ptr(new_centers),
+        ptr(trial_normals), fractions, ptr(stuck), ptr(centers), ptr(normals), int(move_normals), ptr(new_centers),
         ptr(new_normals), ptr(accepted), _lib.stream(value.device),
     )  # fmt: skip
     return new_centers, new_normals, accepted
@@ -151,9 +154,10 @@ def ascent_select(corr, norm, areas, power, real_mode, value, improved, position
 def ascent_update(spec, corr, norm, dcorr, dnorm, areas, power, real_mode, new_centers, new_normals, accepted,
                   centers, normals, value, gradient, inverse):  # fmt: skip
     """Value, ascent gradient, BFGS inverse and parameters of every candidate, in place."""
+    areas = f32(areas)
     call(
         "dsg_ascent_update", ctypes.byref(spec), ptr(torch.view_as_real(corr)), ptr(norm),
-        ptr(torch.view_as_real(dcorr)), ptr(dnorm), ptr(f32(areas)), ptr(power), int(real_mode), len(value),
+        ptr(torch.view_as_real(dcorr)), ptr(dnorm), ptr(areas), ptr(power), int(real_mode), len(value),
         ptr(new_centers), ptr(new_normals), ptr(accepted), ptr(centers), ptr(normals), ptr(value), ptr(gradient),
         ptr(inverse), _lib.stream(value.device),
     )  # fmt: skip

@@ -303,22 +303,27 @@ typedef struct {
  * partition: position[i] is candidate i's slot, pending (device) their number, and batch
  * row r - 1 of batch_centers / batch_normals [(fraction_count - 1) * count, 3] holds
  * trial fraction r of trial_centers / trial_normals [fraction_count, count, 3] at the
- * slots (reference: dsplat/certificate.py:163-177, the backtracking loop). One CTA. */
+ * slots (reference: dsplat/certificate.py:163-177, the backtracking loop). One CTA.
+ * stuck [count] (optional) marks candidates that rejected every fraction in an earlier
+ * iteration: their state is unchanged, so they reject them again and are never pending
+ * (no smaller fraction is scored for them). */
 int dsg_ascent_partition(const float* corr, const float* norm, const float* areas, const double* power,
                          int32_t real_mode, const float* value, int32_t count, const float* trial_centers,
-                         const float* trial_normals, int32_t fraction_count, uint8_t* improved,
+                         const float* trial_normals, int32_t fraction_count, const uint8_t* stuck, uint8_t* improved,
                          int32_t* position, int32_t* pending, float* batch_centers, float* batch_normals,
                          void* stream);
 /* Batched backtracking, second phase: corr / norm [(fraction_count - 1) * count] are the
  * correlations of the batch rows (dsg_surfel_correlate_active with the pending count).
  * Each candidate takes the first fraction whose finite certificate exceeds value:
  * new_centers / new_normals receive the trial (normals only if move_normals) or the
- * current parameters, accepted[i] whether one was taken. */
+ * current parameters, accepted[i] whether one was taken; a stuck candidate (optional
+ * stuck [count], as for dsg_ascent_partition) takes none. */
 int dsg_ascent_select(const float* corr, const float* norm, const float* areas, const double* power,
                       int32_t real_mode, const float* value, int32_t count, const uint8_t* improved,
                       const int32_t* position, const float* trial_centers, const float* trial_normals,
-                      int32_t fraction_count, const float* centers, const float* normals, int32_t move_normals,
-                      float* new_centers, float* new_normals, uint8_t* accepted, void* stream);
+                      int32_t fraction_count, const uint8_t* stuck, const float* centers, const float* normals,
+                      int32_t move_normals, float* new_centers, float* new_normals, uint8_t* accepted,
+                      void* stream);
 /* End of a batched ascent iteration: corr, norm, dcorr [count, width, 2] and dnorm
  * [count, width] are the unscaled correlation gradient at new_centers / new_normals
  * (dsg_surfel_correlate_gradient). Writes the certificate value, the negated gradient in

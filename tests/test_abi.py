@@ -98,12 +98,12 @@ def test_new_batched_entry_points_validate_on_the_host():
     fake = ctypes.c_void_p(16)  # never dereferenced: validation fails first
     assert lib.dsg_trials(fake, fake, fake, fake, 4, 6, ctypes.addressof(fractions), 17, fake, fake, None) == 1
     assert lib.dsg_trials(fake, fake, fake, fake, 4, 5, ctypes.addressof(fractions), 8, fake, fake, None) == 1
-    assert lib.dsg_ascent_partition(fake, fake, fake, fake, 1, fake, 4, fake, fake, 0, fake, fake, fake, fake,
-                                    fake, None) == 1  # fmt: skip
-    assert lib.dsg_ascent_partition(fake, fake, fake, fake, 1, fake, -1, fake, fake, 8, fake, fake, fake, fake,
-                                    fake, None) == 1  # fmt: skip
-    assert lib.dsg_ascent_select(fake, fake, fake, fake, 1, fake, 4, fake, fake, fake, fake, 17, fake, fake, 1,
-                                 fake, fake, fake, None) == 1  # fmt: skip
+    assert lib.dsg_ascent_partition(fake, fake, fake, fake, 1, fake, 4, fake, fake, 0, None, fake, fake, fake,
+                                    fake, fake, None) == 1  # fmt: skip
+    assert lib.dsg_ascent_partition(fake, fake, fake, fake, 1, fake, -1, fake, fake, 8, None, fake, fake, fake,
+                                    fake, fake, None) == 1  # fmt: skip
+    assert lib.dsg_ascent_select(fake, fake, fake, fake, 1, fake, 4, fake, fake, fake, fake, 17, None, fake, fake,
+                                 1, fake, fake, fake, None) == 1  # fmt: skip
     spec = _lib.AscentSpec()
     spec.width = 4
     assert lib.dsg_ascent_update(ctypes.byref(spec), fake, fake, fake, fake, fake, fake, 1, 4, fake, fake, fake,

@@ -179,9 +179,10 @@ def test_fused_ascent_iterations_match_the_pytorch_iterations(fmcw, mode, with_n
     iterate = _iteration(model, residual, controls, masks, specs, config, mode, fractions, eye)
     power = residual.abs().square().sum().double().clamp(min=1e-30).reshape(1)
     fused = _fused_iteration(model, residual, power, controls, specs, config, mode, fractions)
+    stuck = torch.zeros(count, dtype=torch.uint8, device="cuda")
     for _ in range(config.iterations):
         reference = iterate(*reference)
-        fused(*state)
+        fused(*state, stuck)
         moved = (state[0]["centers"] != start["centers"]).any(1)
         expected_moved = (reference[0]["centers"] != start["centers"]).any(1)
         assert torch.equal(moved, expected_moved)
@@ -192,6 +193,8 @@ def test_fused_ascent_iterations_match_the_pytorch_iterations(fmcw, mode, with_n
         close(state[3], reference[3], 1e-4)
     if frozen_z:
         assert torch.equal(state[0]["centers"][:, 2], start["centers"][:, 2])
+    # every candidate flagged stuck is one the PyTorch iterations did not move in the last round
+    assert bool(((stuck == 0) | ~(state[0]["centers"] != reference[0]["centers"]).any(1)).all())
 
 
 @pytest.mark.parametrize("count", [1, 1000, 3000])
