@@ -91,6 +91,10 @@ __device__ __forceinline__ bool precedes(double b, int ib, double a, int ia) {
 constexpr int kPickThreads = 1024;
 constexpr int kRows = 32;  // rows per update CTA
 constexpr int kSplit = 16;  // warps sharing one row's sums (over the factor's rows and the earlier steps)
+// CTAs sharing one row block's factor-column sum (factor form): row block b sums over
+// k >= max(j, 32 b), so the first blocks carry most of the triangle; splitting every
+// block's k range into kParts shares bounds the longest CTA at a quarter of it.
+constexpr int kParts = 4;
 
 // b = W q, diag = real(W_ii), alive = 1, spent = 0.
 template <typename T>
@@ -244,8 +248,9 @@ __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
     double* __restrict__ diag, const double* __restrict__ wdiag, uint8_t* __restrict__ alive,
     T* __restrict__ U, const uint8_t* __restrict__ limited, long long limit, const Pick* __restrict__ pick_in,
     Pick* __restrict__ pick_out, Candidate* __restrict__ partials, unsigned* __restrict__ counter,
-    int64_t* __restrict__ removed) {
+    T* __restrict__ column_parts, unsigned* __restrict__ row_counter, int64_t* __restrict__ removed) {
   extern __shared__ uint8_t s_dyn[];
+  __shared__ bool s_row_last;
   __shared__ T s_partw[FACTOR ? kSplit : 1][kRows];
   __shared__ T s_part[kSplit][kRows];
   __shared__ T s_uj[256];
@@ -261,13 +266,39 @@ __global__ void __launch_bounds__(kRows * kSplit) step_kernel(
   const int i = blockIdx.x * kRows + lane;
   T accw = zero<T>();
   if (FACTOR) {
+    // this CTA's share [kl, kh) of the row block's k range, X's column j staged for it
     T* s_xj = reinterpret_cast<T*>(s_dyn);
-    for (int k = threadIdx.x; k < n; k += blockDim.x) s_xj[k] = k >= j ? W[(size_t)k * n + j] : zero<T>();
-    __syncthreads();
+    const int parts = (int)gridDim.y;
     const int k0 = max(j, (int)blockIdx.x * kRows);
+    const int share = (n - k0 + parts - 1) / parts;
+    const int kl = min(n, k0 + (int)blockIdx.y * share), kh = min(n, kl + share);
+    for (int k = kl + (int)threadIdx.x; k < kh; k += blockDim.x) s_xj[k - kl] = W[(size_t)k * n + j];
+    __syncthreads();
     if (i < n)
-      for (int k = k0 + warp; k < n; k += kSplit) accw = add(accw, mul_conj(W[(size_t)k * n + i], s_xj[k]));
+      for (int k = kl + warp; k < kh; k += kSplit) accw = add(accw, mul_conj(W[(size_t)k * n + i], s_xj[k - kl]));
     s_partw[FACTOR ? warp : 0][lane] = accw;
+    if (parts > 1) {
+      // shares go to the row block's slots; the last CTA of the block adds them in share order
+      __syncthreads();
+      if (warp == 0) {
+        T total = s_partw[0][lane];
+        for (int w = 1; w < kSplit; ++w) total = add(total, s_partw[FACTOR ? w : 0][lane]);
+        column_parts[((size_t)blockIdx.x * parts + blockIdx.y) * kRows + lane] = total;
+        __threadfence();  // the share reaches L2 before the CTA is counted
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) s_row_last = atomicAdd(&row_counter[blockIdx.x], 1u) == (unsigned)parts - 1;
+      __syncthreads();
+      if (!s_row_last) return;
+      __threadfence();
+      if (threadIdx.x == 0) row_counter[blockIdx.x] = 0;
+      if (warp == 0) {
+        T total = zero<T>();
+        for (int y = 0; y < parts; ++y) total = add(total, load_cg(&column_parts[((size_t)blockIdx.x * parts + y) * kRows + lane]));
+        s_partw[0][lane] = total;
+        for (int w = 1; w < kSplit; ++w) s_partw[FACTOR ? w : 0][lane] = zero<T>();
+      }
+    }
   }
   T acc = zero<T>();
   for (int t0 = 0; t0 < step; t0 += 256) {
@@ -402,6 +433,13 @@ int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* l
   Candidate* partials = reinterpret_cast<Candidate*>(picks + 2);
   unsigned* counter = reinterpret_cast<unsigned*>(partials + blocks);
   uint8_t* alive = reinterpret_cast<uint8_t*>(counter + 4);
+  // after alive: the row blocks' counters and share slots (factor form), 16-byte aligned
+  const size_t tail = (reinterpret_cast<uintptr_t>(alive + n) + 15) & ~(uintptr_t)15;
+  unsigned* row_counter = reinterpret_cast<unsigned*>(tail);
+  T* column_parts = reinterpret_cast<T*>(tail + (((size_t)blocks * sizeof(unsigned) + 15) & ~(size_t)15));
+  const int parts = FACTOR ? kParts : 1;
+  if (FACTOR && cudaMemsetAsync(row_counter, 0, (size_t)blocks * sizeof(unsigned), st) != cudaSuccess)
+    return DSG_ERR_LAUNCH;
   const T* W = reinterpret_cast<const T*>(inverse);
   const T* q = reinterpret_cast<const T*>(rhs);
   size_t smem = 0;
@@ -423,9 +461,9 @@ int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* l
   for (int step = 0; step < count; ++step) {
     const T* bi = (step & 1) ? b1 : b0;
     T* bo = (step & 1) ? b0 : b1;
-    step_kernel<T, FACTOR><<<blocks, kRows * kSplit, smem, st>>>(
+    step_kernel<T, FACTOR><<<dim3(blocks, parts), kRows * kSplit, smem, st>>>(
         W, n, step, count, bi, bo, diag, wdiag, alive, U, limited, limit, picks + (step & 1),
-        picks + ((step + 1) & 1), partials, counter, removed);
+        picks + ((step + 1) & 1), partials, counter, column_parts, row_counter, removed);
   }
   dsg_count_launches((FACTOR ? 3 : 2) + count);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
@@ -440,7 +478,8 @@ size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_comp
   const size_t elem = is_complex ? 16 : 8;
   const size_t blocks = ((size_t)n + kRows - 1) / kRows;
   return elem * 2 * (size_t)n + 16 * (size_t)n + elem * (size_t)count * n + 2 * sizeof(Pick) +
-         blocks * sizeof(Candidate) + 16 + (size_t)n + 64;
+         blocks * sizeof(Candidate) + 16 + (size_t)n + 64 + 16 + blocks * sizeof(unsigned) + 16 +
+         blocks * kParts * kRows * elem;
 }
 
 int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, int32_t count,
