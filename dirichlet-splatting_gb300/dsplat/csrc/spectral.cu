@@ -105,6 +105,24 @@ __device__ __forceinline__ void footprint(const GridC& g, const float* __restric
   d[2] = cscale(cmul(cmul(k[0], k[1]), dk[2]), -1.0f);
 }
 
+// Per-axis tables of the separable atoms: for axis d, grid bin u < nfft[d] and atom s,
+// values[d][u][s] = K_d(u - c_s[d]) and derivatives[d][u][s] = dK_d / d(delta) (complex,
+// interleaved; atoms contiguous, so a table is the row-major [nfft[d], count] operand of
+// the products that assemble the grid). A thread per (axis, bin, atom).
+__global__ void axis_tables_kernel(GridC g, const float* __restrict__ taps, const float* __restrict__ centers,
+                                   int count, int width, float2* __restrict__ values, float2* __restrict__ derivs) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per_axis = (long long)width * count;
+  if (e >= per_axis * g.dim) return;
+  const int d = (int)(e / per_axis);
+  const int u = (int)((e % per_axis) / count), s = (int)(e % count);
+  if (u >= g.nfft[d]) return;
+  float2 k, dk;
+  axis_kernel(g, taps, d, (float)u - __ldg(centers + (size_t)s * g.dim + d), k, dk);
+  values[e] = k;
+  derivs[e] = dk;
+}
+
 __global__ void spectral_forward_kernel(GridC g, const float* __restrict__ taps,
                                         const float* __restrict__ centers, int count,
                                         const float2* __restrict__ coeff,
@@ -238,6 +256,23 @@ int spectral_spans(int count, int size, int& span) {
 }  // namespace
 
 extern "C" {
+
+int dsg_spectral_axis_tables(const DsgGrid* grid, const float* taps, const float* centers, int32_t count,
+                             float* values, float* derivatives, void* stream) {
+  GridC g;
+  if (!grid_ok(grid, g)) return DSG_ERR_ARGUMENT;
+  if (count < 0) return DSG_ERR_ARGUMENT;
+  if (count == 0) return DSG_OK;
+  if (!centers || !values || !derivatives || (g.window == 3 && !taps)) return DSG_ERR_ARGUMENT;
+  int width = 1;
+  for (int d = 0; d < g.dim; ++d) width = g.nfft[d] > width ? g.nfft[d] : width;
+  const long long total = (long long)g.dim * width * count;
+  if (total > 0x7fffffffLL * 128) return DSG_ERR_ARGUMENT;
+  axis_tables_kernel<<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      g, taps, centers, count, width, reinterpret_cast<float2*>(values), reinterpret_cast<float2*>(derivatives));
+  dsg_count_launches(1);
+  return status();
+}
 
 int dsg_spectral_render(const DsgGrid* grid, const float* taps, const float* centers,
                         int32_t count, const float* coeff, const float* bins, int32_t size,

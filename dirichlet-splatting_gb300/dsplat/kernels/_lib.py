@@ -108,6 +108,7 @@ SIGNATURES = {
     ),
     "dsg_surfel_design": (ctypes.c_int, [CP, P, I32, P, P, P, I32, I32, P, P]),
     "dsg_surfel_jacobian": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, P]),
+    "dsg_spectral_axis_tables": (ctypes.c_int, [GP, P, P, I32, P, P, P]),
     "dsg_spectral_render": (ctypes.c_int, [GP, P, P, I32, P, P, I32, P, P]),
     "dsg_spectral_jvp": (ctypes.c_int, [GP, P, P, I32, P, P, P, P, I32, P, P]),
     "dsg_spectral_vjp_workspace_bytes": (SZ, [GP, I32, I32]),

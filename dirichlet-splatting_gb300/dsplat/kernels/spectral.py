@@ -113,3 +113,101 @@ def vjp(grid, centers, coefficients, upstream, bins):
     """Gradients of Re(conj(upstream) . render) for centers and complex coefficients."""
     gc, gb = _backward(grid, centers, real_view(coefficients), bins, real_view(upstream))
     return gc, torch.view_as_complex(gb)
+
+
+# --- The whole grid as products of per-axis tables -------------------------------------------
+# An atom's spectrum is a product over axes, A[(u0, u1, ...), s] = prod_d K_d(u_d - c_sd),
+# so on the full grid the forward is (K_0 * b) @ KR(K_1, ...)^T with KR the column-wise
+# Kronecker (Khatri-Rao) product of the other axes' [nfft_d, S] tables: the kernel is
+# evaluated dim * nfft * S times instead of prod(nfft) * S (41 k instead of 5.2 M sincos
+# pairs on a 256^2 grid with 80 atoms), and the sums are complex products (cuBLAS).
+
+
+def axis_tables(grid, centers):
+    """([K_0, K_1, ...], [dK_0, ...]) per-axis kernel tables [nfft_d, S] (complex64)."""
+    centers = f32(centers)
+    c, taps = _grid(grid, centers.device)
+    dim, width, count = len(grid.shape), max(grid.shape), len(centers)
+    values = torch.zeros((dim, width, count, 2), dtype=torch.float32, device=centers.device)
+    derivatives = torch.zeros_like(values)
+    call("dsg_spectral_axis_tables", c, ptr(taps), ptr(centers), count, ptr(values), ptr(derivatives),
+         _lib.stream(centers.device))  # fmt: skip
+    values, derivatives = torch.view_as_complex(values), torch.view_as_complex(derivatives)
+    return ([values[d, :n] for d, n in enumerate(grid.shape)],
+            [derivatives[d, :n] for d, n in enumerate(grid.shape)])  # fmt: skip
+
+
+def _khatri_rao(tables):
+    """Column-wise Kronecker product [prod n_d, S] of [n_d, S] tables, row-major over axes."""
+    out = tables[0]
+    for table in tables[1:]:
+        out = (out[:, None, :] * table[None, :, :]).reshape(-1, out.shape[-1])
+    return out
+
+
+def _assemble(tables, weights):
+    """Grid values [prod nfft] of sum_s weights_s prod_d tables_d[u_d, s]."""
+    if len(tables) == 1:
+        return tables[0] @ weights
+    return ((tables[0] * weights) @ _khatri_rao(tables[1:]).mT).reshape(-1)
+
+
+def _adjoint(tables, upstream):
+    """Per atom sum_m conj(prod_d tables_d[u_d, s]) upstream[m] (the dictionary's A^H u)."""
+    first = tables[0]
+    if len(tables) == 1:
+        return first.mH @ upstream
+    rows = upstream.reshape(first.shape[0], -1)
+    return (first.conj() * (rows @ _khatri_rao(tables[1:]).conj())).sum(0)
+
+
+def render_grid(grid, centers, coefficients):
+    """Coherent sum of the atoms on the whole grid [prod shape] (row-major), complex64."""
+    values, _ = axis_tables(grid, centers)
+    return _assemble(values, coefficients.to(torch.complex64))
+
+
+def jvp_grid(grid, centers, coefficients, delta_centers, delta_coefficients):
+    """Directional derivative of render_grid along (delta_centers, delta_coefficients)."""
+    values, derivatives = axis_tables(grid, centers)
+    b = coefficients.to(torch.complex64)
+    out = _assemble(values, delta_coefficients.to(torch.complex64))
+    dc = f32(delta_centers)
+    for axis in range(len(values)):
+        # d atom / d centre_axis = -dK_axis times the other axes' values
+        tables = [derivatives[d] if d == axis else values[d] for d in range(len(values))]
+        out = out - _assemble(tables, b * dc[:, axis])
+    return out
+
+
+def vjp_grid(grid, centers, coefficients, upstream):
+    """Gradients of Re(conj(upstream) . render_grid) for centers [S, D] and coefficients."""
+    values, derivatives = axis_tables(grid, centers)
+    u = upstream.reshape(-1).to(torch.complex64)
+    b = coefficients.to(torch.complex64)
+    grad_b = _adjoint(values, u)
+    grad_c = torch.stack([-(b * _adjoint([derivatives[d] if d == axis else values[d] for d in range(len(values))],
+                                         u).conj()).real for axis in range(len(values))], -1)  # fmt: skip
+    return grad_c.float(), grad_b
+
+
+class _RenderGrid(torch.autograd.Function):
+    """render_grid with the separable adjoint as its backward."""
+
+    @staticmethod
+    def forward(ctx, centers, coefficients, grid):
+        ctx.save_for_backward(centers, coefficients)
+        ctx.grid = grid
+        return render_grid(grid, centers, coefficients)
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        centers, coefficients = ctx.saved_tensors
+        gc, gb = vjp_grid(ctx.grid, centers, coefficients, grad)
+        return gc.to(centers.dtype), gb.to(coefficients.dtype), None
+
+
+def render_on_grid(grid, centers, coefficients):
+    """render_grid, differentiable in centers and coefficients."""
+    return _RenderGrid.apply(centers.contiguous(), coefficients, grid)

@@ -76,17 +76,18 @@ class SpectralModel:
         derivatives = kernel.design(self.grid, params["centers"][atoms], self._bins(params)[rows], derivatives=True)
         return {"centers": derivatives[1]}
 
+    # The model's products cover the whole grid, so they run in the separable form: per-axis
+    # kernel tables (dsg_spectral_axis_tables) combined by complex matrix products.
+
     def render(self, params, coefficients):
-        return kernel.render(self.grid, params["centers"], coefficients, self._bins(params)).reshape(self.shape)
+        return kernel.render_on_grid(self.grid, params["centers"], coefficients).reshape(self.shape)
 
     def jvp(self, params, coefficients, tangent, delta_coefficients):
-        change = kernel.jvp(self.grid, params["centers"], coefficients, tangent["centers"], delta_coefficients,
-                            self._bins(params))  # fmt: skip
+        change = kernel.jvp_grid(self.grid, params["centers"], coefficients, tangent["centers"], delta_coefficients)
         return change.reshape(self.shape)
 
     def vjp(self, params, coefficients, upstream):
-        centers, weights = kernel.vjp(self.grid, params["centers"], coefficients, upstream.reshape(-1),
-                                      self._bins(params))  # fmt: skip
+        centers, weights = kernel.vjp_grid(self.grid, params["centers"], coefficients, upstream)
         return {"centers": centers}, weights
 
     def correlate(self, params, residual, active=None):

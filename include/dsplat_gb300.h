@@ -223,6 +223,15 @@ int dsg_surfel_jacobian(const DsgChirp* chirp, const float* positions, int32_t a
 
 /* ---- Spectral atoms --------------------------------------------------------------- */
 
+/* Per-axis tables of the separable spectral atoms (the redesign of the reference's
+ * per-bin evaluation, dsplat/kernels/spectral.slang:4-47): for axis d < dim, bin
+ * u < nfft[d] and atom s, values[d][u][s] = K_d(u - centers[s][d]) and derivatives the
+ * same of dK_d / d(delta), complex interleaved, with width = max nfft: values and
+ * derivatives hold dim * width * count complex values (rows u >= nfft[d] untouched). The
+ * grid's forward, JVP and VJP are then products of these [nfft[d], count] tables. */
+int dsg_spectral_axis_tables(const DsgGrid* grid, const float* taps, const float* centers, int32_t count,
+                             float* values, float* derivatives, void* stream);
+
 /* out[M] = sum_s a_ms coeff_s (reference: dsplat/kernels/spectral.py:168-189). */
 int dsg_spectral_render(const DsgGrid* grid, const float* taps, const float* centers,
                         int32_t count, const float* coeff, const float* bins, int32_t size,

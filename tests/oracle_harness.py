@@ -44,6 +44,13 @@ def import_package_on_oracle():
         return full_correlate(config, positions, centers, normals, residual, fresnel_n)
 
     shims["surfel"].correlate = correlate
+    # the spectral model's whole-grid products, restated on the oracle's per-bin bindings
+    spectral = shims["spectral"]
+    spectral.render_on_grid = lambda grid, centers, b: spectral.render(grid, centers, b, grid.bins(centers.device))
+    spectral.jvp_grid = lambda grid, centers, b, dc, db: spectral.jvp(grid, centers, b, dc, db,
+                                                                      grid.bins(centers.device))  # fmt: skip
+    spectral.vjp_grid = lambda grid, centers, b, u: spectral.vjp(grid, centers, b, u.reshape(-1),
+                                                                 grid.bins(centers.device))  # fmt: skip
     for name, module in shims.items():
         sys.modules[f"dsplat.kernels.{name}"] = module
     sys.path.insert(0, str(ROOT / "dirichlet-splatting_gb300"))
