@@ -701,17 +701,24 @@ def run_kernels(args):
     record("dsg_surfel_jvp", ms, A * S * K, 24)
     ms = _event_time(lambda: kernel.vjp(config, positions, centers, normals, weights, upstream, 0.0), it, wu, flush)
     record("dsg_surfel_vjp", ms, A * S * K, 20)
+    with kernel.correlation_form("exact"):
+        ms = _event_time(lambda: kernel.vjp(config, positions, centers, normals, weights, upstream, 0.0), it, wu,
+                         flush)  # fmt: skip
+    record("dsg_surfel_vjp [exact bin sums]", ms, A * S * K, 20)
     if args.only == "splat":  # the three splat kernels alone (the ncu captures of render / JVP / VJP)
         print(json.dumps({"case": args.case, "apertures": A, "surfels": S, "bins": K, "kernels": rows}), flush=True)
         return
     sub = positions[: min(A, 768)].contiguous()
     cand = centers.repeat(max(1, 8192 // S), 1)[:8192].contiguous()
     cand_n = normals.repeat(max(1, 8192 // S), 1)[:8192].contiguous()
-    ms = _event_time(lambda: kernel.correlate(config, sub, cand, cand_n, upstream[: len(sub)], 0.0), it, wu, flush)
-    record("dsg_surfel_correlate", ms, len(sub) * len(cand) * K, 18)
-    ms = _event_time(lambda: kernel.correlate_gradient(config, sub, cand[:1024], cand_n[:1024], upstream[: len(sub)],
-                                                       0.0, True), it, wu, flush)  # fmt: skip
-    record("dsg_surfel_correlate_gradient", ms, len(sub) * 1024 * K, 30)
+    for form, suffix in (("interp", ""), ("exact", " [exact bin sums]")):
+        with kernel.correlation_form(form):
+            ms = _event_time(lambda: kernel.correlate(config, sub, cand, cand_n, upstream[: len(sub)], 0.0), it, wu,
+                             flush)  # fmt: skip
+            record("dsg_surfel_correlate" + suffix, ms, len(sub) * len(cand) * K, 18)
+            ms = _event_time(lambda: kernel.correlate_gradient(config, sub, cand[:1024], cand_n[:1024],
+                                                               upstream[: len(sub)], 0.0, True), it, wu, flush)  # fmt: skip
+            record("dsg_surfel_correlate_gradient" + suffix, ms, len(sub) * 1024 * K, 30)
     bank = fibonacci_sphere(24, device)
     ncand = 200000 if args.case == "full" else 50000
     grid = centers.repeat(ncand // S + 1, 1)[:ncand].contiguous()
@@ -721,6 +728,17 @@ def run_kernels(args):
     ms = _event_time(lambda: kernel.correlate_orientations(config, prop, grid, grid_n, bank, upstream[: len(prop)],
                                                            0.0, table), it, wu, flush)  # fmt: skip
     record("dsg_surfel_correlate_orientations", ms, len(prop) * len(grid) * 25, 12, "pair-normals")
+    # greedy separated peaks as a search level runs them: 1024 peaks kept from 1024 cubes of
+    # 4^3 offsets (0.25 mm pitch) at separation 0.25 mm, scores in random order
+    from dsplat.kernels import search
+
+    cubes = centers.repeat(1024 // S + 1, 1)[:1024]
+    axis = (torch.arange(4, device=device, dtype=torch.float32) - 1.5) * 2.5e-4
+    offsets = torch.cartesian_prod(axis, axis, axis)
+    points = (cubes[:, None, :] + offsets[None]).reshape(-1, 3).contiguous()
+    scores = torch.rand(len(points), generator=torch.Generator().manual_seed(5)).to(device)
+    ms = _event_time(lambda: search.peaks(scores, points, 1024, 2.5e-4), it, wu, flush)
+    rows.append({"kernel": f"dsg_peaks ({len(points)} candidates, 1024 peaks, sort included)", "ms": round(ms, 4)})
     from dsplat.groundtruth import synthesize
 
     amplitudes = (reflectivity * params["areas"].sqrt()).to(torch.complex64)

@@ -27,6 +27,8 @@
 void dsg_count_launches(int kernels);
 // Launch-shape knob (DSG_TUNE_*) set through dsg_tuning_set; 0 means automatic.
 int dsg_tuning_value(int knob);
+// Unique id of the calling thread's current CUDA context; 0 when unavailable (surfel.cu).
+unsigned long long dsg_current_context_id();
 
 namespace dsg {
 

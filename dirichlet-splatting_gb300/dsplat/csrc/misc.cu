@@ -87,7 +87,7 @@ uint64_t dsg_launch_count(void) { return g_launches.load(); }
 
 int dsg_tuning_set(int32_t knob, int32_t value) {
   if (knob < 0 || knob >= DSG_TUNE_COUNT || value < 0) return DSG_ERR_ARGUMENT;
-  static const int kMax[DSG_TUNE_COUNT] = {32, 8, 8};
+  static const int kMax[DSG_TUNE_COUNT] = {32, 8, 8, 2};
   if (value > kMax[knob]) return DSG_ERR_ARGUMENT;
   g_tuning[knob].store(value);
   return DSG_OK;

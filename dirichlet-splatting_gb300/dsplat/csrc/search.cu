@@ -47,19 +47,122 @@ bool allow_shared(Kernel kernel, size_t dynamic) {
 // (reference: dsplat/kernels/search.slang:26-64). Chunks of 1024 candidates are first
 // checked against the taken set in parallel; a chunk's survivors are then resolved in
 // order, each taken one suppressing the later ones within separation.
+//
+// In one to three dimensions the taken peaks are also filed in a shared-memory hash of
+// cells of side separation (1 + 2^-16), so a candidate looks only at the peaks of its own
+// and the 3^d - 1 neighbouring cells (any peak nearer than separation lies there) instead
+// of scanning every taken peak, and one warp resolves a chunk's survivors, a lane per
+// neighbouring cell, without a block barrier per taken peak; the selection is the same.
+constexpr unsigned long long kEmptyCell = ~0ull;
+
+__device__ __forceinline__ int cell_of(float x, float inv_cell) {
+  const float c = floorf(x * inv_cell);
+  return (int)fminf(fmaxf(c, -1048000.0f), 1048000.0f);
+}
+
+__device__ __forceinline__ unsigned long long cell_key(int cx, int cy, int cz) {
+  return ((unsigned long long)(cx + (1 << 20)) << 42) | ((unsigned long long)(cy + (1 << 20)) << 21) |
+         (unsigned long long)(cz + (1 << 20));
+}
+
+__device__ __forceinline__ unsigned cell_slot(unsigned long long key, unsigned mask) {
+  return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 40) & mask;
+}
+
+struct PeakCells {
+  unsigned long long* keys;  // [slots], kEmptyCell when free
+  int* heads;                // [slots] first taken peak filed in the cell
+  int* next;                 // [peaks] next taken peak of the same cell, -1 at the end
+  unsigned mask;             // slots - 1
+  float inv_cell;
+};
+
+__device__ __forceinline__ void cell_coords(const PeakCells& h, const float* c, int dimension, int* cc) {
+  cc[0] = cell_of(c[0], h.inv_cell);
+  cc[1] = dimension > 1 ? cell_of(c[1], h.inv_cell) : 0;
+  cc[2] = dimension > 2 ? cell_of(c[2], h.inv_cell) : 0;
+}
+
+// Files taken peak `slot` (coordinates c) under its cell (one thread).
+__device__ void file_peak(const PeakCells& h, const float* c, int dimension, int slot) {
+  int cc[3];
+  cell_coords(h, c, dimension, cc);
+  const unsigned long long key = cell_key(cc[0], cc[1], cc[2]);
+  unsigned s = cell_slot(key, h.mask);
+  for (unsigned probe = 0; probe <= h.mask; ++probe, s = (s + 1) & h.mask) {
+    if (h.keys[s] == key) {
+      h.next[slot] = h.heads[s];
+      h.heads[s] = slot;
+      return;
+    }
+    if (h.keys[s] == kEmptyCell) {
+      h.keys[s] = key;
+      h.heads[s] = slot;
+      h.next[slot] = -1;
+      return;
+    }
+  }
+}
+
+// Whether a taken peak filed in the cell at offset (dx, dy, dz) from c's cell lies within
+// separation of c (sep2 = separation^2).
+__device__ bool cell_hit(const PeakCells& h, const float* c, int dimension, const int* cc, int dx, int dy, int dz,
+                         const float* taken_xyz, float sep2) {
+  const unsigned long long key = cell_key(cc[0] + dx, cc[1] + dy, cc[2] + dz);
+  unsigned s = cell_slot(key, h.mask);
+  for (unsigned probe = 0; probe <= h.mask; ++probe, s = (s + 1) & h.mask) {
+    const unsigned long long k = h.keys[s];
+    if (k == kEmptyCell) return false;
+    if (k != key) continue;
+    for (int t = h.heads[s]; t >= 0; t = h.next[t]) {
+      float d2 = 0.0f;
+      for (int j = 0; j < dimension; ++j) {
+        const float d = c[j] - taken_xyz[t * dimension + j];
+        d2 += d * d;
+      }
+      if (d2 < sep2) return true;
+    }
+    return false;
+  }
+  return false;
+}
+
+// Whether a taken peak lies within separation of c: its own and the neighbouring cells.
+__device__ bool near_taken(const PeakCells& h, const float* c, int dimension, const float* taken_xyz,
+                           float sep2) {
+  int cc[3];
+  cell_coords(h, c, dimension, cc);
+  const int ry = dimension > 1 ? 1 : 0, rz = dimension > 2 ? 1 : 0;
+  for (int dz = -rz; dz <= rz; ++dz)
+    for (int dy = -ry; dy <= ry; ++dy)
+      for (int dx = -1; dx <= 1; ++dx)
+        if (cell_hit(h, c, dimension, cc, dx, dy, dz, taken_xyz, sep2)) return true;
+  return false;
+}
+
 __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __restrict__ scores,
                                                              const int* __restrict__ order,
                                                              const float* __restrict__ centers,
                                                              int count, int dimension, int peaks,
-                                                             float separation,
+                                                             float separation, int slots,
                                                              int* __restrict__ output) {
-  extern __shared__ float taken_xyz[];  // [peaks][dimension]
+  extern __shared__ unsigned long long peak_smem[];
+  __shared__ float chunk_xyz[kPeakThreads * 3];  // hashed: the chunk's candidates, for warp 0
   __shared__ int alive[kPeakThreads];
   __shared__ int alive_list[kPeakThreads];  // the chunk's survivors, in order
   __shared__ int warp_alive[kPeakThreads / 32];
   __shared__ int n_taken;
+  const bool hashed = slots > 0;  // uniform
+  PeakCells cells;
+  cells.keys = peak_smem;
+  cells.heads = reinterpret_cast<int*>(peak_smem + slots);
+  cells.next = cells.heads + slots;
+  cells.mask = (unsigned)slots - 1u;
+  cells.inv_cell = 1.0f / (separation * (1.0f + 1.0f / 65536.0f));
+  float* taken_xyz = reinterpret_cast<float*>(cells.next + (hashed ? peaks : 0));  // [peaks][dimension]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float sep2 = separation * separation;
+  for (int i = tid; i < slots; i += kPeakThreads) cells.keys[i] = kEmptyCell;
   if (tid == 0) n_taken = 0;
   __syncthreads();
   for (int base = 0; base < count; base += kPeakThreads) {
@@ -74,15 +177,19 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
       for (int j = 0; j < dimension; ++j) c[j] = centers[(size_t)index * dimension + j];
     }
     const int taken_now = n_taken;
-    // Latest peaks first: a suppressed candidate mostly lies near a recent, slightly
-    // better one, so its scan ends early (the outcome does not depend on the order).
-    for (int t = taken_now - 1; ok && t >= 0; --t) {
-      float d2 = 0.0f;
-      for (int j = 0; j < dimension; ++j) {
-        const float d = c[j] - taken_xyz[t * dimension + j];
-        d2 += d * d;
+    if (hashed) {
+      if (ok && taken_now > 0) ok = !near_taken(cells, c, dimension, taken_xyz, sep2);
+    } else {
+      // Latest peaks first: a suppressed candidate mostly lies near a recent, slightly
+      // better one, so its scan ends early (the outcome does not depend on the order).
+      for (int t = taken_now - 1; ok && t >= 0; --t) {
+        float d2 = 0.0f;
+        for (int j = 0; j < dimension; ++j) {
+          const float d = c[j] - taken_xyz[t * dimension + j];
+          d2 += d * d;
+        }
+        if (d2 < sep2) ok = false;
       }
-      if (d2 < sep2) ok = false;
     }
     alive[tid] = ok ? 1 : 0;
     const unsigned ballot = __ballot_sync(0xffffffffu, ok);
@@ -94,7 +201,41 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
       survivors += warp_alive[w];
     }
     if (ok) alive_list[before] = tid;
+    if (hashed)
+      for (int j = 0; j < dimension; ++j) chunk_xyz[tid * 3 + j] = c[j];
     __syncthreads();
+    if (hashed) {
+      // Warp 0 resolves the survivors in order: lane l probes neighbouring cell l (3^d of
+      // them) for a peak taken earlier in this chunk; a survivor nobody hits is taken and
+      // filed at once. No block barrier per taken peak.
+      if (warp == 0) {
+        const int ncells = dimension == 1 ? 3 : dimension == 2 ? 9 : 27;
+        const int dx = lane % 3 - 1, dy = dimension > 1 ? (lane / 3) % 3 - 1 : 0,
+                  dz = dimension > 2 ? lane / 9 - 1 : 0;
+        int taken = n_taken;
+        for (int q = 0; q < survivors && taken < peaks; ++q) {
+          const int k = alive_list[q];
+          const float* ck = chunk_xyz + k * 3;
+          bool hit = false;
+          if (lane < ncells) {
+            int cc[3];
+            cell_coords(cells, ck, dimension, cc);
+            hit = cell_hit(cells, ck, dimension, cc, dx, dy, dz, taken_xyz, sep2);
+          }
+          if (__any_sync(0xffffffffu, hit)) continue;
+          if (lane == 0) {
+            for (int j = 0; j < dimension; ++j) taken_xyz[taken * dimension + j] = ck[j];
+            output[taken] = order[base + k];
+            file_peak(cells, ck, dimension, taken);
+          }
+          ++taken;
+          __syncwarp();
+        }
+        if (lane == 0) n_taken = taken;
+      }
+      __syncthreads();
+      continue;
+    }
     const int limit = min(kPeakThreads, count - base);
     for (int q = 0; q < survivors; ++q) {
       const int k = alive_list[q];
@@ -297,10 +438,17 @@ int dsg_peaks(const float* scores, const int32_t* order, const float* centers, i
   if (!output || (count > 0 && (!scores || !order || !centers))) return DSG_ERR_ARGUMENT;
   cudaMemsetAsync(output, 0xff, (size_t)peaks * sizeof(int32_t), (cudaStream_t)stream);
   if (count == 0) return status();
-  const size_t smem = (size_t)peaks * dimension * sizeof(float);
+  // cell hash (1..3 dimensions, a finite positive separation): twice the peaks' slots
+  int slots = 0;
+  if (dimension <= 3 && separation > 0.0f && isfinite(separation)) {
+    slots = 64;
+    while (slots < 2 * peaks) slots <<= 1;
+  }
+  const size_t smem = (size_t)slots * (sizeof(unsigned long long) + sizeof(int)) +
+                      (slots > 0 ? (size_t)peaks * sizeof(int) : 0) + (size_t)peaks * dimension * sizeof(float);
   if (!allow_shared(peaks_kernel, smem)) return DSG_ERR_LAUNCH;
-  peaks_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(scores, order, centers, count,
-                                                               dimension, peaks, separation, output);
+  peaks_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(scores, order, centers, count, dimension,
+                                                               peaks, separation, slots, output);
   dsg_count_launches(1);
   return status();
 }

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <vector>
 #include "common.cuh"
+#include "reduce.cuh"
 
 namespace dsg {
 
@@ -354,13 +355,6 @@ __global__ void segment_sum_kernel(const float2* __restrict__ partial, int segme
 // Reference: dsplat/kernels/correlate.slang:75-108 (surfel_correlate), :171-235
 // (surfel_correlate_gradient), dsplat/kernels/surfel.slang:223-311 (vjp_bins).
 // ------------------------------------------------------------------------------------
-template <int MODE>
-struct ModeInfo;
-template <> struct ModeInfo<0> { static constexpr int NV = 3; static constexpr int W = 0; };
-template <> struct ModeInfo<1> { static constexpr int NV = 12; static constexpr int W = 3; };
-template <> struct ModeInfo<2> { static constexpr int NV = 21; static constexpr int W = 6; };
-template <> struct ModeInfo<3> { static constexpr int NV = 8; static constexpr int W = 0; };
-
 template <int P>
 __host__ __device__ constexpr int reduce_record() { return 16 + 2 * P; }
 
@@ -563,52 +557,10 @@ __global__ void __launch_bounds__(128) reduce_kernel(Consts c, const float* __re
         if (kGrad) n1 += d0.x * d1.x + d0.y * d1.y;
       }
       // chain to the outputs
-      const float2 rot = make_float2(r[R_ROT], r[R_ROT + 1]);
-      const float2 e0 = cmulc(rot, z0);
-      if (MODE == 0) {
-        accv[0] += amp * e0.x;
-        accv[1] += amp * e0.y;
-        accv[2] += amp * amp * n0;
-      } else {
-        const float2 e1 = cmulc(rot, z1);
-        const float amp_cos = r[R_AMPC], cosv = r[R_COS], inv_r = r[R_INVR], rate = r[R_RATE];
-        const float uu[3] = {r[R_U], r[R_U + 1], r[R_U + 2]};
-        const float nv[3] = {nx, ny, nz};
-        // kpm E1 + i rate E0
-        const float2 inner = make_float2(c.kpm * e1.x - rate * e0.y, c.kpm * e1.y + rate * e0.x);
-        if (kGrad) {
-          constexpr int W = ModeInfo<MODE>::W;
-          accv[0] += amp * e0.x;
-          accv[1] += amp * e0.y;
-          accv[2] += amp * amp * n0;
-#pragma unroll
-          for (int jj = 0; jj < 3; ++jj) {
-            const float da = (amp * uu[jj] + amp_cos * (cosv * uu[jj] - nv[jj])) * inv_r;
-            const float au = amp * uu[jj];
-            accv[3 + jj] += da * e0.x + au * inner.x;
-            accv[3 + W + jj] += da * e0.y + au * inner.y;
-            accv[3 + 2 * W + jj] += 2.0f * amp * (da * n0 + au * c.kpm * n1);
-            if (W == 6) {
-              const float acu = amp_cos * uu[jj];
-              accv[6 + jj] += acu * e0.x;
-              accv[3 + W + 3 + jj] += acu * e0.y;
-              accv[3 + 2 * W + 3 + jj] += 2.0f * amp * acu * n0;
-            }
-          }
-        } else {  // VJP: Re(conj(w) dcorr) per coordinate, and corr for the weight
-#pragma unroll
-          for (int jj = 0; jj < 3; ++jj) {
-            const float da = (amp * uu[jj] + amp_cos * (cosv * uu[jj] - nv[jj])) * inv_r;
-            const float au = amp * uu[jj];
-            const float2 dcj = make_float2(da * e0.x + au * inner.x, da * e0.y + au * inner.y);
-            accv[jj] += ws.x * dcj.x + ws.y * dcj.y;
-            const float acu = amp_cos * uu[jj];
-            accv[3 + jj] += acu * (ws.x * e0.x + ws.y * e0.y);
-          }
-          accv[6] += amp * e0.x;
-          accv[7] += amp * e0.y;
-        }
-      }
+      const float uu[3] = {r[R_U], r[R_U + 1], r[R_U + 2]};
+      const float nv[3] = {nx, ny, nz};
+      chain_outputs<MODE>(c, amp, r[R_AMPC], r[R_COS], r[R_INVR], r[R_RATE], uu,
+                          make_float2(r[R_ROT], r[R_ROT + 1]), nv, ws, z0, z1, n0, n1, accv);
     }
     __syncwarp();
   }
@@ -618,38 +570,6 @@ __global__ void __launch_bounds__(128) reduce_kernel(Consts c, const float* __re
     float* p = partial + ((size_t)s * chunks + blockIdx.y) * NV;
 #pragma unroll
     for (int v = 0; v < NV; ++v) p[v] = live ? accv[v] : 0.0f;
-  }
-}
-
-// Double-precision, fixed-order sum of chunk partials; scatters to the outputs. A thread
-// owns one value of one candidate (adjacent threads take adjacent values, so a warp reads
-// whole partial records) and adds its chunks in order.
-template <int MODE>
-__global__ void chunk_sum_kernel(const float* __restrict__ partial, int S, int chunks,
-                                 float* __restrict__ o0, float* __restrict__ o1,
-                                 float* __restrict__ o2, float* __restrict__ o3) {
-  constexpr int NV = ModeInfo<MODE>::NV;
-  const long long index = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (index >= (long long)S * NV) return;
-  const int s = (int)(index / NV), v = (int)(index % NV);
-  const float* p = partial + (size_t)s * chunks * NV + v;
-  double t = 0.0;
-  for (int g = 0; g < chunks; ++g) t += (double)p[(size_t)g * NV];
-  const float out = (float)t;
-  if (MODE == 0) {  // corr [S,2], norm [S]
-    if (v < 2) o0[2 * s + v] = out;
-    else o1[s] = out;
-  } else if (MODE == 3) {  // grad centers [S,3], normals [S,3], weights [S,2]
-    if (v < 3) o0[3 * s + v] = out;
-    else if (v < 6) o1[3 * s + v - 3] = out;
-    else o2[2 * s + v - 6] = out;
-  } else {  // corr, norm, dcorr [S,W,2], dnorm [S,W]
-    constexpr int W = ModeInfo<MODE>::W;
-    if (v < 2) o0[2 * s + v] = out;
-    else if (v == 2) o1[s] = out;
-    else if (v < 3 + W) o2[((size_t)s * W + v - 3) * 2] = out;
-    else if (v < 3 + 2 * W) o2[((size_t)s * W + v - 3 - W) * 2 + 1] = out;
-    else o3[(size_t)s * W + v - 3 - 2 * W] = out;
   }
 }
 
@@ -780,14 +700,19 @@ __global__ void __launch_bounds__(128) jacobian_kernel(Consts c, const float* __
 // correlation in parallel (from the exact bin sum, or by Catmull-Rom interpolation of an
 // oversampled FFT range table) into a per-warp record; then each lane takes one normal
 // of the bank (lane 0 of the first chunk: the candidate's own normal) and adds the 32
-// apertures in order. Every sum runs over apertures in ascending order, so the result
-// is fixed; a lane holds three accumulators, not three per normal, which keeps the
-// kernel at full occupancy.
+// apertures two at a time with packed FP32x2 arithmetic (fma.rn.f32x2: one instruction
+// for an even and an odd aperture), so the bank phase issues about half the
+// instructions of a scalar loop. The even and the odd apertures are summed in ascending
+// order in the two halves and the halves added at the end, so the result is fixed; a
+// lane holds three packed accumulators, not three per normal, which keeps the kernel at
+// full occupancy.
 // ------------------------------------------------------------------------------------
 constexpr int kOrientWarps = 8;
-// per aperture: ux, uy, uz, pad, path corr.re, path corr.im, path^2 norm, pad, with
-// path = lambda / (8 pi r); the amplitude of a normal is then path cos^2 F(cos).
-constexpr int kOrientRec = 8;
+// per aperture 6 floats: ux, uy, uz, path corr.re, path corr.im, path^2 norm, with
+// path = lambda / (8 pi r); the amplitude of a normal is then path cos^2 F(cos). An
+// aperture pair (2i, 2i + 1) is stored as 12 floats, each quantity's even value beside
+// its odd one: [ux ux uy uy | uz uz cr cr | ci ci nn nn], three 16-byte loads.
+constexpr int kOrientRec = 6;
 
 // cos^2 F(cos) for cos > 0, else 0 (the angular part of the scattering amplitude).
 template <bool FRESNEL>
@@ -835,7 +760,8 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
       ey = __ldg(bank + 3 * (j - 1) + 1);
       ez = __ldg(bank + 3 * (j - 1) + 2);
     }
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f;
+    const float2 ex2 = make_float2(ex, ex), ey2 = make_float2(ey, ey), ez2 = make_float2(ez, ez);
+    float2 acc0 = make_float2(0.f, 0.f), acc1 = acc0, acc2 = acc0;
     for (int a0 = 0; a0 < A; a0 += 32) {
       const int a = a0 + lane;
       if (a < A) {
@@ -890,28 +816,45 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
           norm = n0;
         }
         const float path = c.amp_scale * q.inv_r;
-        *reinterpret_cast<float4*>(rec + lane * kOrientRec) = make_float4(q.ux, q.uy, q.uz, 0.0f);
-        *reinterpret_cast<float4*>(rec + lane * kOrientRec + 4) =
-            make_float4(path * corr.x, path * corr.y, path * path * norm, 0.0f);
+        float* slot = rec + (lane >> 1) * 12 + (lane & 1);
+        slot[0] = q.ux;
+        slot[2] = q.uy;
+        slot[4] = q.uz;
+        slot[6] = path * corr.x;
+        slot[8] = path * corr.y;
+        slot[10] = path * path * norm;
+      } else {  // past the last aperture: a zero record adds nothing to the odd half
+        float* slot = rec + (lane >> 1) * 12 + (lane & 1);
+#pragma unroll
+        for (int k = 0; k < 12; k += 2) slot[k] = 0.0f;
       }
       __syncwarp();
-      const int count = min(32, A - a0);
-#pragma unroll 4
-      for (int i = 0; i < count; ++i) {
-        const float4 g = *reinterpret_cast<const float4*>(rec + i * kOrientRec);
-        const float4 v = *reinterpret_cast<const float4*>(rec + i * kOrientRec + 4);
-        const float cosv = g.x * ex + g.y * ey + g.z * ez;
-        const float a = bank_angular<FRESNEL>(c, cosv);
-        acc0 += a * v.x;
-        acc1 += a * v.y;
-        acc2 += a * a * v.z;
+      const int pairs = (min(32, A - a0) + 1) >> 1;
+#pragma unroll 2
+      for (int i = 0; i < pairs; ++i) {
+        const float4 g0 = *reinterpret_cast<const float4*>(rec + i * 12);
+        const float4 g1 = *reinterpret_cast<const float4*>(rec + i * 12 + 4);
+        const float4 g2 = *reinterpret_cast<const float4*>(rec + i * 12 + 8);
+        float2 cosv = __fmul2_rn(make_float2(g0.x, g0.y), ex2);
+        cosv = __ffma2_rn(make_float2(g0.z, g0.w), ey2, cosv);
+        cosv = __ffma2_rn(make_float2(g1.x, g1.y), ez2, cosv);
+        float2 a;
+        if (FRESNEL) {
+          a = make_float2(bank_angular<true>(c, cosv.x), bank_angular<true>(c, cosv.y));
+        } else {  // cos^2 where cos > 0, else 0 (fmaxf also maps NaN to 0)
+          a = make_float2(fmaxf(cosv.x, 0.0f), fmaxf(cosv.y, 0.0f));
+          a = __fmul2_rn(a, a);
+        }
+        acc0 = __ffma2_rn(a, make_float2(g1.z, g1.w), acc0);
+        acc1 = __ffma2_rn(a, make_float2(g2.x, g2.y), acc1);
+        acc2 = __ffma2_rn(__fmul2_rn(a, a), make_float2(g2.z, g2.w), acc2);
       }
       __syncwarp();
     }
     if (j < normals) {
-      o[3 * j] = acc0;
-      o[3 * j + 1] = acc1;
-      o[3 * j + 2] = acc2;
+      o[3 * j] = acc0.x + acc0.y;
+      o[3 * j + 1] = acc1.x + acc1.y;
+      o[3 * j + 2] = acc2.x + acc2.y;
     }
   }
 }
@@ -924,12 +867,6 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
 using namespace dsg;
 
 namespace {
-
-// CTAs the segment / chunk splits aim for: 152 SMs x (DSG_TUNE_SPLAT_CTAS_PER_SM, default 6).
-int target_ctas() {
-  const int per_sm = dsg_tuning_value(DSG_TUNE_SPLAT_CTAS_PER_SM);
-  return 152 * (per_sm > 0 ? per_sm : 6);
-}
 
 bool chirp_ok(const DsgChirp* c) {
   if (!c) return false;
@@ -1251,16 +1188,31 @@ int dsg_surfel_render_scenes(const DsgRenderScene* scenes, int32_t count, void* 
   return launch_status();
 }
 
+// Chunk partials of the exact (bin-sum) form.
+static size_t exact_workspace_bytes(int32_t apertures, int32_t surfels, int32_t values_per_surfel) {
+  return (size_t)surfels * reduce_chunks(apertures, surfels) * values_per_surfel * sizeof(float);
+}
+
+// Both forms fit: the interpolated form (the default) also holds the aperture tables.
 size_t dsg_surfel_reduce_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels,
                                          int32_t values_per_surfel) {
   if (!chirp_ok(chirp) || apertures <= 0 || surfels <= 0 || values_per_surfel <= 0) return 0;
-  return (size_t)surfels * reduce_chunks(apertures, surfels) * values_per_surfel * sizeof(float);
+  const size_t exact = exact_workspace_bytes(apertures, surfels, values_per_surfel);
+  const size_t interp = interp_workspace_bytes(make_consts(*chirp), apertures, surfels, values_per_surfel);
+  return exact > interp ? exact : interp;
+}
+
+// The interpolated form unless the caller needs the exact one (fixed scratch) or the
+// DSG_TUNE_CORRELATION_FORM knob selects it.
+static bool use_interp(bool allowed) {
+  return allowed && dsg_tuning_value(DSG_TUNE_CORRELATION_FORM) != DSG_CORRELATION_EXACT;
 }
 
 static int reduce_common(int mode, const DsgChirp* chirp, const float* positions, int32_t A,
                          const float* centers, const float* normals, const float* weights,
                          int32_t S, const float* residual, float* o0, float* o1, float* o2,
-                         float* o3, void* workspace, size_t workspace_bytes, void* stream) {
+                         float* o3, void* workspace, size_t workspace_bytes, void* stream,
+                         bool interp_allowed = true) {
   if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
   if (A < 0 || S < 0) return DSG_ERR_ARGUMENT;
   cudaStream_t st = (cudaStream_t)stream;
@@ -1280,11 +1232,14 @@ static int reduce_common(int mode, const DsgChirp* chirp, const float* positions
     return launch_status();
   }
   if (!positions || !residual) return DSG_ERR_ARGUMENT;
-  const size_t need = dsg_surfel_reduce_workspace_bytes(chirp, A, S, nv);
-  if (workspace == nullptr || workspace_bytes < need) return DSG_ERR_WORKSPACE;
   const Consts c = make_consts(*chirp);
   const float2* w = reinterpret_cast<const float2*>(weights);
   const float2* res = reinterpret_cast<const float2*>(residual);
+  if (use_interp(interp_allowed))
+    return interp_reduce(mode, c, positions, A, centers, normals, w, S, res, workspace, workspace_bytes,
+                         o0, o1, o2, o3, nullptr, 1, st);
+  const size_t need = exact_workspace_bytes(A, S, nv);
+  if (workspace == nullptr || workspace_bytes < need) return DSG_ERR_WORKSPACE;
   float* part = reinterpret_cast<float*>(workspace);
   switch (mode) {
     case 0: { ReduceLaunch<0> L{c, positions, A, centers, normals, w, S, res, part, o0, o1, o2, o3, st};
@@ -1329,9 +1284,13 @@ int dsg_surfel_correlate_active(const DsgChirp* chirp, const float* positions, i
     return reduce_common(0, chirp, positions, apertures, centers, normals, nullptr, candidates,
                          residual, corr, norm, nullptr, nullptr, workspace, workspace_bytes, stream);
   if (!positions || !residual || !centers || !normals || !corr || !norm) return DSG_ERR_ARGUMENT;
-  const size_t need = dsg_surfel_reduce_workspace_bytes(chirp, apertures, candidates, 3);
-  if (workspace == nullptr || workspace_bytes < need) return DSG_ERR_WORKSPACE;
   const Consts c = make_consts(*chirp);
+  if (use_interp(true))
+    return interp_reduce(0, c, positions, apertures, centers, normals, nullptr, candidates,
+                         reinterpret_cast<const float2*>(residual), workspace, workspace_bytes, corr, norm,
+                         nullptr, nullptr, active, period, (cudaStream_t)stream);
+  const size_t need = exact_workspace_bytes(apertures, candidates, 3);
+  if (workspace == nullptr || workspace_bytes < need) return DSG_ERR_WORKSPACE;
   ReduceLaunch<0> L{c, positions, apertures, centers, normals, nullptr, candidates,
                     reinterpret_cast<const float2*>(residual), reinterpret_cast<float*>(workspace),
                     corr, norm, nullptr, nullptr, (cudaStream_t)stream};
@@ -1498,6 +1457,8 @@ int vjp_scratch_address(void** out) {
 
 }  // namespace
 
+unsigned long long dsg_current_context_id() { return current_context_id(); }
+
 extern "C" int dsg_surfel_vjp_fixed_scratch(const DsgChirp* chirp, const float* positions,
                                             int32_t apertures, const float* centers,
                                             const float* normals, const float* weights,
@@ -1507,13 +1468,14 @@ extern "C" int dsg_surfel_vjp_fixed_scratch(const DsgChirp* chirp, const float* 
   if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
   if (apertures < 0 || surfels < 0) return DSG_ERR_ARGUMENT;
   if (surfels > 0 && (!weights || !grad_weights)) return DSG_ERR_ARGUMENT;
-  const size_t need = dsg_surfel_reduce_workspace_bytes(chirp, apertures, surfels, 8);
-  if (need > DSG_VJP_SCRATCH_MAX_BYTES) return DSG_ERR_WORKSPACE;
+  // the exact form: its chunk partials are all the scratch it needs
+  if (apertures > 0 && exact_workspace_bytes(apertures, surfels, 8) > DSG_VJP_SCRATCH_MAX_BYTES)
+    return DSG_ERR_WORKSPACE;
   if (surfels == 0) return DSG_OK;
   void* scratch = nullptr;
   const int status = vjp_scratch_address(&scratch);
   if (status != DSG_OK) return status;
   return reduce_common(3, chirp, positions, apertures, centers, normals, weights, surfels,
                        upstream, grad_centers, grad_normals, grad_weights, nullptr, scratch,
-                       DSG_VJP_SCRATCH_MAX_BYTES, stream);
+                       DSG_VJP_SCRATCH_MAX_BYTES, stream, /*interp_allowed=*/false);
 }

@@ -9,6 +9,8 @@ Complex gradients follow PyTorch: dL/dx = Re(conj(upstream) dy/dx).
 
 from __future__ import annotations
 
+from contextlib import contextmanager
+
 import torch
 from torch.autograd.function import once_differentiable
 
@@ -23,6 +25,25 @@ FLOPS_PER_UNIT = {
     "dsg_surfel_correlate_active": 18, "dsg_surfel_correlate_gradient": 30,
     "dsg_surfel_correlate_orientations": 12,
 }  # fmt: skip
+
+
+# DSG_TUNE_CORRELATION_FORM: how correlate, correlate_active, correlate_gradient and vjp
+# evaluate their sums over range bins.
+CORRELATION_FORMS = {"auto": 0, "exact": 1, "interp": 2}
+_CORRELATION_FORM_KNOB = 3
+
+
+@contextmanager
+def correlation_form(name):
+    """Inside the block the aperture-reduced kernels use form name: "interp" (the default:
+    per-pair statistics interpolated from per-aperture tables, a type-2 nonuniform FFT)
+    or "exact" (the closed-form kernel summed over every bin)."""
+    previous = int(_lib.library().dsg_tuning_get(_CORRELATION_FORM_KNOB))
+    call("dsg_tuning_set", _CORRELATION_FORM_KNOB, CORRELATION_FORMS[name])
+    try:
+        yield
+    finally:
+        call("dsg_tuning_set", _CORRELATION_FORM_KNOB, previous)
 
 
 def _work(name, units):

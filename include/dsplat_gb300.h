@@ -76,11 +76,20 @@ uint64_t dsg_launch_count(void);
  *                               deepest ring that fits shared memory; 2..4, capped at that)
  *   DSG_TUNE_ORIENT_WARPS       dsg_surfel_correlate_orientations warps per CTA (automatic:
  *                               8; 1..8)
+ *   DSG_TUNE_CORRELATION_FORM   how dsg_surfel_correlate(_active, _gradient) and
+ *                               dsg_surfel_vjp evaluate their sums over range bins:
+ *                               DSG_CORRELATION_INTERP (automatic) interpolates each pair's
+ *                               statistics from per-aperture tables (a type-2 nonuniform FFT,
+ *                               ~1e-7 relative to the exact sums); DSG_CORRELATION_EXACT sums
+ *                               the closed-form kernel over every bin
  * Knobs are process-wide; set them between launches, not while another thread launches. */
 #define DSG_TUNE_SPLAT_CTAS_PER_SM 0
 #define DSG_TUNE_PROJECT_STAGES 1
 #define DSG_TUNE_ORIENT_WARPS 2
-#define DSG_TUNE_COUNT 3
+#define DSG_TUNE_CORRELATION_FORM 3
+#define DSG_TUNE_COUNT 4
+#define DSG_CORRELATION_EXACT 1
+#define DSG_CORRELATION_INTERP 2
 int dsg_tuning_set(int32_t knob, int32_t value);
 /* Current value of a knob (0: automatic), or -1 for an unknown knob. */
 int32_t dsg_tuning_get(int32_t knob);
@@ -134,7 +143,12 @@ int dsg_surfel_jvp(const DsgChirp* chirp, const float* positions, int32_t apertu
                    const float* delta_weights, int32_t surfels, float* out, void* workspace,
                    size_t workspace_bytes, void* stream);
 
-/* Workspace of the aperture-reduced kernels (vjp, correlate, correlate_gradient). */
+/* Workspace of the aperture-reduced kernels (vjp, correlate, correlate_gradient), for
+ * either DSG_TUNE_CORRELATION_FORM. The interpolated form keeps per-aperture tables here
+ * (apertures x 2 n_fft / pad complex values, twice that with derivatives) and reads fixed
+ * per-chirp tables that the library builds on the host and uploads at the first call
+ * with that chirp's samples, pad and bins on a device and context (one cudaMalloc and a
+ * synchronous copy): make that first call before any stream capture. */
 size_t dsg_surfel_reduce_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels,
                                          int32_t values_per_surfel);
 
@@ -147,6 +161,15 @@ int dsg_surfel_vjp(const DsgChirp* chirp, const float* positions, int32_t apertu
                    float* grad_normals, float* grad_weights, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* The fixed tables of the interpolated form (DSG_TUNE_CORRELATION_FORM) for a chirp of
+ * `samples` ADC samples (a power of two, at least 8) and zero-padding factor `pad`, built
+ * on the host in double precision and returned as float32, without a GPU: correlation
+ * [K][2 samples][2] complex interleaved (K = samples pad / 2 bins; per grid cell the
+ * coefficients of Z0 and of Z1), norm [4 samples][2] (per grid cell the coefficients of
+ * N0 and N1). For checks of the tables; the kernels build their own. */
+int dsg_surfel_interp_tables(int32_t samples, int32_t pad, float* correlation, size_t correlation_floats,
+                             float* norm, size_t norm_floats);
+
 /* Upper bound of the fixed device scratch of dsg_surfel_vjp_fixed_scratch (4 MiB per GPU). */
 #define DSG_VJP_SCRATCH_MAX_BYTES ((size_t)4 << 20)
 
@@ -155,8 +178,9 @@ int dsg_surfel_vjp(const DsgChirp* chirp, const float* positions, int32_t apertu
  * acceptable to them). No counterpart in the reference. Same inputs, outputs and results
  * as dsg_surfel_vjp, but no workspace argument: the chunk partials go to one fixed
  * scratch array of DSG_VJP_SCRATCH_MAX_BYTES in the library, held by every GPU that
- * loads it until the process exits. Returns DSG_ERR_WORKSPACE, without launching, when
- * dsg_surfel_reduce_workspace_bytes(chirp, apertures, surfels, 8) exceeds that bound
+ * loads it until the process exits. It always sums over bins (the exact form of
+ * DSG_TUNE_CORRELATION_FORM), whose chunk partials are surfels x 8 floats per aperture
+ * chunk; it returns DSG_ERR_WORKSPACE, without launching, when they exceed that bound
  * (with the 152-SM grid sizing that is above about 131k surfels). The first call on a
  * device looks up the scratch address there (and may load the module), so make it
  * before any stream capture on that device; the address is remembered per device and

@@ -89,7 +89,7 @@ def test_range_response_matches_the_oracle():
 @pytest.mark.parametrize("dimension,separation", [(1, 0.002), (2, 0.03), (3, 0.02), (4, 0.3)])
 def test_peaks_in_every_dimension_and_dense_clusters(dimension, separation):
     """Clustered candidates (many suppressed, many taken), up to the 4096-peak limit; one to
-    three dimensions take the hashed single-warp kernel, four the block kernel."""
+    three dimensions look up the taken peaks in the kernel's cell hash, four scan them all."""
     from dsplat.kernels import search
 
     generator = torch.Generator().manual_seed(dimension)
