@@ -13,6 +13,9 @@ kernel    Dirichlet kernel and windows (tests/reference/kernel.py:8-57)
 fmcw      surfel columns, analytic derivatives, render / JVP / VJP / correlations,
           ADC synthesis (dsplat/groundtruth.py:40-90, tests/reference/oracle.py:34-41,
           dsplat/kernels/scattering.slang:16-50)
+adjoint   the reference VJP kernel's hand-derived adjoint (per-class cotangent sums, nearest
+          bin apart, chain rule; dsplat/kernels/surfel.slang:227-311) in float64, pinned to
+          autograd of the closed form by tests/test_oracle_adjoint.py
 spectral  separable atoms and derivatives (tests/reference/oracle.py:10-31)
 search    range gate, greedy peaks, quasi-Newton direction and trial step
           (dsplat/kernels/search.slang:7-109)

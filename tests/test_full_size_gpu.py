@@ -20,6 +20,7 @@ import pytest
 import torch
 from conftest import rel_l2
 
+from oracle import adjoint as oadjoint
 from oracle import fmcw as ofmcw
 
 pytestmark = pytest.mark.gpu
@@ -75,6 +76,19 @@ def test_full_array_vjp_matches_float64_autograd_on_the_subset(cap):
     upstream = _upstream(index, config.num_range_bins)
     gc, gn, gw = kernel.vjp(config, positions, params["centers"], params["normals"], weights, upstream.cuda(), 0.0)
     ec, en, ew = ofmcw.vjp(config, *_oracle_inputs(positions, params, weights, index), upstream[index.cpu()])
+    assert rel_l2(gc, ec) < DERIV_TOL
+    assert rel_l2(gn, en) < DERIV_TOL
+    assert rel_l2(gw, ew) < DERIV_TOL
+
+
+def test_full_array_vjp_matches_the_reference_adjoint_formulas(cap):
+    """The CUDA VJP against the reference VJP kernel's own formulas evaluated in float64."""
+    from dsplat.kernels import surfel as kernel
+
+    config, positions, params, weights, index = cap
+    upstream = _upstream(index, config.num_range_bins, seed=7)
+    gc, gn, gw = kernel.vjp(config, positions, params["centers"], params["normals"], weights, upstream.cuda(), 0.0)
+    ec, en, ew = oadjoint.vjp(config, *_oracle_inputs(positions, params, weights, index), upstream[index.cpu()])
     assert rel_l2(gc, ec) < DERIV_TOL
     assert rel_l2(gn, en) < DERIV_TOL
     assert rel_l2(gw, ew) < DERIV_TOL

@@ -11,6 +11,7 @@ import pytest
 import torch
 from conftest import aperture_grid, close, rel_l2, surfels
 
+from oracle import adjoint as oadjoint
 from oracle import fmcw as ofmcw
 
 pytestmark = pytest.mark.gpu
@@ -194,6 +195,10 @@ def test_vjp_near_the_peak_and_across_pads(pad):
     ec, en, ew = ofmcw.vjp(config, positions.cpu(), params["centers"].cpu(), params["normals"].cpu(),
                            w.cpu(), upstream.cpu())  # fmt: skip
     assert rel_l2(gc, ec) < DERIV_TOL and rel_l2(gn, en) < DERIV_TOL and rel_l2(gw, ew) < DERIV_TOL
+    # the reference VJP kernel's own formulas (class sums, nearest bin apart) in float64
+    ac, an, aw = oadjoint.vjp(config, positions.cpu(), params["centers"].cpu(), params["normals"].cpu(),
+                              w.cpu(), upstream.cpu())  # fmt: skip
+    assert rel_l2(gc, ac) < DERIV_TOL and rel_l2(gn, an) < DERIV_TOL and rel_l2(gw, aw) < DERIV_TOL
     dc = torch.randn_like(params["centers"]) * 1e-4
     dn = torch.randn_like(params["normals"]) * 1e-2
     dw = _weights(9, seed=5)
