@@ -124,7 +124,7 @@ def _fusable(model, params, fractions):
             and 1 <= len(fractions) <= 16)  # fmt: skip
 
 
-def _fused_iteration(model, residual, power, controls, specs, config, mode, fractions):
+def _fused_iteration(model, residual, power, controls, specs, config, mode, fractions, tables=None):
     """One batched ascent iteration on the state buffers, in place, in eight launches.
 
     The correlations run on the surfel kernels without the area factors, which the
@@ -137,6 +137,10 @@ def _fused_iteration(model, residual, power, controls, specs, config, mode, frac
     did not change, so the same trials fail again in every later iteration (the kernels
     are deterministic); they are kept out of the active set, which removes most of the
     backtracking work once the ascent converges, without changing any result.
+
+    tables (kernel.residual_tables of the residual, with derivative) lets the three
+    correlations of every iteration read the residual's interpolation tables instead of
+    rebuilding them from the residual (bitwise the same results).
     """
     from .kernels import surfel as kernel
 
@@ -150,19 +154,20 @@ def _fused_iteration(model, residual, power, controls, specs, config, mode, frac
         centers, normals, areas = params["centers"], params["normals"], params["areas"]
         direction = search.direction(inverse, grad, normals, controls[1], config.trust_radius)
         trial_centers, trial_normals = search.trials(centers, normals, direction, controls, fractions)
-        corr, norm = kernel.correlate(chirp, positions, trial_centers[0], trial_normals[0], shaped, model.fresnel_n)
+        corr, norm = kernel.correlate(chirp, positions, trial_centers[0], trial_normals[0], shaped, model.fresnel_n,
+                                      tables=tables)  # fmt: skip
         improved, position, pending, batch_centers, batch_normals = search.ascent_partition(
             corr, norm, areas, power, real_mode, value, trial_centers, trial_normals, stuck)  # fmt: skip
         corr2 = norm2 = None
         if len(fractions) > 1:
             corr2, norm2 = kernel.correlate(chirp, positions, batch_centers, batch_normals, shaped, model.fresnel_n,
-                                            active=(pending, len(value)))  # fmt: skip
+                                            active=(pending, len(value)), tables=tables)  # fmt: skip
         new_centers, new_normals, accepted = search.ascent_select(
             corr2, norm2, areas, power, real_mode, value, improved, position, trial_centers, trial_normals,
             centers, normals, move_normals, stuck)  # fmt: skip
         stuck.copy_(stuck | (accepted == 0).to(torch.uint8))
         c, n, dc, dn = kernel.correlate_gradient(chirp, positions, new_centers, new_normals, shaped, model.fresnel_n,
-                                                 move_normals)  # fmt: skip
+                                                 move_normals, tables=tables)  # fmt: skip
         search.ascent_update(spec, c, n, dc, dn, areas, power, real_mode, new_centers, new_normals, accepted,
                              centers, normals, value, grad, inverse)  # fmt: skip
 
@@ -178,9 +183,11 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
     replays it, a later one replays every iteration.
     """
     from .kernels import _lib
+    from .kernels import surfel as kernel
 
     positions = model.scan.scan_positions_m
-    key = ("fused", repr(model.scan.fmcw_config), model.fresnel_n, tuple(positions.shape), tuple(residual.shape),
+    tabled = kernel.interpolated()
+    key = ("fused", tabled, repr(model.scan.fmcw_config), model.fresnel_n, tuple(positions.shape), tuple(residual.shape),
            residual.dtype, mode, repr(specs), repr(config), tuple(fractions), positions.device,
            tuple((k, tuple(v.shape)) for k, v in params.items()), tuple(grad.shape))  # fmt: skip
     power = residual.abs().square().sum().double().clamp(min=1e-30).reshape(1)
@@ -189,6 +196,8 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
         graph, inputs, state, per_replay = entry
         inputs["positions"].copy_(positions)
         inputs["residual"].copy_(residual)
+        if tabled:  # once per search: every iteration's correlations read them
+            kernel.residual_tables(model.sensor[0], inputs["residual"].reshape(model.shape), out=inputs["tables"])
         inputs["controls"].copy_(controls)
         inputs["power"].copy_(power)
         inputs["stuck"].zero_()
@@ -205,11 +214,13 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
         inputs = {"positions": positions.clone(), "residual": residual.contiguous().clone(),
                   "controls": controls.contiguous().clone(), "power": power.clone(),
                   "stuck": torch.zeros(len(value), dtype=torch.uint8, device=value.device)}  # fmt: skip
+        inputs["tables"] = (kernel.residual_tables(model.sensor[0], inputs["residual"].reshape(model.shape))
+                            if tabled else None)  # fmt: skip
         state = ({k: v.float().contiguous().clone() for k, v in params.items()}, value.float().contiguous().clone(),
                  grad.float().contiguous().clone(), inverse.float().contiguous().clone())  # fmt: skip
         static_model = replace(model, scan=replace(model.scan, scan_positions_m=inputs["positions"]))
         iterate = _fused_iteration(static_model, inputs["residual"], inputs["power"], inputs["controls"], specs,
-                                   config, mode, fractions)  # fmt: skip
+                                   config, mode, fractions, inputs["tables"])  # fmt: skip
         device = value.device
         side = torch.cuda.Stream(device)
         side.wait_stream(torch.cuda.current_stream(device))

@@ -444,10 +444,49 @@ int launch_interp(const Consts& c, const float* pos, int A, const float* cen, co
 
 }  // namespace
 
+size_t interp_partial_bytes(int A, int S, int nv) {
+  return align_up((size_t)S * interp_chunks(A, S) * nv * sizeof(float));
+}
+
+size_t interp_tables_bytes(const Consts& c, int A, bool derivative) {
+  return (size_t)A * (2 * c.S) * (derivative ? 2 : 1) * sizeof(float2);
+}
+
 size_t interp_workspace_bytes(const Consts& c, int A, int S, int nv) {
-  const int nt = nv == 3 ? 1 : 2;
-  const size_t partial = (size_t)S * interp_chunks(A, S) * nv * sizeof(float);
-  return align_up(partial) + (size_t)A * (2 * c.S) * nt * sizeof(float2);
+  return interp_partial_bytes(A, S, nv) + interp_tables_bytes(c, A, nv != 3);
+}
+
+int interp_residual_tables(const Consts& c, const float2* res, int A, bool derivative, float2* tables,
+                           cudaStream_t st) {
+  DeviceTables fixed;
+  const int status = device_tables(c.S, c.P, &fixed);
+  if (status != DSG_OK) return status;
+  const int M = 2 * c.S;
+  // u0 [A][M] = residual [A][K] . H0 [K][M], then u1 with H1: one GEMM gives u0 to every mode
+  int out = table_gemm(res, A, c.K, fixed.h0, M, tables, st);
+  if (out == DSG_OK && derivative) out = table_gemm(res, A, c.K, fixed.h1, M, tables + (size_t)A * M, st);
+  return out;
+}
+
+int interp_reduce_tabled(int mode, const Consts& c, const float* pos, int A, const float* cen, const float* nrm,
+                         const float2* w, int S, const float2* tables, void* workspace, size_t workspace_bytes,
+                         float* o0, float* o1, float* o2, float* o3, const int* active, int period,
+                         cudaStream_t st) {
+  const int nv = nv_of(mode);
+  if (workspace == nullptr || workspace_bytes < interp_partial_bytes(A, S, nv)) return DSG_ERR_WORKSPACE;
+  DeviceTables fixed;
+  const int status = device_tables(c.S, c.P, &fixed);
+  if (status != DSG_OK) return status;
+  const int M = 2 * c.S, M0 = 4 * c.S;
+  float* partial = reinterpret_cast<float*>(workspace);
+  const float2* u0 = tables;
+  const float2* u1 = tables + (size_t)A * M;  // read by the derivative modes only
+  switch (mode) {
+    case 0: return launch_interp<0>(c, pos, A, cen, nrm, w, S, u0, u1, M, fixed.norm, M0, partial, o0, o1, o2, o3, active, period, st);
+    case 1: return launch_interp<1>(c, pos, A, cen, nrm, w, S, u0, u1, M, fixed.norm, M0, partial, o0, o1, o2, o3, active, period, st);
+    case 2: return launch_interp<2>(c, pos, A, cen, nrm, w, S, u0, u1, M, fixed.norm, M0, partial, o0, o1, o2, o3, active, period, st);
+    default: return launch_interp<3>(c, pos, A, cen, nrm, w, S, u0, u1, M, fixed.norm, M0, partial, o0, o1, o2, o3, active, period, st);
+  }
 }
 
 int interp_reduce(int mode, const Consts& c, const float* pos, int A, const float* cen, const float* nrm,
@@ -456,25 +495,12 @@ int interp_reduce(int mode, const Consts& c, const float* pos, int A, const floa
                   cudaStream_t st) {
   const int nv = nv_of(mode);
   if (workspace == nullptr || workspace_bytes < interp_workspace_bytes(c, A, S, nv)) return DSG_ERR_WORKSPACE;
-  DeviceTables tables;
-  const int status = device_tables(c.S, c.P, &tables);
+  const size_t partial_bytes = interp_partial_bytes(A, S, nv);
+  float2* tables = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + partial_bytes);
+  const int status = interp_residual_tables(c, res, A, mode != 0, tables, st);
   if (status != DSG_OK) return status;
-  const int M = 2 * c.S, M0 = 4 * c.S;
-  float* partial = reinterpret_cast<float*>(workspace);
-  float2* u0 = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) +
-                                         align_up((size_t)S * interp_chunks(A, S) * nv * sizeof(float)));
-  float2* u1 = u0 + (size_t)A * M;
-  // u0 [A][M] = residual [A][K] . H0 [K][M], and u1 with H1 when the mode takes derivatives:
-  // the same GEMM gives u0 to every mode
-  int status2 = table_gemm(res, A, c.K, tables.h0, M, u0, st);
-  if (status2 == DSG_OK && mode != 0) status2 = table_gemm(res, A, c.K, tables.h1, M, u1, st);
-  if (status2 != DSG_OK) return status2;
-  switch (mode) {
-    case 0: return launch_interp<0>(c, pos, A, cen, nrm, w, S, u0, u1, M, tables.norm, M0, partial, o0, o1, o2, o3, active, period, st);
-    case 1: return launch_interp<1>(c, pos, A, cen, nrm, w, S, u0, u1, M, tables.norm, M0, partial, o0, o1, o2, o3, active, period, st);
-    case 2: return launch_interp<2>(c, pos, A, cen, nrm, w, S, u0, u1, M, tables.norm, M0, partial, o0, o1, o2, o3, active, period, st);
-    default: return launch_interp<3>(c, pos, A, cen, nrm, w, S, u0, u1, M, tables.norm, M0, partial, o0, o1, o2, o3, active, period, st);
-  }
+  return interp_reduce_tabled(mode, c, pos, A, cen, nrm, w, S, tables, workspace, partial_bytes, o0, o1, o2, o3,
+                              active, period, st);
 }
 
 }  // namespace dsg

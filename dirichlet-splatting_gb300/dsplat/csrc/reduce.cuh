@@ -130,5 +130,16 @@ int interp_reduce(int mode, const Consts& c, const float* pos, int A, const floa
                   const float2* w, int S, const float2* res, void* workspace, size_t workspace_bytes,
                   float* o0, float* o1, float* o2, float* o3, const int* active, int period,
                   cudaStream_t st);
+// The two halves of interp_reduce, for callers that correlate one residual many times:
+// the residual's aperture tables [u0 | u1] (interp_tables_bytes; u1 only with derivative),
+// then any mode's outputs from them (workspace: interp_partial_bytes).
+size_t interp_partial_bytes(int A, int S, int nv);
+size_t interp_tables_bytes(const Consts& c, int A, bool derivative);
+int interp_residual_tables(const Consts& c, const float2* res, int A, bool derivative, float2* tables,
+                           cudaStream_t st);
+int interp_reduce_tabled(int mode, const Consts& c, const float* pos, int A, const float* cen, const float* nrm,
+                         const float2* w, int S, const float2* tables, void* workspace, size_t workspace_bytes,
+                         float* o0, float* o1, float* o2, float* o3, const int* active, int period,
+                         cudaStream_t st);
 
 }  // namespace dsg

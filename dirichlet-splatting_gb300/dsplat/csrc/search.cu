@@ -29,6 +29,7 @@ __global__ void range_gate_kernel(const float* __restrict__ points, int count,
 
 constexpr int kPeakThreads = 1024;
 constexpr int kMaxAccepted = 4096;  // peaks held in shared memory per launch
+constexpr int kChunkSlots = 2048;   // cells of one chunk's survivors (at most kPeakThreads)
 
 // Opt a kernel in to `dynamic` bytes of dynamic shared memory when that and its static
 // arrays exceed the default 48 KB.
@@ -51,8 +52,12 @@ bool allow_shared(Kernel kernel, size_t dynamic) {
 // In one to three dimensions the taken peaks are also filed in a shared-memory hash of
 // cells of side separation (1 + 2^-16), so a candidate looks only at the peaks of its own
 // and the 3^d - 1 neighbouring cells (any peak nearer than separation lies there) instead
-// of scanning every taken peak, and one warp resolves a chunk's survivors, a lane per
-// neighbouring cell, without a block barrier per taken peak; the selection is the same.
+// of scanning every taken peak. A chunk's survivors are then filed in a second hash of the
+// same cells and resolved in parallel rounds: a survivor is suppressed as soon as an
+// earlier survivor within separation is taken, and taken once every earlier survivor
+// within separation is suppressed. Each round settles at least the earliest open
+// survivor (all of its earlier neighbours are settled), so the rounds end, and the
+// decisions are those of the in-order greedy pass; the selection is the same.
 constexpr unsigned long long kEmptyCell = ~0ull;
 
 __device__ __forceinline__ int cell_of(float x, float inv_cell) {
@@ -72,7 +77,7 @@ __device__ __forceinline__ unsigned cell_slot(unsigned long long key, unsigned m
 struct PeakCells {
   unsigned long long* keys;  // [slots], kEmptyCell when free
   int* heads;                // [slots] first taken peak filed in the cell
-  int* next;                 // [peaks] next taken peak of the same cell, -1 at the end
+  int* next;                 // [peaks] next entry of the same cell, -1 at the end
   unsigned mask;             // slots - 1
   float inv_cell;
 };
@@ -81,27 +86,6 @@ __device__ __forceinline__ void cell_coords(const PeakCells& h, const float* c, 
   cc[0] = cell_of(c[0], h.inv_cell);
   cc[1] = dimension > 1 ? cell_of(c[1], h.inv_cell) : 0;
   cc[2] = dimension > 2 ? cell_of(c[2], h.inv_cell) : 0;
-}
-
-// Files taken peak `slot` (coordinates c) under its cell (one thread).
-__device__ void file_peak(const PeakCells& h, const float* c, int dimension, int slot) {
-  int cc[3];
-  cell_coords(h, c, dimension, cc);
-  const unsigned long long key = cell_key(cc[0], cc[1], cc[2]);
-  unsigned s = cell_slot(key, h.mask);
-  for (unsigned probe = 0; probe <= h.mask; ++probe, s = (s + 1) & h.mask) {
-    if (h.keys[s] == key) {
-      h.next[slot] = h.heads[s];
-      h.heads[s] = slot;
-      return;
-    }
-    if (h.keys[s] == kEmptyCell) {
-      h.keys[s] = key;
-      h.heads[s] = slot;
-      h.next[slot] = -1;
-      return;
-    }
-  }
 }
 
 // Whether a taken peak filed in the cell at offset (dx, dy, dz) from c's cell lies within
@@ -140,14 +124,66 @@ __device__ bool near_taken(const PeakCells& h, const float* c, int dimension, co
   return false;
 }
 
-__global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __restrict__ scores,
+// Files taken peak `slot` under its cell; any number of threads at once.
+__device__ __forceinline__ void file_peak_shared(const PeakCells& h, const float* c, int dimension, int slot) {
+  int cc[3];
+  cell_coords(h, c, dimension, cc);
+  const unsigned long long key = cell_key(cc[0], cc[1], cc[2]);
+  unsigned s = cell_slot(key, h.mask);
+  for (unsigned probe = 0; probe <= h.mask; ++probe, s = (s + 1) & h.mask) {
+    const unsigned long long seen = atomicCAS(&h.keys[s], kEmptyCell, key);
+    if (seen == kEmptyCell || seen == key) {
+      h.next[slot] = atomicExch(&h.heads[s], slot);
+      return;
+    }
+  }
+}
+
+// Settles survivor q of a chunk (chunk cells `cc` of the survivors, coordinates xyz[q]):
+// 1 taken, 2 suppressed, 0 still open (an earlier neighbour is open).
+__device__ __forceinline__ int settle_survivor(const PeakCells& h, const float* xyz, int dimension, int q, float sep2,
+                               const volatile int* state) {
+  int cc[3];
+  const float* c = xyz + q * 3;
+  cell_coords(h, c, dimension, cc);
+  const int ry = dimension > 1 ? 1 : 0, rz = dimension > 2 ? 1 : 0;
+  bool open = false;
+  for (int dz = -rz; dz <= rz; ++dz)
+    for (int dy = -ry; dy <= ry; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const unsigned long long key = cell_key(cc[0] + dx, cc[1] + dy, cc[2] + dz);
+        unsigned s = cell_slot(key, h.mask);
+        for (unsigned probe = 0; probe <= h.mask; ++probe, s = (s + 1) & h.mask) {
+          const unsigned long long k = h.keys[s];
+          if (k == kEmptyCell) break;
+          if (k != key) continue;
+          for (int t = h.heads[s]; t >= 0; t = h.next[t]) {
+            if (t >= q) continue;
+            float d2 = 0.0f;
+            for (int j = 0; j < dimension; ++j) {
+              const float d = c[j] - xyz[t * 3 + j];
+              d2 += d * d;
+            }
+            if (d2 < sep2) {
+              const int st = state[t];
+              if (st == 1) return 2;
+              if (st == 0) open = true;
+            }
+          }
+          break;
+        }
+      }
+  return open ? 0 : 1;
+}
+
+__global__ void __launch_bounds__(kPeakThreads, 1) peaks_kernel(const float* __restrict__ scores,
                                                              const int* __restrict__ order,
                                                              const float* __restrict__ centers,
                                                              int count, int dimension, int peaks,
                                                              float separation, int slots,
                                                              int* __restrict__ output) {
   extern __shared__ unsigned long long peak_smem[];
-  __shared__ float chunk_xyz[kPeakThreads * 3];  // hashed: the chunk's candidates, for warp 0
+  __shared__ float chunk_xyz[kPeakThreads * 3];  // hashed: the chunk's survivors' coordinates
   __shared__ int alive[kPeakThreads];
   __shared__ int alive_list[kPeakThreads];  // the chunk's survivors, in order
   __shared__ int warp_alive[kPeakThreads / 32];
@@ -160,9 +196,21 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
   cells.mask = (unsigned)slots - 1u;
   cells.inv_cell = 1.0f / (separation * (1.0f + 1.0f / 65536.0f));
   float* taken_xyz = reinterpret_cast<float*>(cells.next + (hashed ? peaks : 0));  // [peaks][dimension]
+  // hashed: the chunk's survivors filed by cell (kChunkSlots keys and heads, next per survivor)
+  PeakCells chunk_cells;
+  chunk_cells.keys = reinterpret_cast<unsigned long long*>(
+      (reinterpret_cast<uintptr_t>(taken_xyz + (size_t)peaks * dimension) + 7) & ~(uintptr_t)7);
+  chunk_cells.heads = reinterpret_cast<int*>(chunk_cells.keys + kChunkSlots);
+  chunk_cells.next = chunk_cells.heads + kChunkSlots;
+  chunk_cells.mask = kChunkSlots - 1u;
+  chunk_cells.inv_cell = cells.inv_cell;
+  int* state = alive;  // hashed: per survivor, 0 open, 1 taken, 2 suppressed
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float sep2 = separation * separation;
-  for (int i = tid; i < slots; i += kPeakThreads) cells.keys[i] = kEmptyCell;
+  for (int i = tid; i < slots; i += kPeakThreads) {
+    cells.keys[i] = kEmptyCell;
+    cells.heads[i] = -1;
+  }
   if (tid == 0) n_taken = 0;
   __syncthreads();
   for (int base = 0; base < count; base += kPeakThreads) {
@@ -201,38 +249,55 @@ __global__ void __launch_bounds__(kPeakThreads) peaks_kernel(const float* __rest
       survivors += warp_alive[w];
     }
     if (ok) alive_list[before] = tid;
-    if (hashed)
-      for (int j = 0; j < dimension; ++j) chunk_xyz[tid * 3 + j] = c[j];
     __syncthreads();
     if (hashed) {
-      // Warp 0 resolves the survivors in order: lane l probes neighbouring cell l (3^d of
-      // them) for a peak taken earlier in this chunk; a survivor nobody hits is taken and
-      // filed at once. No block barrier per taken peak.
-      if (warp == 0) {
-        const int ncells = dimension == 1 ? 3 : dimension == 2 ? 9 : 27;
-        const int dx = lane % 3 - 1, dy = dimension > 1 ? (lane / 3) % 3 - 1 : 0,
-                  dz = dimension > 2 ? lane / 9 - 1 : 0;
-        int taken = n_taken;
-        for (int q = 0; q < survivors && taken < peaks; ++q) {
-          const int k = alive_list[q];
-          const float* ck = chunk_xyz + k * 3;
-          bool hit = false;
-          if (lane < ncells) {
-            int cc[3];
-            cell_coords(cells, ck, dimension, cc);
-            hit = cell_hit(cells, ck, dimension, cc, dx, dy, dz, taken_xyz, sep2);
-          }
-          if (__any_sync(0xffffffffu, hit)) continue;
-          if (lane == 0) {
-            for (int j = 0; j < dimension; ++j) taken_xyz[taken * dimension + j] = ck[j];
-            output[taken] = order[base + k];
-            file_peak(cells, ck, dimension, taken);
-          }
-          ++taken;
-          __syncwarp();
-        }
-        if (lane == 0) n_taken = taken;
+      // survivor q's coordinates at q, its cell filed in the chunk hash; every survivor open
+      float* sxyz = chunk_xyz;
+      float mine[3] = {0.f, 0.f, 0.f};
+      if (ok)
+        for (int j = 0; j < dimension; ++j) mine[j] = c[j];
+      for (int i = tid; i < kChunkSlots; i += kPeakThreads) {
+        chunk_cells.keys[i] = kEmptyCell;
+        chunk_cells.heads[i] = -1;
       }
+      __syncthreads();
+      if (ok) {
+        for (int j = 0; j < dimension; ++j) sxyz[before * 3 + j] = mine[j];
+        state[before] = 0;
+      }
+      __syncthreads();
+      if (ok) file_peak_shared(chunk_cells, mine, dimension, before);
+      __syncthreads();
+      // rounds: each settles at least the earliest open survivor, so survivors + 1 bound them
+      for (int round = 0; round <= survivors; ++round) {
+        int open = 0;
+        if (tid < survivors && state[tid] == 0) {
+          const int verdict = settle_survivor(chunk_cells, sxyz, dimension, tid, sep2, state);
+          if (verdict != 0) state[tid] = verdict;
+          open = verdict == 0;
+        }
+        if (!__syncthreads_or(open)) break;
+      }
+      // the taken survivors in order, up to the peaks still wanted
+      const bool took = tid < survivors && state[tid] == 1;
+      const unsigned tb = __ballot_sync(0xffffffffu, took);
+      __syncthreads();  // every state read is done before warp_alive is rewritten
+      if (lane == 0) warp_alive[warp] = __popc(tb);
+      __syncthreads();
+      int rank = __popc(tb & ((1u << lane) - 1u)), total = 0;
+      for (int w = 0; w < kPeakThreads / 32; ++w) {
+        rank += w < warp ? warp_alive[w] : 0;
+        total += warp_alive[w];
+      }
+      const int room = peaks - taken_now;
+      if (took && rank < room) {
+        const int slot = taken_now + rank;
+        for (int j = 0; j < dimension; ++j) taken_xyz[slot * dimension + j] = sxyz[tid * 3 + j];
+        output[slot] = order[base + alive_list[tid]];
+        file_peak_shared(cells, sxyz + tid * 3, dimension, slot);
+      }
+      __syncthreads();
+      if (tid == 0) n_taken = taken_now + min(total, room);
       __syncthreads();
       continue;
     }
@@ -444,8 +509,11 @@ int dsg_peaks(const float* scores, const int32_t* order, const float* centers, i
     slots = 64;
     while (slots < 2 * peaks) slots <<= 1;
   }
-  const size_t smem = (size_t)slots * (sizeof(unsigned long long) + sizeof(int)) +
-                      (slots > 0 ? (size_t)peaks * sizeof(int) : 0) + (size_t)peaks * dimension * sizeof(float);
+  size_t smem = (size_t)slots * (sizeof(unsigned long long) + sizeof(int)) +
+                (slots > 0 ? (size_t)peaks * sizeof(int) : 0) + (size_t)peaks * dimension * sizeof(float);
+  if (slots > 0)  // the chunk's survivor hash, 8-byte aligned after the taken coordinates
+    smem = (smem + 7) / 8 * 8 + (size_t)kChunkSlots * (sizeof(unsigned long long) + sizeof(int)) +
+           (size_t)kPeakThreads * sizeof(int);
   if (!allow_shared(peaks_kernel, smem)) return DSG_ERR_LAUNCH;
   peaks_kernel<<<1, kPeakThreads, smem, (cudaStream_t)stream>>>(scores, order, centers, count, dimension,
                                                                peaks, separation, slots, output);

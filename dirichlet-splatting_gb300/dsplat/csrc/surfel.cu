@@ -1311,6 +1311,71 @@ int dsg_surfel_correlate_gradient(const DsgChirp* chirp, const float* positions,
                        workspace_bytes, stream);
 }
 
+size_t dsg_surfel_residual_tables_bytes(const DsgChirp* chirp, int32_t apertures, int32_t derivative) {
+  if (!chirp_ok(chirp) || apertures <= 0) return 0;
+  return interp_tables_bytes(make_consts(*chirp), apertures, derivative != 0);
+}
+
+int dsg_surfel_residual_tables(const DsgChirp* chirp, const float* residual, int32_t apertures,
+                               int32_t derivative, float* tables, size_t tables_bytes, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0) return DSG_ERR_ARGUMENT;
+  if (apertures == 0) return DSG_OK;
+  if (!residual || !tables) return DSG_ERR_ARGUMENT;
+  const Consts c = make_consts(*chirp);
+  if (tables_bytes < interp_tables_bytes(c, apertures, derivative != 0)) return DSG_ERR_WORKSPACE;
+  return interp_residual_tables(c, reinterpret_cast<const float2*>(residual), apertures, derivative != 0,
+                                reinterpret_cast<float2*>(tables), (cudaStream_t)stream);
+}
+
+size_t dsg_surfel_tabled_workspace_bytes(int32_t apertures, int32_t candidates, int32_t values_per_surfel) {
+  if (apertures <= 0 || candidates <= 0 || values_per_surfel <= 0) return 0;
+  return interp_partial_bytes(apertures, candidates, values_per_surfel);
+}
+
+int dsg_surfel_correlate_tabled(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                                const float* centers, const float* normals, int32_t candidates,
+                                const float* tables, const int32_t* active, int32_t period, float* corr,
+                                float* norm, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || candidates < 0 || (active && period < 1)) return DSG_ERR_ARGUMENT;
+  if (candidates == 0) return DSG_OK;
+  if (!centers || !normals || !corr || !norm) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (apertures == 0) {
+    cudaMemsetAsync(corr, 0, (size_t)candidates * 2 * sizeof(float), st);
+    cudaMemsetAsync(norm, 0, (size_t)candidates * sizeof(float), st);
+    return launch_status();
+  }
+  if (!positions || !tables) return DSG_ERR_ARGUMENT;
+  return interp_reduce_tabled(0, make_consts(*chirp), positions, apertures, centers, normals, nullptr, candidates,
+                              reinterpret_cast<const float2*>(tables), workspace, workspace_bytes, corr, norm,
+                              nullptr, nullptr, active, active ? period : 1, st);
+}
+
+int dsg_surfel_correlate_gradient_tabled(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                                         const float* centers, const float* normals, int32_t candidates,
+                                         const float* tables, int32_t width, float* corr, float* norm,
+                                         float* dcorr, float* dnorm, void* workspace, size_t workspace_bytes,
+                                         void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || candidates < 0 || (width != 3 && width != 6)) return DSG_ERR_ARGUMENT;
+  if (candidates == 0) return DSG_OK;
+  if (!centers || !normals || !corr || !norm || !dcorr || !dnorm) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (apertures == 0) {
+    cudaMemsetAsync(corr, 0, (size_t)candidates * 2 * sizeof(float), st);
+    cudaMemsetAsync(norm, 0, (size_t)candidates * sizeof(float), st);
+    cudaMemsetAsync(dcorr, 0, (size_t)candidates * width * 2 * sizeof(float), st);
+    cudaMemsetAsync(dnorm, 0, (size_t)candidates * width * sizeof(float), st);
+    return launch_status();
+  }
+  if (!positions || !tables) return DSG_ERR_ARGUMENT;
+  return interp_reduce_tabled(width == 3 ? 1 : 2, make_consts(*chirp), positions, apertures, centers, normals,
+                              nullptr, candidates, reinterpret_cast<const float2*>(tables), workspace,
+                              workspace_bytes, corr, norm, dcorr, dnorm, nullptr, 1, st);
+}
+
 int dsg_surfel_correlate_orientations(const DsgChirp* chirp, const float* positions,
                                       int32_t apertures, const float* centers,
                                       const float* normals, int32_t candidates, const float* bank,

@@ -97,6 +97,11 @@ SIGNATURES = {
     "dsg_surfel_vjp": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, P, P, P, SZ, P]),
     "dsg_surfel_vjp_fixed_scratch": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, P, P, P]),
     "dsg_surfel_interp_tables": (ctypes.c_int, [I32, I32, P, SZ, P, SZ]),
+    "dsg_surfel_residual_tables_bytes": (SZ, [CP, I32, I32]),
+    "dsg_surfel_residual_tables": (ctypes.c_int, [CP, P, I32, I32, P, SZ, P]),
+    "dsg_surfel_tabled_workspace_bytes": (SZ, [I32, I32, I32]),
+    "dsg_surfel_correlate_tabled": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, I32, P, P, P, SZ, P]),
+    "dsg_surfel_correlate_gradient_tabled": (ctypes.c_int, [CP, P, I32, P, P, I32, P, I32, P, P, P, P, P, SZ, P]),
     "dsg_surfel_correlate": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, P, P, SZ, P]),
     "dsg_surfel_correlate_active": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, I32, P, P, P, SZ, P]),
     "dsg_surfel_correlate_gradient": (

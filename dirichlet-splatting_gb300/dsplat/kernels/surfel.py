@@ -216,29 +216,65 @@ def jacobian(config, positions, centers, normals, fresnel_n):
     return torch.view_as_complex(cols), jac[..., :3], jac[..., 3:]
 
 
-def correlate(config, positions, centers, normals, residual, fresnel_n, active=None):
+def interpolated():
+    """Whether the aperture-reduced kernels run in the interpolated form (the default)."""
+    return int(_lib.library().dsg_tuning_get(_CORRELATION_FORM_KNOB)) != CORRELATION_FORMS["exact"]
+
+
+def residual_tables(config, residual, derivative=True, out=None):
+    """Aperture tables of a residual [A, K] for the interpolated correlations (float32, flat).
+
+    Computed once, they serve every correlate / correlate_gradient call given them
+    (tables=...) with the same residual: the per-residual product of the interpolated form
+    then runs once instead of once per call. derivative=False makes the correlation tables
+    only (enough for correlate). out, when given, is filled in place (a static buffer).
+    """
+    r = real_view(residual)
+    chirp = _lib.chirp(config)
+    apertures = r.shape[0]
+    nbytes = _lib.query("dsg_surfel_residual_tables_bytes", chirp, apertures, int(bool(derivative)))
+    if out is None:
+        out = torch.empty(nbytes // 4, dtype=torch.float32, device=r.device)
+    elif out.numel() * 4 < nbytes:
+        raise _lib.DsplatKernelError("residual tables buffer too small")
+    call("dsg_surfel_residual_tables", chirp, ptr(r), apertures, int(bool(derivative)), ptr(out), out.numel() * 4,
+         _lib.stream(r.device))  # fmt: skip
+    return out
+
+
+def correlate(config, positions, centers, normals, residual, fresnel_n, active=None, tables=None):
     """conj(column) . residual and |column|^2 per candidate, without area.
 
     active = (count, period), count an int32 device tensor of one element: only candidates
-    whose index mod period is below count are computed; the others get zeros.
+    whose index mod period is below count are computed; the others get zeros. tables, from
+    residual_tables(residual), replaces residual (the same results, bitwise).
     """
     positions, centers, normals = f32(positions), f32(centers), f32(normals)
-    r = real_view(residual)
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
     _tuned("splat", config, apertures, count, centers.device)
     corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
+    name = "dsg_surfel_correlate" if active is None else "dsg_surfel_correlate_active"
+    _work(name, apertures * count * config.num_range_bins)
+    if tables is not None:
+        nbytes = _lib.query("dsg_surfel_tabled_workspace_bytes", apertures, count, 3)
+        work, nbytes = _lib.workspace(nbytes, centers.device)
+        limit, period = (None, 1) if active is None else (ptr(active[0]), int(active[1]))
+        call(
+            "dsg_surfel_correlate_tabled", chirp, ptr(positions), apertures, ptr(centers), ptr(normals), count,
+            ptr(tables), limit, period, ptr(corr), ptr(norm), ptr(work), nbytes, _lib.stream(centers.device),
+        )  # fmt: skip
+        return torch.view_as_complex(corr), norm
+    r = real_view(residual)
     nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3)
     work, nbytes = _lib.workspace(nbytes, centers.device)
     if active is None:
-        _work("dsg_surfel_correlate", apertures * count * config.num_range_bins)
         call(
             "dsg_surfel_correlate", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
             count, ptr(r), ptr(corr), ptr(norm), ptr(work), nbytes, _lib.stream(centers.device),
         )  # fmt: skip
     else:
         limit, period = active
-        _work("dsg_surfel_correlate_active", apertures * count * config.num_range_bins)
         call(
             "dsg_surfel_correlate_active", chirp, ptr(positions), apertures, ptr(centers),
             ptr(normals), count, ptr(r), ptr(limit), int(period), ptr(corr), ptr(norm), ptr(work),
@@ -273,26 +309,36 @@ def correlate_orientations(config, positions, centers, normals, bank, residual, 
     return torch.complex(out[..., 0], out[..., 1]), out[..., 2]
 
 
-def correlate_gradient(config, positions, centers, normals, residual, fresnel_n, include_normals):
-    """Correlation, norm and their center (and normal) derivatives [S, 3 or 6], without area."""
+def correlate_gradient(config, positions, centers, normals, residual, fresnel_n, include_normals, tables=None):
+    """Correlation, norm and their center (and normal) derivatives [S, 3 or 6], without area.
+
+    tables, from residual_tables(residual) with derivative, replaces residual (the same
+    results, bitwise)."""
     positions, centers, normals = f32(positions), f32(centers), f32(normals)
-    r = real_view(residual)
     width = 6 if include_normals else 3
     chirp = _lib.chirp(config, fresnel_n)
     count, apertures = len(centers), len(positions)
     _tuned("splat", config, apertures, count, centers.device)
     corr, norm = _outputs(centers, count, 2), _outputs(centers, count)
     dcorr, dnorm = _outputs(centers, count, width, 2), _outputs(centers, count, width)
-    nbytes = _lib.query(
-        "dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3 + 3 * width
-    )
-    work, nbytes = _lib.workspace(nbytes, centers.device)
     _work("dsg_surfel_correlate_gradient", apertures * count * config.num_range_bins)
-    call(
-        "dsg_surfel_correlate_gradient", chirp, ptr(positions), apertures, ptr(centers),
-        ptr(normals), count, ptr(r), width, ptr(corr), ptr(norm), ptr(dcorr), ptr(dnorm),
-        ptr(work), nbytes, _lib.stream(centers.device),
-    )  # fmt: skip
+    if tables is not None:
+        nbytes = _lib.query("dsg_surfel_tabled_workspace_bytes", apertures, count, 3 + 3 * width)
+        work, nbytes = _lib.workspace(nbytes, centers.device)
+        call(
+            "dsg_surfel_correlate_gradient_tabled", chirp, ptr(positions), apertures, ptr(centers), ptr(normals),
+            count, ptr(tables), width, ptr(corr), ptr(norm), ptr(dcorr), ptr(dnorm), ptr(work), nbytes,
+            _lib.stream(centers.device),
+        )  # fmt: skip
+    else:
+        r = real_view(residual)
+        nbytes = _lib.query("dsg_surfel_reduce_workspace_bytes", chirp, apertures, count, 3 + 3 * width)
+        work, nbytes = _lib.workspace(nbytes, centers.device)
+        call(
+            "dsg_surfel_correlate_gradient", chirp, ptr(positions), apertures, ptr(centers),
+            ptr(normals), count, ptr(r), width, ptr(corr), ptr(norm), ptr(dcorr), ptr(dnorm),
+            ptr(work), nbytes, _lib.stream(centers.device),
+        )  # fmt: skip
     return (
         torch.view_as_complex(corr),
         norm,

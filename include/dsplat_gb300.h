@@ -222,6 +222,35 @@ int dsg_surfel_correlate_gradient(const DsgChirp* chirp, const float* positions,
                                   float* corr, float* norm, float* dcorr, float* dnorm,
                                   void* workspace, size_t workspace_bytes, void* stream);
 
+/* The residual's aperture tables for the interpolated correlations, computed once and
+ * read by any number of the *_tabled calls below. No counterpart in the reference, whose
+ * certificate ascent (dsplat/certificate.py:159-194, search_certificate) correlates the
+ * same residual with every trial of every iteration; the interpolated form's per-residual
+ * work (a [A,K]x[K,2 samples] complex product per table) is done once per search here.
+ * tables: [A][2 samples] complex for Z0, then (derivative != 0) the same for Z1;
+ * dsg_surfel_residual_tables_bytes gives the size. The first call with a chirp's
+ * samples and pad on a device builds its fixed tables (cudaMalloc and a synchronous copy):
+ * make it before any stream capture. */
+size_t dsg_surfel_residual_tables_bytes(const DsgChirp* chirp, int32_t apertures, int32_t derivative);
+int dsg_surfel_residual_tables(const DsgChirp* chirp, const float* residual, int32_t apertures,
+                               int32_t derivative, float* tables, size_t tables_bytes, void* stream);
+/* Workspace of the tabled calls: the chunk partials only. */
+size_t dsg_surfel_tabled_workspace_bytes(int32_t apertures, int32_t candidates, int32_t values_per_surfel);
+/* dsg_surfel_correlate (active == NULL) or dsg_surfel_correlate_active from a residual's
+ * tables: the same outputs, bitwise, as those calls in the interpolated form. values per
+ * surfel 3. */
+int dsg_surfel_correlate_tabled(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                                const float* centers, const float* normals, int32_t candidates,
+                                const float* tables, const int32_t* active, int32_t period, float* corr,
+                                float* norm, void* workspace, size_t workspace_bytes, void* stream);
+/* dsg_surfel_correlate_gradient from a residual's tables (made with derivative != 0); the
+ * same outputs, bitwise, as that call in the interpolated form. values per surfel 3 + 3 width. */
+int dsg_surfel_correlate_gradient_tabled(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                                         const float* centers, const float* normals, int32_t candidates,
+                                         const float* tables, int32_t width, float* corr, float* norm,
+                                         float* dcorr, float* dnorm, void* workspace, size_t workspace_bytes,
+                                         void* stream);
+
 /* Scores of each candidate's own normal and every bank normal (reference:
  * dsplat/kernels/surfel.py:263-290 correlate_orientations). bank [Nb,3];
  * out [C, 1+Nb, 3] = (Re corr, Im corr, norm). range_table [A, n_fft*oversample, 2] and

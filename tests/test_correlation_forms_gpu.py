@@ -104,3 +104,34 @@ def test_forms_agree_at_the_ascent_size_with_back_facing_pairs_and_far_peaks():
     corr, _ = got["interp"][3]
     inactive = (torch.arange(len(cen), device="cuda") % 550) >= 200
     assert bool((corr[inactive] == 0).all())
+
+
+@pytest.mark.parametrize("samples,pad", [(128, 2), (64, 4)])
+def test_tabled_calls_equal_the_residual_calls_bitwise(samples, pad):
+    """A residual's interpolation tables computed once (dsg_surfel_residual_tables) give
+    the correlations, the active-set correlations and the gradients bit for bit."""
+    from dsplat import FMCWConfig
+    from dsplat.kernels import surfel as kernel
+
+    config = FMCWConfig(adc_samples=samples, pad_factor=pad)
+    positions = aperture_grid(9)  # 81 apertures
+    cand = surfels(77, seed=5, spread=0.04)
+    cen, nrm = cand["centers"], cand["normals"]
+    residual = _upstream(len(positions), config.num_range_bins, seed=12)
+    active = torch.tensor([20], dtype=torch.int32, device="cuda")
+    with kernel.correlation_form("interp"):
+        tables = kernel.residual_tables(config, residual)
+        plain = (kernel.correlate(config, positions, cen, nrm, residual, 0.0),
+                 kernel.correlate(config, positions, cen, nrm, residual, 0.0, active=(active, 40)),
+                 kernel.correlate_gradient(config, positions, cen, nrm, residual, 0.0, True),
+                 kernel.correlate_gradient(config, positions, cen, nrm, residual, 0.0, False))  # fmt: skip
+        tabled = (kernel.correlate(config, positions, cen, nrm, None, 0.0, tables=tables),
+                  kernel.correlate(config, positions, cen, nrm, None, 0.0, active=(active, 40), tables=tables),
+                  kernel.correlate_gradient(config, positions, cen, nrm, None, 0.0, True, tables=tables),
+                  kernel.correlate_gradient(config, positions, cen, nrm, None, 0.0, False, tables=tables))  # fmt: skip
+        short = kernel.residual_tables(config, residual, derivative=False)
+        corr_short = kernel.correlate(config, positions, cen, nrm, None, 0.0, tables=short)
+    for a, b in zip(plain, tabled, strict=True):
+        for x, y in zip(a, b, strict=True):
+            assert torch.equal(x, y)
+    assert torch.equal(corr_short[0], plain[0][0]) and torch.equal(corr_short[1], plain[0][1])
