@@ -19,6 +19,7 @@ from dataclasses import replace
 
 import torch
 
+from .graphs import recording
 from .kernels import search
 from .tracing import stage
 
@@ -232,7 +233,7 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
                 torch.cuda.current_stream(device).wait_stream(side)
                 graph = torch.cuda.CUDAGraph()
                 before = _lib.library().dsg_launch_count()
-                with torch.cuda.graph(graph):
+                with recording(graph):
                     iterate(*state, inputs["stuck"])
                 per_replay = _lib.library().dsg_launch_count() - before
             with stage("ascent.replay"):
@@ -289,7 +290,7 @@ def _graphed_ascent(iterate, iterations, params, value, grad, inverse, keep=None
             torch.cuda.current_stream(device).wait_stream(side)
             graph = torch.cuda.CUDAGraph()
             before = _lib.library().dsg_launch_count()
-            with torch.cuda.graph(graph):
+            with recording(graph):
                 out = iterate(*static)
                 for key, v in out[0].items():
                     static[0][key].copy_(v)

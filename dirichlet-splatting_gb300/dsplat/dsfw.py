@@ -24,6 +24,7 @@ from dataclasses import dataclass, replace
 import torch
 
 from .parameters import ParameterConfig
+from .normal import PROJECTIONS
 from .refinement import dense_slide, joint_slide, trainable
 from .replacement import merge_support, replace_one
 from .spatial import propose
@@ -118,6 +119,8 @@ def initialize(model, target, params, config, *, candidates=None, parameters=Non
     specs = {key: given.get(key, ParameterConfig(trainable=False)) for key in params}
     start = {key: specs[key].project(value.detach().clone(), value.detach()) for key, value in params.items()}
     model = model.prepare(specs)
+    if getattr(config, "gram", "fp32") == "bf16x3" and config.replacement == "merged":
+        PROJECTIONS.track(model)  # the support's projected rows serve the next pool
     pool = start if candidates is None else {key: value.detach().clone() for key, value in candidates.items()}
     power = float(target.abs().square().mean())
     fit = varpro(model, start, target, config)

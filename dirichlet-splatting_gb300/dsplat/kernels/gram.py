@@ -49,15 +49,26 @@ def k_splits(n_pad, k_pad, column_from=0):
 
 
 class GramRows:
-    """Transposed bf16 hi/lo storage of up to `capacity` real rows of `columns` unknowns."""
+    """Transposed bf16 hi/lo storage of up to `capacity` real rows of `columns` unknowns.
 
-    def __init__(self, columns, capacity, device):
+    reserve adds storage for that many more unknowns (set_columns widens to them later
+    without moving the stored ones; the Gram only ever covers the current columns).
+    """
+
+    def __init__(self, columns, capacity, device, reserve=0):
+        self.k_pad = _round_up(max(capacity, 1), 64)
+        self.n_alloc = _round_up(max(columns + reserve, 1), 128)
+        self.hi = torch.empty((self.n_alloc, self.k_pad), dtype=torch.bfloat16, device=device)
+        self.lo = torch.empty_like(self.hi)
+        self.set_columns(columns)
+        self.rows = 0
+
+    def set_columns(self, columns):
+        """Cover `columns` unknowns (at most the allocated ones); stored rows stay."""
+        if _round_up(max(columns, 1), 128) > self.n_alloc:
+            raise DsplatKernelError("GramRows column capacity exceeded")
         self.columns = columns
         self.n_pad = _round_up(max(columns, 1), 128)
-        self.k_pad = _round_up(max(capacity, 1), 64)
-        self.hi = torch.empty((self.n_pad, self.k_pad), dtype=torch.bfloat16, device=device)
-        self.lo = torch.empty_like(self.hi)
-        self.rows = 0
 
     def append(self, block):
         """Store block [m, columns] (FP32) as the next m reduction indices."""
@@ -79,14 +90,14 @@ class GramRows:
         k_splits).
         """
         if self.rows < self.k_pad:
-            self.hi[:, self.rows :].zero_()
-            self.lo[:, self.rows :].zero_()
+            self.hi[: self.n_pad, self.rows :].zero_()
+            self.lo[: self.n_pad, self.rows :].zero_()
         if self.n_pad > self.columns:
-            self.hi[self.columns :].zero_()
-            self.lo[self.columns :].zero_()
+            self.hi[self.columns : self.n_pad].zero_()
+            self.lo[self.columns : self.n_pad].zero_()
         k_pad = _round_up(max(self.rows, 1), 64)
         status = torch.zeros(1, dtype=torch.int32, device=total.device)
-        hi, lo = self.hi[:, :k_pad], self.lo[:, :k_pad]
+        hi, lo = self.hi[: self.n_pad, :k_pad], self.lo[: self.n_pad, :k_pad]
         if k_pad != self.k_pad:  # a narrower view needs contiguous rows for the tensor map
             hi, lo = hi.contiguous(), lo.contiguous()
         # logical FP32 flops of the needed symmetric block (a SYRK count)
@@ -130,14 +141,19 @@ def fused_supported(config, basis):
             and config.num_range_bins in (32, 64, 128) and config.pad_factor in (1, 2, 4))  # fmt: skip
 
 
-def append_projected(store, config, positions, params, basis, fresnel_n, status):
-    """Store the basis-projected real dictionary rows of apertures `positions` (fused kernel)."""
+def append_projected(store, config, positions, params, basis, fresnel_n, status, first_unknown=0, row=None):
+    """Store the basis-projected real dictionary rows of apertures `positions` (fused kernel).
+
+    The unknowns (params' surfels) fill the store's rows from first_unknown; the reduction
+    index starts at row (default: after the stored rows, which then advance).
+    """
     from . import _lib as lib
 
     hi, lo = split_basis(basis.interleaved)
     rank2 = basis.interleaved.shape[0]
     count = len(positions) * rank2
-    if store.rows + count > store.k_pad:
+    start = store.rows if row is None else row
+    if start + count > store.k_pad or first_unknown + len(params["centers"]) > store.n_alloc:
         raise DsplatKernelError("GramRows capacity exceeded")
     positions = positions.to(torch.float32).contiguous()
     centers = params["centers"].to(torch.float32).contiguous()
@@ -152,10 +168,13 @@ def append_projected(store, config, positions, params, basis, fresnel_n, status)
                  float(len(positions)) * len(centers) * 2 * (2 * config.num_range_bins) * rank2)  # fmt: skip
     call(
         "dsg_design_project_bf16x3", lib.chirp(config, fresnel_n), ptr(positions), len(positions),
-        ptr(centers), ptr(normals), ptr(areas), len(centers), ptr(hi), ptr(lo), rank2, ptr(store.hi),
-        ptr(store.lo), store.k_pad, store.rows, ptr(status), lib.stream(positions.device),
+        ptr(centers), ptr(normals), ptr(areas), len(centers), ptr(hi), ptr(lo), rank2,
+        ptr(store.hi[first_unknown:]), ptr(store.lo[first_unknown:]), store.k_pad, start, ptr(status),
+        lib.stream(positions.device),
     )  # fmt: skip
-    store.rows += count
+    if row is None:
+        store.rows += count
+    return start + count
 
 
 def check(status):

@@ -20,6 +20,8 @@ from __future__ import annotations
 
 import torch
 
+from .graphs import recording
+
 POWER_STEPS = 24  # power iterations for the largest eigenvalue of a Gram
 SHIFT_RETRIES = 4
 # Cumulative shift multipliers of the retries: each retry adds nine times everything
@@ -256,7 +258,7 @@ def _pcg_graphed(operator, rhs, diagonal, iterations, tolerance):
         torch.cuda.current_stream(device).wait_stream(side)
         graph = torch.cuda.CUDAGraph()
         before = _lib.library().dsg_launch_count()
-        with torch.cuda.graph(graph):
+        with recording(graph):
             iteration()
         per_replay = _lib.library().dsg_launch_count() - before
         for _ in range(iterations - 1):

@@ -51,12 +51,14 @@ def projected_rows(model, chunk):
     return total
 
 
-def fused_rows(model, params, store, chunk):
+def fused_rows(model, params, store, chunk, first_unknown=0):
     """Store every projected real row block with the fused design-projection kernel.
 
     Consecutive blocks sharing one basis go to the kernel as one aperture range. Returns
     the kernel status tensor, or None (nothing stored) when the model or a block's basis
-    is outside what the kernel covers; the caller then streams explicit blocks.
+    is outside what the kernel covers; the caller then streams explicit blocks. With
+    first_unknown > 0 params' surfels fill the store's rows from there, beside unknowns
+    stored before with the same model and chunk (the same reduction rows).
     """
     from .kernels.gram import append_projected, fused_supported
 
@@ -75,9 +77,79 @@ def fused_rows(model, params, store, chunk):
         else:
             runs.append([first, stop, basis])
     status = torch.zeros(1, dtype=torch.int32, device=positions.device)
+    row = 0
     for first, stop, basis in runs:
-        append_projected(store, config, positions[first:stop], params, basis, model.fresnel_n, status)
+        row = append_projected(store, config, positions[first:stop], params, basis, model.fresnel_n, status,
+                               first_unknown=first_unknown, row=row)  # fmt: skip
+    if first_unknown == 0:
+        store.rows = row
+    elif row != store.rows:
+        raise RuntimeError("projected rows do not line up with the stored unknowns")
     return status
+
+
+class ProjectionCache:
+    """Projected rows (bf16 hi/lo) of the latest supports, reused when a pool extends one.
+
+    The merged replacement pools the support with new candidates. When the support's rows
+    were stored by an earlier normal-equation pass of the same model over the very same
+    parameter tensors (states never write their tensors in place, so identity means equal
+    values), only the candidates are projected, into the rows after the support's, with
+    that pass's block layout. After a replacement the survivors' rows are moved into their
+    slots (adopt) so the next step's pool finds the new support. Only models registered
+    with track (the fitted states' models, not their aperture subsets) are kept; holds the
+    last LIMIT stores (a few GB each at 16 384 apertures).
+    """
+
+    LIMIT = 3
+    MODELS = 4
+
+    def __init__(self):
+        self.entries = []  # [model, params (the tensors), store, chunk], most recent last
+        self.models = []
+
+    def track(self, model):
+        """Keep the projected rows of this model's normal equations from now on."""
+        if not any(m is model for m in self.models):
+            self.models.append(model)
+            del self.models[: -self.MODELS]
+            self.entries = [e for e in self.entries if any(m is e[0] for m in self.models)]
+
+    def tracks(self, model):
+        return any(m is model for m in self.models)
+
+    def put(self, model, params, store, chunk):
+        if not self.tracks(model):
+            return None
+        self.entries = [e for e in self.entries if e[2] is not store]
+        self.entries.append([model, dict(params), store, chunk])
+        del self.entries[: -self.LIMIT]
+        return self.entries[-1]
+
+    def find(self, model, params):
+        for entry in reversed(self.entries):
+            if entry[0] is model and entry[1].keys() == params.keys() and all(
+                    entry[1][key] is params[key] for key in params):  # fmt: skip
+                return entry
+        return None
+
+    def adopt(self, entry, slots, owners, params):
+        """The stored support after a replacement: slot j takes the pooled row slots[j]."""
+        store = entry[2]
+        if len(owners):
+            sources = slots[owners]
+            store.hi.index_copy_(0, owners, store.hi.index_select(0, sources))
+            store.lo.index_copy_(0, owners, store.lo.index_select(0, sources))
+        store.set_columns(len(slots))
+        entry[1] = dict(params)
+        self.entries = [e for e in self.entries if e is not entry] + [entry]  # by identity: models hold tensors
+
+    def clear(self):
+        self.entries = []
+        self.models = []
+
+
+PROJECTIONS = ProjectionCache()
 
 
 def _symmetrize_upper(total, size):
@@ -110,12 +182,20 @@ class Fp32Syrk:
 
 
 class TensorCoreGram:
-    """Split-BF16x3 rows stored for one tcgen05 Gram launch (real coefficients)."""
+    """Split-BF16x3 rows stored for one tcgen05 Gram launch (real coefficients).
 
-    def __init__(self, model, count, chunk, device):
+    store, when given, is a GramRows already holding rows (ProjectionCache); reserve
+    allocates room for that many more unknowns.
+    """
+
+    def __init__(self, model, count, chunk, device, store=None, reserve=0):
         from .kernels.gram import GramRows
 
-        self.store = GramRows(count, projected_rows(model, chunk), device)
+        if store is None:
+            store = GramRows(count, projected_rows(model, chunk), device, reserve=reserve)
+        else:
+            store.set_columns(count)
+        self.store = store
         self.total = torch.zeros((count, count), dtype=torch.float64, device=device)
         self.rhs = torch.zeros(count, dtype=torch.float64, device=device)
 
@@ -147,7 +227,8 @@ def normal_equations(model, params, target, config):
         return (gram + gram.mH) / (2 * model.size), rhs / model.size
     device = target.device
     if getattr(config, "gram", "fp32") == "bf16x3":
-        acc = TensorCoreGram(model, count, chunk, device)
+        merged = getattr(config, "replacement", "merged") == "merged" and PROJECTIONS.tracks(model)
+        acc = TensorCoreGram(model, count, chunk, device, reserve=config.batch if merged else 0)
         status = fused_rows(model, params, acc.store, chunk)
         if status is None:
             for a, y in model.blocks(params, target, True, chunk):
@@ -157,6 +238,8 @@ def normal_equations(model, params, target, config):
 
             acc.rhs += model.correlate(params, target)[0].real.double()
             check(status)
+            if merged:
+                PROJECTIONS.put(model, params, acc.store, chunk)
         total, rhs = acc.finish()
     else:
         acc = Fp32Syrk(count, device)

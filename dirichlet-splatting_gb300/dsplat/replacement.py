@@ -25,7 +25,7 @@ import torch
 from .certificate import certificate
 from .kernels import search
 from .linalg import shifted_cholesky
-from .normal import TensorCoreGram, fused_rows, row_chunk
+from .normal import PROJECTIONS, TensorCoreGram, fused_rows, row_chunk
 from .parameters import periodic_delta
 from .tracing import stage
 from .varpro import Fit, accept, refined_coefficients, rendered_loss, screen_bar, varpro
@@ -202,11 +202,26 @@ def _distinct(scores, points, occupied, period, separation, width):
     return torch.cat(kept)[:width] if kept else ranked[:0]
 
 
-def _cross_on_tensor_cores(model, pool, target, support, chunk):
-    """(cross [total, added] = A^T A[:, support:], right = A[:, support:]^T y), tcgen05 Gram."""
+def _cross_on_tensor_cores(model, pool, target, support, chunk, support_params=None):
+    """(cross [total, added] = A^T A[:, support:], right = A[:, support:]^T y), tcgen05 Gram.
+
+    When the support's projected rows are still stored (normal.PROJECTIONS, found by the
+    support's own parameter tensors) only the new atoms are projected, beside them.
+    Returns the cross, the right-hand side and the cache entry now holding the pool's rows.
+    """
     total = len(pool["centers"])
-    gram = TensorCoreGram(model, total, chunk, target.device)
-    status = fused_rows(model, pool, gram.store, chunk)
+    entry = None if support_params is None else PROJECTIONS.find(model, support_params)
+    if entry is not None and -(-total // 128) * 128 <= entry[2].n_alloc:
+        store, chunk = entry[2], entry[3]
+        gram = TensorCoreGram(model, total, chunk, target.device, store=store)
+        fresh = {key: value[support:] for key, value in pool.items()}
+        status = fused_rows(model, fresh, store, chunk, first_unknown=support)
+    else:
+        gram = TensorCoreGram(model, total, chunk, target.device)
+        status = fused_rows(model, pool, gram.store, chunk)
+        entry = None
+        if status is not None and support_params is not None:
+            entry = PROJECTIONS.put(model, support_params, gram.store, chunk)
     if status is None:
         right = torch.zeros(total - support, dtype=torch.float64, device=target.device)
         for a, y in model.blocks(pool, target, True, chunk):
@@ -220,19 +235,22 @@ def _cross_on_tensor_cores(model, pool, target, support, chunk):
     products, _ = gram.finish(column_from=support)
     new = products[support:, support:]
     cross = torch.cat((products[:support, support:], torch.triu(new) + torch.triu(new, 1).T))
-    return cross.float(), right.float()
+    return cross.float(), right.float(), entry
 
 
-def pooled_statistics(state, pool, config):
+def pooled_statistics(state, pool, config, projections=None):
     """Gram and right-hand side of the support followed by the pooled new atoms.
 
-    Only the new columns are streamed; the support block is the state's.
+    Only the new columns are streamed; the support block is the state's. projections, a
+    list, receives the ProjectionCache entry holding the pool's rows (tensor-core path).
     """
     model, support = state.model, len(state.coefficients)
     total = len(pool["centers"])
     chunk = row_chunk(model, total, config)
     if config.real and getattr(config, "gram", "fp32") == "bf16x3":
-        cross, right = _cross_on_tensor_cores(model, pool, state.target, support, chunk)
+        cross, right, entry = _cross_on_tensor_cores(model, pool, state.target, support, chunk, state.params)
+        if projections is not None:
+            projections.append(entry)
     else:
         cross = state.gram.new_zeros((total, total - support))
         right = state.rhs.new_zeros(total - support)
@@ -261,8 +279,9 @@ class _PooledFit:
     def __init__(self, state, pool, config):
         self.state, self.pool, self.config = state, pool, config
         self.support = len(state.coefficients)
+        self.projections = []
         with stage("replace.pooled"):
-            self.gram, self.rhs = pooled_statistics(state, pool, config)
+            self.gram, self.rhs = pooled_statistics(state, pool, config, self.projections)
         h = self.gram.real if config.real else self.gram
         if config.ridge:
             h = h.clone()
@@ -341,6 +360,9 @@ def merge_support(state, config, pool, scores=None):
             return state, 0
         atoms, result = fit.trial(slots, owners)
         if result.objective < state.objective:
+            entry = fit.projections[0] if fit.projections else None
+            if entry is not None and PROJECTIONS.find(state.model, state.params) is entry:
+                PROJECTIONS.adopt(entry, slots, owners, atoms)  # the next pool starts from it
             return replace(state, params=atoms, **result._asdict()), len(owners)
         limit = len(owners) // 2
         if limit < 1:
