@@ -211,8 +211,8 @@ def _cross_on_tensor_cores(model, pool, target, support, chunk, support_params=N
     """
     total = len(pool["centers"])
     entry = None if support_params is None else PROJECTIONS.find(model, support_params)
-    if entry is not None and -(-total // 128) * 128 <= entry[2].n_alloc:
-        store, chunk = entry[2], entry[3]
+    if entry is not None and -(-total // 128) * 128 <= entry[2].n_alloc and entry[3] == chunk:
+        store = entry[2]
         gram = TensorCoreGram(model, total, chunk, target.device, store=store)
         fresh = {key: value[support:] for key, value in pool.items()}
         status = fused_rows(model, fresh, store, chunk, first_unknown=support)
@@ -248,7 +248,12 @@ def pooled_statistics(state, pool, config, projections=None):
     total = len(pool["centers"])
     chunk = row_chunk(model, total, config)
     if config.real and getattr(config, "gram", "fp32") == "bf16x3":
-        cross, right, entry = _cross_on_tensor_cores(model, pool, state.target, support, chunk, state.params)
+        # The fused projection stores no dictionary block, so its block layout follows the
+        # support's size, as the support's own refits do: the stored rows of a refit and
+        # the pool's new rows then share one layout, and a pool gives the same Gram whether
+        # or not the support's rows were still stored.
+        fused_chunk = row_chunk(model, support, config)
+        cross, right, entry = _cross_on_tensor_cores(model, pool, state.target, support, fused_chunk, state.params)
         if projections is not None:
             projections.append(entry)
     else:
