@@ -301,7 +301,10 @@ def run_ours(args, world, rank, local):
     """Mixed+batched arm (default) or plain arm; every arm times the same step indices.
 
     Order of work, all from one initialize():
-      1. steps 1..W untimed (warm-up; first CUDA-graph captures), state S_W kept;
+      0. one discarded step of each arm from its own initialize() (process warm-up: lazy
+         library loads and the first CUDA-graph captures, which would otherwise land in
+         step 1 of whichever arm runs first);
+      1. steps 1..W untimed (warm-up), state S_W kept;
       2. value: steps W+1..W+K from S_W, device-resident, nothing instrumented;
       3. e2e: steps W+1..W+K again from S_W (the step is a pure function of the state and
          the seeds), each step's inputs copied in from pinned host memory and its result out;
@@ -331,6 +334,12 @@ def run_ours(args, world, rank, local):
     _lib.TIMERS = None
     tracing.disable()
 
+    # Process warm-up, untimed and discarded: one step of each arm from the start loads the
+    # lazily loaded libraries (cuSOLVER, cuFFT, cuBLAS handles) and captures the CUDA graphs
+    # that later searches of the same shapes replay, so no timed step of either arm pays a
+    # one-time cost. The fits below start again from initialize().
+    for warm_config in (config, DSFWConfig(iterations=args.iterations, batch=256)):
+        step(initialize(model, target, start, warm_config, parameters=parameters), warm_config, search)
     torch.cuda.synchronize(device)
     init_begin = time.perf_counter()
     state = initialize(model, target, start, config, parameters=parameters)
