@@ -253,7 +253,12 @@ def joint_slide(state, config, screen=None):
         ids, model = model.sample_apertures(config.joint_apertures, config.seed + state.iteration)
         target = target[ids]
     accepted = 0
+    overlap = getattr(config, "batched", False) and screen is not None and target.is_cuda
     for inner in range(config.lm_steps):
+        ready = None
+        if overlap:  # the state's tensors are complete in stream order here
+            ready = torch.cuda.Event()
+            ready.record()
         with stage("slide.system"):
             matvec, gradient, diagonal, proposal = joint_system(
                 model, state.params, state.coefficients, target, state.parameters, config,
@@ -261,11 +266,22 @@ def joint_slide(state, config, screen=None):
         with stage("slide.pcg"):
             delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations, tolerance=config.cg_tolerance,
                         capture=getattr(config, "batched", False))  # fmt: skip
+        if overlap:
+            # The screening objective of the current geometry needs neither the system
+            # nor its solution: it runs on a second stream while the conjugate gradients
+            # (enqueued above) run on this one, and is simply unused if no step follows.
+            current = torch.cuda.current_stream()
+            side = torch.cuda.Stream(current.device)
+            side.wait_event(ready)
+            with torch.cuda.stream(side), stage("slide.screen"):
+                bar = screen_bar(screen, state.params, config)
+            current.wait_stream(side)
         descent = torch.isfinite(delta).all() & (delta @ gradient < 0)
         if not bool(descent):
             break
-        with stage("slide.screen"):
-            bar = screen_bar(screen, state.params, config)
+        if not overlap:
+            with stage("slide.screen"):
+                bar = screen_bar(screen, state.params, config)
         for fraction in BACKTRACK_JOINT:
             with stage("slide.accept"):
                 trial = accept(state, proposal(delta, fraction), config, bar)
