@@ -362,7 +362,9 @@ def run_ours(args, world, rank, local):
     with ClockSampler(local) as clocks:
         _barrier(world)
         torch.cuda.synchronize(device)
+        torch.cuda.nvtx.range_push("timed_steps")  # ncu --nvtx --nvtx-include "timed_steps/"
         state, step_ms = _timed_steps(saved, config, search, args.steps, flush, device)
+        torch.cuda.nvtx.range_pop()
         # One more flush-sized fill after the last timed step: in a kernel launch list the
         # timed steps lie between the first and the last of these fills.
         flush.view(torch.float32).fill_(2.0)
@@ -706,6 +708,14 @@ def run_kernels(args):
     it, wu = args.steps, args.warmup
     ms = _event_time(lambda: kernel.render(config, positions, centers, normals, weights, 0.0), it, wu, flush)
     record("dsg_surfel_render", ms, A * S * K, 16)
+    # the forward through the ADC samples: phasor recurrence (6 FP32 flops per pair-sample,
+    # one anchor per lane and pair) plus the n_fft-point cuFFT, counted per pair-bin as above
+    samples_only = _event_time(lambda: kernel.render_samples(config, positions, centers, normals, weights, 0.0),
+                               it, wu, flush)  # fmt: skip
+    record("dsg_surfel_render_samples (kernel alone)", samples_only, A * S * config.adc_samples, 6, "pair-samples")
+    with kernel.render_form("samples"):
+        ms = _event_time(lambda: kernel.render(config, positions, centers, normals, weights, 0.0), it, wu, flush)
+    record("dsg_surfel_render [samples form + FFT]", ms, A * S * K, 16)
     ms = _event_time(lambda: kernel.jvp(config, positions, centers, normals, weights, dc, dn, dw, 0.0), it, wu, flush)
     record("dsg_surfel_jvp", ms, A * S * K, 24)
     ms = _event_time(lambda: kernel.vjp(config, positions, centers, normals, weights, upstream, 0.0), it, wu, flush)

@@ -19,7 +19,7 @@ from dataclasses import replace
 
 import torch
 
-from .graphs import recording
+from .graphs import recording, side_stream
 from .kernels import search
 from .tracing import stage
 
@@ -223,7 +223,7 @@ def _fused_ascent(model, residual, controls, specs, config, mode, fractions, par
         iterate = _fused_iteration(static_model, inputs["residual"], inputs["power"], inputs["controls"], specs,
                                    config, mode, fractions, inputs["tables"])  # fmt: skip
         device = value.device
-        side = torch.cuda.Stream(device)
+        side = side_stream(device)
         side.wait_stream(torch.cuda.current_stream(device))
         timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be timed inside a graph
         try:
@@ -278,7 +278,7 @@ def _graphed_ascent(iterate, iterations, params, value, grad, inverse, keep=None
     from .kernels import _lib
 
     device = value.device
-    side = torch.cuda.Stream(device)
+    side = side_stream(device)
     side.wait_stream(torch.cuda.current_stream(device))
     timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be timed inside a graph
     try:

@@ -98,11 +98,13 @@ def fibonacci_sphere(count, device="cuda"):
 
 
 @torch.no_grad()
-def orient_candidates(model, params, residual, count, mode, table=None, chunk=1 << 21):
+def orient_candidates(model, params, residual, count, mode, table=None, chunk=1 << 21, fused=False):
     """Each position with the best normal among its own and a count-normal sphere bank.
 
     Returns the candidates with the chosen normals and their squared certificates. One
-    launch scores a chunk of positions against all 1 + count normals.
+    launch scores a chunk of positions against all 1 + count normals; fused (models with
+    orient_best) also selects the best normal in that launch instead of writing every
+    normal's scores for the selection here.
     """
     centers = params["centers"]
     bank = fibonacci_sphere(count, centers.device)
@@ -110,6 +112,14 @@ def orient_candidates(model, params, residual, count, mode, table=None, chunk=1 
     best_scores, best_normals = [], []
     for start in range(0, len(centers), chunk):
         part = {key: value[start : start + chunk] for key, value in params.items()}
+        if fused:
+            which, top = model.orient_best(part, residual, bank, energy, mode == "real", table)
+            own = part["normals"]
+            if len(bank):
+                own = torch.where((which == 0)[:, None], own, bank[(which - 1).clamp(min=0)])
+            best_normals.append(own)
+            best_scores.append(top)
+            continue
         corr, norm = model.correlate_orientations(part, residual, bank, table)
         c = corr.to(torch.complex128)
         projected = c.real if mode == "real" else c

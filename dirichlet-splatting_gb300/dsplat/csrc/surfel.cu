@@ -17,6 +17,7 @@
 #include <vector>
 #include "common.cuh"
 #include "reduce.cuh"
+#include "tc.cuh"
 
 namespace dsg {
 
@@ -140,6 +141,184 @@ __global__ void __launch_bounds__(128) render_kernel(Consts c, const float* __re
   const int s_begin = blockIdx.y * seg_len;
   render_tile<BPL, P>(c, pos, A, cen, nrm, w, s_begin, min(S, s_begin + seg_len), blockIdx.x, blockIdx.y, out,
                       smem);
+}
+
+// ------------------------------------------------------------------------------------
+// Range profiles through the ADC samples (the reference sums the closed-form kernel over
+// bins; this variant sums over samples): profile[a][k] = sum_{n<S} y[a][n] e^{-2 pi i n k/N}
+// with y[a][n] = sum_s w_s c_s / S e^{2 pi i n k0_s / N}, so the profiles are the N-point DFT
+// of the zero-padded samples (cuFFT, by the caller). A pair's samples form a geometric
+// sequence: a lane owns SPL consecutive samples n0 .. n0 + SPL - 1, anchors the first one
+// exactly (sincospif of the turn (n0 lobe mod N) / N - n0 off / N, lobe and off as in
+// pair_setup) and advances by the pair's step e^{2 pi i (lobe - off) / N}, one complex
+// multiply per sample: the sweep issues no MUFU operation, and every lane re-anchors each
+// pair, so a rounding never travels more than SPL samples. Chunks of 32 surfels (centers,
+// normals, weights) reach shared memory by bulk copies (cp.async.bulk with mbarrier
+// completion, double buffered) when the inputs are 16-byte aligned; every wait is bounded
+// and a wait that runs out sets the status word.
+// ------------------------------------------------------------------------------------
+constexpr int kAdcChunk = 32;
+constexpr int kAdcRec = 6;  // per (surfel, aperture): g.re, g.im, step.re, step.im, lobe bits, off
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          tc::smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+      : "memory");
+}
+
+template <int SPL>
+__global__ void __launch_bounds__(128) render_adc_kernel(Consts c, const float* __restrict__ pos, int A,
+                                                         const float* __restrict__ cen,
+                                                         const float* __restrict__ nrm,
+                                                         const float2* __restrict__ w, int S, int seg_len,
+                                                         int bulk, float2* __restrict__ out,
+                                                         int* __restrict__ status) {
+  __shared__ __align__(16) float s_cen[2][3 * kAdcChunk];
+  __shared__ __align__(16) float s_nrm[2][3 * kAdcChunk];
+  __shared__ __align__(16) float2 s_w[2][kAdcChunk];
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ __align__(16) float s_rec[kWarps][kAdcChunk * 4 * kAdcRec];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int qd = lane >> 3, lp = lane & 7;
+  const int s_begin = blockIdx.y * seg_len;
+  const int s_end = min(S, s_begin + seg_len);
+  const int count = max(0, s_end - s_begin);
+  const int whole = bulk ? count / kAdcChunk : 0;  // chunks that arrive by bulk copies
+  const int nchunk = (count + kAdcChunk - 1) / kAdcChunk;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&s_bar[0], 1);
+    tc::mbar_init(&s_bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (whole > 0) {
+      tc::mbar_expect_tx(&s_bar[0], 32 * kAdcChunk);
+      bulk_load(s_cen[0], cen + 3 * (size_t)s_begin, 12 * kAdcChunk, &s_bar[0]);
+      bulk_load(s_nrm[0], nrm + 3 * (size_t)s_begin, 12 * kAdcChunk, &s_bar[0]);
+      bulk_load(s_w[0], w + s_begin, 8 * kAdcChunk, &s_bar[0]);
+    }
+  }
+  __syncthreads();
+
+  const int a_base = (blockIdx.x * kWarps + warp) * 4;
+  float apx[4], apy[4], apz[4];
+  bool aok[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int a = a_base + t;
+    aok[t] = a < A;
+    const int ac = aok[t] ? a : 0;
+    apx[t] = __ldg(pos + 3 * ac);
+    apy[t] = __ldg(pos + 3 * ac + 1);
+    apz[t] = __ldg(pos + 3 * ac + 2);
+  }
+  float2 acc[SPL];
+#pragma unroll
+  for (int i = 0; i < SPL; ++i) acc[i] = make_float2(0.f, 0.f);
+  float* rec = s_rec[warp];
+  const int n0 = lp * SPL;
+  uint32_t parity0 = 0, parity1 = 0;
+  bool failed = false;
+  const float two_over_N = 2.0f / (float)c.N;
+
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const int buf = ch & 1;
+    const int s = s_begin + ch * kAdcChunk + lane;
+    const bool sv = s < s_end;
+    float cx = 0.f, cy = 0.f, cz = 0.f, nx = 0.f, ny = 0.f, nz = 1.f;
+    float2 ws = make_float2(0.f, 0.f);
+    if (ch < whole) {
+      const bool ok = tc::mbar_wait_plain(&s_bar[buf], buf ? parity1 : parity0);
+      if (buf) parity1 ^= 1u; else parity0 ^= 1u;
+      failed |= !ok;
+      cx = s_cen[buf][3 * lane];
+      cy = s_cen[buf][3 * lane + 1];
+      cz = s_cen[buf][3 * lane + 2];
+      nx = s_nrm[buf][3 * lane];
+      ny = s_nrm[buf][3 * lane + 1];
+      nz = s_nrm[buf][3 * lane + 2];
+      ws = s_w[buf][lane];
+    } else if (sv) {
+      cx = __ldg(cen + 3 * s);
+      cy = __ldg(cen + 3 * s + 1);
+      cz = __ldg(cen + 3 * s + 2);
+      nx = __ldg(nrm + 3 * s);
+      ny = __ldg(nrm + 3 * s + 1);
+      nz = __ldg(nrm + 3 * s + 2);
+      ws = ldg2(w + s);
+    }
+    // every thread has read this chunk's buffer; the other one was read before the last
+    // barrier, so the next chunk may overwrite it
+    __syncthreads();
+    if (threadIdx.x == 0 && ch + 1 < whole) {
+      const int nb = buf ^ 1, s1 = s_begin + (ch + 1) * kAdcChunk;
+      tc::mbar_expect_tx(&s_bar[nb], 32 * kAdcChunk);
+      bulk_load(s_cen[nb], cen + 3 * (size_t)s1, 12 * kAdcChunk, &s_bar[nb]);
+      bulk_load(s_nrm[nb], nrm + 3 * (size_t)s1, 12 * kAdcChunk, &s_bar[nb]);
+      bulk_load(s_w[nb], w + s1, 8 * kAdcChunk, &s_bar[nb]);
+    }
+    bool any = false;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      Pair q;
+      pair_setup(c, apx[t], apy[t], apz[t], cx, cy, cz, nx, ny, nz, q);
+      const bool ok = sv && aok[t] && q.amp > 0.0f && (ws.x != 0.0f || ws.y != 0.0f);
+      float* r = rec + (lane * 4 + t) * kAdcRec;
+      if (ok) {
+        const float2 g = cscale(cmul(q.rot, ws), q.amp * c.inv_S);
+        float s1, c1, s2, c2;
+        sincospif((float)q.lobe * two_over_N, &s1, &c1);  // exact turn: lobe < N, N a power of two
+        sincospif(-q.off * two_over_N, &s2, &c2);
+        const float2 step = cmul(make_float2(c1, s1), make_float2(c2, s2));
+        r[0] = g.x;
+        r[1] = g.y;
+        r[2] = step.x;
+        r[3] = step.y;
+        r[4] = __int_as_float(q.lobe);
+        r[5] = q.off;
+      } else {
+        r[0] = 0.0f;
+        r[1] = 0.0f;
+      }
+      any |= ok;
+    }
+    const unsigned mask = __ballot_sync(kFull, any);
+    __syncwarp();
+    const int nb = min(kAdcChunk, s_end - (s_begin + ch * kAdcChunk));
+    for (int j = 0; j < nb; ++j) {
+      if (!((mask >> j) & 1u)) continue;
+      const float* r = rec + (j * 4 + qd) * kAdcRec;
+      const float2 g = make_float2(r[0], r[1]);
+      if (g.x == 0.0f && g.y == 0.0f) continue;  // the quarter's own pair is empty
+      const float2 step = make_float2(r[2], r[3]);
+      const int lobe = __float_as_int(r[4]);
+      // turn of sample n0: (n0 lobe mod N) / N - n0 off / N, the integer part exactly
+      const int whole_turn = (n0 * lobe) & (c.N - 1);
+      const float turn = (float)whole_turn / (float)c.N - (float)n0 * r[5] / (float)c.N;
+      float sa, ca;
+      sincospif(2.0f * turn, &sa, &ca);
+      float2 z = cmul(g, make_float2(ca, sa));
+#pragma unroll
+      for (int i = 0; i < SPL; ++i) {
+        acc[i].x += z.x;
+        acc[i].y += z.y;
+        z = cmul(z, step);
+      }
+    }
+    __syncwarp();
+  }
+  if (failed) {  // a copy never arrived: the status word says so and the tile's samples are NaN
+    atomicExch(status, 1);
+#pragma unroll
+    for (int i = 0; i < SPL; ++i) acc[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+  }
+  const int a = a_base + qd;
+  if (a < A) {
+    float2* o = out + ((size_t)blockIdx.y * A + a) * c.S + n0;
+#pragma unroll
+    for (int i = 0; i < SPL; ++i) o[i] = acc[i];
+  }
 }
 
 // ------------------------------------------------------------------------------------
@@ -727,12 +906,32 @@ __device__ __forceinline__ float bank_angular(const Consts& c, float cosv) {
   return a;
 }
 
-template <int P, bool FRESNEL>
+// Selection of the best normal per candidate (BEST): the certificate of each normal,
+// |Re corr|^2 (real mode) or |corr|^2, over max(norm, 1e-60) times the residual energy, in
+// float64, with corr and norm scaled by the candidate's sqrt(area) and area in float32 first
+// (the arithmetic of dsplat.certificate.orient_candidates); the largest wins, NaN first and
+// the lowest normal index on ties, as torch.max. which = 0 is the candidate's own normal.
+struct OrientBest {
+  const float* areas;    // [C]
+  const double* energy;  // one value on the device
+  int real_mode;
+  int* which;            // [C]
+  float* top;            // [C]
+};
+
+__device__ __forceinline__ bool orient_better(double v, int i, double bv, int bi) {
+  const bool vn = v != v, bn = bv != bv;
+  if (vn != bn) return vn;
+  if (vn) return i < bi;
+  return v > bv || (v == bv && i < bi);
+}
+
+template <int P, bool FRESNEL, bool BEST>
 __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
     Consts c, const float* __restrict__ pos, int A, const float* __restrict__ cen,
     const float* __restrict__ nrm, int C, const float* __restrict__ bank, int bank_size,
     const float2* __restrict__ res, const float2* __restrict__ table,
-    const float* __restrict__ norm_table, int oversample, float* __restrict__ out) {
+    const float* __restrict__ norm_table, int oversample, float* __restrict__ out, OrientBest best) {
   extern __shared__ float smem[];
   const int tbl_n = c.N + c.K;
   float* tbl = smem;
@@ -747,7 +946,9 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
   const float own[3] = {__ldg(nrm + 3 * s), __ldg(nrm + 3 * s + 1), __ldg(nrm + 3 * s + 2)};
   const int size = c.N * oversample;
   const int normals = bank_size + 1;
-  float* o = out + (size_t)s * normals * 3;
+  float* o = BEST ? nullptr : out + (size_t)s * normals * 3;
+  double best_value = 0.0;
+  int best_index = 0x7fffffff;
   for (int j0 = 0; j0 < normals; j0 += 32) {
     const int j = j0 + lane;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
@@ -852,9 +1053,41 @@ __global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
       __syncwarp();
     }
     if (j < normals) {
-      o[3 * j] = acc0.x + acc0.y;
-      o[3 * j + 1] = acc1.x + acc1.y;
-      o[3 * j + 2] = acc2.x + acc2.y;
+      if (BEST) {
+        const float root = sqrtf(__ldg(best.areas + s));
+        const float re = (acc0.x + acc0.y) * root, im = (acc1.x + acc1.y) * root;
+        const float nm = (acc2.x + acc2.y) * (root * root);
+        double num;
+        if (best.real_mode) {
+          num = (double)re * (double)re;
+        } else {
+          const double mag = hypot((double)re, (double)im);
+          num = mag * mag;
+        }
+        const double value = num / (fmax((double)nm, 1e-60) * __ldg(best.energy));
+        if (best_index == 0x7fffffff || orient_better(value, j, best_value, best_index)) {
+          best_value = value;
+          best_index = j;
+        }
+      } else {
+        o[3 * j] = acc0.x + acc0.y;
+        o[3 * j + 1] = acc1.x + acc1.y;
+        o[3 * j + 2] = acc2.x + acc2.y;
+      }
+    }
+  }
+  if (BEST) {
+    for (int off = 16; off > 0; off >>= 1) {
+      const double ov = __shfl_xor_sync(kFull, best_value, off);
+      const int oi = __shfl_xor_sync(kFull, best_index, off);
+      if (oi != 0x7fffffff && (best_index == 0x7fffffff || orient_better(ov, oi, best_value, best_index))) {
+        best_value = ov;
+        best_index = oi;
+      }
+    }
+    if (lane == 0) {
+      best.which[s] = best_index;
+      best.top[s] = (float)best_value;
     }
   }
 }
@@ -1037,18 +1270,26 @@ struct OrientLaunch {
   Consts c; const float* pos; int A; const float* cen; const float* nrm; int C; const float* bank;
   int nb; const float2* res; const float2* table; const float* ntab; int ov; float* out;
   cudaStream_t st;
+  OrientBest best{};  // selection mode when best.which is set
   template <int P>
   int run() {
     const int tuned = dsg_tuning_value(DSG_TUNE_ORIENT_WARPS);
     const int warps = tuned > 0 && tuned <= kOrientWarps ? tuned : kOrientWarps;
     const size_t smem = (((c.N + c.K + 3) & ~3) + warps * 32 * kOrientRec) * sizeof(float);
     const dim3 grid((C + warps - 1) / warps);
-    if (c.fresnel_n > 1.0f)
-      orientations_kernel<P, true><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res, table,
-                                                                   ntab, ov, out);
+    const bool fresnel = c.fresnel_n > 1.0f, select = best.which != nullptr;
+    if (fresnel && select)
+      orientations_kernel<P, true, true><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res,
+                                                                         table, ntab, ov, out, best);
+    else if (fresnel)
+      orientations_kernel<P, true, false><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res,
+                                                                          table, ntab, ov, out, best);
+    else if (select)
+      orientations_kernel<P, false, true><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res,
+                                                                          table, ntab, ov, out, best);
     else
-      orientations_kernel<P, false><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res, table,
-                                                                    ntab, ov, out);
+      orientations_kernel<P, false, false><<<grid, warps * 32, smem, st>>>(c, pos, A, cen, nrm, C, bank, nb, res,
+                                                                           table, ntab, ov, out, best);
     dsg_count_launches(1);
     return launch_status();
   }
@@ -1084,6 +1325,57 @@ int dsg_surfel_render(const DsgChirp* chirp, const float* positions, int32_t ape
                  reinterpret_cast<const float2*>(weights), surfels, reinterpret_cast<float2*>(out),
                  reinterpret_cast<float2*>(workspace), render_segments(chirp, apertures, surfels), st};
   return dispatch_kp(chirp->num_bins, chirp->pad, L);
+}
+
+size_t dsg_surfel_render_samples_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels) {
+  if (!chirp_ok(chirp) || apertures <= 0 || surfels <= 0) return 0;
+  const int seg = render_segments(chirp, apertures, surfels);
+  if (seg <= 1) return 0;
+  return (size_t)seg * apertures * chirp->samples * 2 * sizeof(float);
+}
+
+int dsg_surfel_render_samples(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                              const float* centers, const float* normals, const float* weights,
+                              int32_t surfels, float* samples, void* workspace, size_t workspace_bytes,
+                              int32_t* status, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  const int spl = chirp->samples / 8;
+  if (chirp->samples % 8 != 0 || !(spl == 2 || spl == 4 || spl == 8 || spl == 16 || spl == 32))
+    return DSG_ERR_UNSUPPORTED;
+  if (apertures < 0 || surfels < 0 || (apertures > 0 && (!positions || !samples))) return DSG_ERR_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (apertures == 0) return DSG_OK;
+  if (surfels == 0) {
+    cudaMemsetAsync(samples, 0, (size_t)apertures * chirp->samples * 2 * sizeof(float), st);
+    return launch_status();
+  }
+  if (!centers || !normals || !weights || !status) return DSG_ERR_ARGUMENT;
+  const size_t need = dsg_surfel_render_samples_workspace_bytes(chirp, apertures, surfels);
+  if (need > 0 && (workspace == nullptr || workspace_bytes < need)) return DSG_ERR_WORKSPACE;
+  const Consts c = make_consts(*chirp);
+  const int seg = render_segments(chirp, apertures, surfels);
+  const int seg_len = ((surfels + seg - 1) / seg + 31) / 32 * 32;  // whole chunks: 16-byte-aligned copies
+  const int nseg = (surfels + seg_len - 1) / seg_len;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(centers) | reinterpret_cast<uintptr_t>(normals) |
+                         reinterpret_cast<uintptr_t>(weights)) & 15u) == 0;
+  dim3 grid((apertures + 15) / 16, nseg > 0 ? nseg : 1);
+  float2* dst = grid.y == 1 ? reinterpret_cast<float2*>(samples) : reinterpret_cast<float2*>(workspace);
+  const float2* w = reinterpret_cast<const float2*>(weights);
+  switch (spl) {
+    case 2: render_adc_kernel<2><<<grid, 128, 0, st>>>(c, positions, apertures, centers, normals, w, surfels, seg_len, aligned, dst, status); break;
+    case 4: render_adc_kernel<4><<<grid, 128, 0, st>>>(c, positions, apertures, centers, normals, w, surfels, seg_len, aligned, dst, status); break;
+    case 8: render_adc_kernel<8><<<grid, 128, 0, st>>>(c, positions, apertures, centers, normals, w, surfels, seg_len, aligned, dst, status); break;
+    case 16: render_adc_kernel<16><<<grid, 128, 0, st>>>(c, positions, apertures, centers, normals, w, surfels, seg_len, aligned, dst, status); break;
+    default: render_adc_kernel<32><<<grid, 128, 0, st>>>(c, positions, apertures, centers, normals, w, surfels, seg_len, aligned, dst, status); break;
+  }
+  dsg_count_launches(1);
+  if (grid.y > 1) {
+    const int64_t n = (int64_t)apertures * chirp->samples;
+    segment_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<const float2*>(workspace),
+                                                                     grid.y, n, reinterpret_cast<float2*>(samples));
+    dsg_count_launches(1);
+  }
+  return launch_status();
 }
 
 int dsg_surfel_jvp(const DsgChirp* chirp, const float* positions, int32_t apertures,
@@ -1399,6 +1691,27 @@ int dsg_surfel_correlate_orientations(const DsgChirp* chirp, const float* positi
                  bank_size, reinterpret_cast<const float2*>(residual),
                  reinterpret_cast<const float2*>(range_table), norm_table,
                  use_table ? oversample : 1, out, st};
+  return dispatch_p(chirp->pad, L);
+}
+
+int dsg_surfel_orient_best(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                           const float* centers, const float* normals, const float* areas, int32_t candidates,
+                           const float* bank, int32_t bank_size, const float* residual, const float* range_table,
+                           const float* norm_table, int32_t oversample, const double* energy, int32_t real_mode,
+                           int32_t* which, float* top, void* stream) {
+  if (!chirp_ok(chirp)) return DSG_ERR_UNSUPPORTED;
+  if (apertures <= 0 || candidates < 0 || bank_size < 0) return DSG_ERR_ARGUMENT;
+  if (candidates == 0) return DSG_OK;
+  if (!positions || !centers || !normals || !areas || !energy || !which || !top || (bank_size > 0 && !bank))
+    return DSG_ERR_ARGUMENT;
+  const bool use_table = range_table != nullptr;
+  if (use_table && (!norm_table || oversample < 1)) return DSG_ERR_ARGUMENT;
+  if (!use_table && !residual) return DSG_ERR_ARGUMENT;
+  OrientLaunch L{make_consts(*chirp), positions, apertures, centers, normals, candidates, bank,
+                 bank_size, reinterpret_cast<const float2*>(residual),
+                 reinterpret_cast<const float2*>(range_table), norm_table,
+                 use_table ? oversample : 1, nullptr, (cudaStream_t)stream};
+  L.best = OrientBest{areas, energy, real_mode != 0, which, top};
   return dispatch_p(chirp->pad, L);
 }
 

@@ -321,6 +321,10 @@ class FMCWModel:
         return surfel.correlate_orientations(*self.sensor, params, bank, residual.reshape(self.shape),
                                              self.fresnel_n, table)  # fmt: skip
 
+    def orient_best(self, params, residual, bank, energy, real_mode, table=None):
+        return surfel.orient_best(*self.sensor, params, bank, residual.reshape(self.shape), energy, real_mode,
+                                  self.fresnel_n, table)  # fmt: skip
+
     # -- spatial-search helpers --------------------------------------------------------------------
 
     @torch.no_grad()

@@ -16,11 +16,29 @@ from contextlib import contextmanager
 import torch
 
 
+_SIDE_STREAMS: dict = {}
+
+
+def side_stream(device=None):
+    """This device's one second stream for work beside the current stream.
+
+    One stream per device, not a new one per use: PyTorch's caching allocator keeps the
+    blocks freed by a stream for that stream, so work that allocates gigabytes (Gram row
+    stores) on ever new streams would take new device memory every time.
+    """
+    device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    stream = _SIDE_STREAMS.get(device.index)
+    if stream is None:
+        stream = torch.cuda.Stream(device)
+        _SIDE_STREAMS[device.index] = stream
+    return stream
+
+
 @contextmanager
 def recording(graph):
     """Capture the launches of the block into graph (a torch.cuda.CUDAGraph)."""
     current = torch.cuda.current_stream()
-    side = torch.cuda.Stream(current.device)
+    side = side_stream(current.device)
     side.wait_stream(current)
     with torch.cuda.stream(side):
         graph.capture_begin()

@@ -90,6 +90,8 @@ SIGNATURES = {
     "dsg_tuning_get": (I32, [I32]),
     "dsg_surfel_render_workspace_bytes": (SZ, [CP, I32, I32]),
     "dsg_surfel_render": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, SZ, P]),
+    "dsg_surfel_render_samples_workspace_bytes": (SZ, [CP, I32, I32]),
+    "dsg_surfel_render_samples": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, P, SZ, P, P]),
     "dsg_surfel_render_scenes_workspace_bytes": (SZ, [RSP, I32]),
     "dsg_surfel_render_scenes": (ctypes.c_int, [RSP, I32, P, SZ, P, P]),
     "dsg_surfel_jvp": (ctypes.c_int, [CP, P, I32, P, P, P, P, P, P, I32, P, P, SZ, P]),
@@ -112,6 +114,7 @@ SIGNATURES = {
         ctypes.c_int,
         [CP, P, I32, P, P, I32, P, I32, P, P, P, I32, P, P],
     ),
+    "dsg_surfel_orient_best": (ctypes.c_int, [CP, P, I32, P, P, P, I32, P, I32, P, P, P, I32, P, I32, P, P, P]),
     "dsg_surfel_design": (ctypes.c_int, [CP, P, I32, P, P, P, I32, I32, P, P]),
     "dsg_surfel_jacobian": (ctypes.c_int, [CP, P, I32, P, P, I32, P, P, P]),
     "dsg_spectral_axis_tables": (ctypes.c_int, [GP, P, P, I32, P, P, P]),

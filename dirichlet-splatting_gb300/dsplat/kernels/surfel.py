@@ -21,9 +21,9 @@ from ._lib import call, f32, ptr, real_view
 # FP32 flops per counting unit (pair-bin; pair-normal for the normal bank) used for the
 # roofline accounting of the FP32-issue-bound kernels.
 FLOPS_PER_UNIT = {
-    "dsg_surfel_render": 16, "dsg_surfel_jvp": 24, "dsg_surfel_vjp": 20, "dsg_surfel_correlate": 18,
+    "dsg_surfel_render": 16, "dsg_surfel_render_samples": 6, "dsg_surfel_jvp": 24, "dsg_surfel_vjp": 20, "dsg_surfel_correlate": 18,
     "dsg_surfel_correlate_active": 18, "dsg_surfel_correlate_gradient": 30,
-    "dsg_surfel_correlate_orientations": 12,
+    "dsg_surfel_correlate_orientations": 12, "dsg_surfel_orient_best": 12,
 }  # fmt: skip
 
 
@@ -62,8 +62,56 @@ def _outputs(centers, *shape, dtype=torch.float32):
     return torch.empty(shape, dtype=dtype, device=centers.device)
 
 
+# How the forward evaluates the profiles: "bins" sums the closed-form kernel over the range
+# bins (dsg_surfel_render); "samples" sums the pairs' ADC samples by phasor recurrence and
+# takes the N-point FFT (dsg_surfel_render_samples + cuFFT).
+RENDER_FORMS = ("bins", "samples")
+_RENDER_FORM = ["bins"]
+
+
+@contextmanager
+def render_form(name):
+    """Inside the block the forward uses form name ("bins", the default, or "samples")."""
+    if name not in RENDER_FORMS:
+        raise KeyError(name)
+    previous, _RENDER_FORM[0] = _RENDER_FORM[0], name
+    try:
+        yield
+    finally:
+        _RENDER_FORM[0] = previous
+
+
+def render_samples(config, positions, centers, normals, weights, fresnel_n, status=None):
+    """ADC samples y [A, S] complex64 whose N-point FFT's first K bins are the profiles.
+
+    status, an int32 device tensor of one element, is set to 1 if a surfel copy never
+    arrived (the affected samples are then NaN); by default a scratch word is used.
+    """
+    positions, centers, normals = f32(positions), f32(centers), f32(normals)
+    w = real_view(weights)
+    chirp = _lib.chirp(config, fresnel_n)
+    count, apertures = len(centers), len(positions)
+    _tuned("splat", config, apertures, count, centers.device)
+    out = _outputs(centers, apertures, config.adc_samples, 2)
+    if status is None:
+        status = torch.zeros(1, dtype=torch.int32, device=centers.device)
+    nbytes = _lib.query("dsg_surfel_render_samples_workspace_bytes", chirp, apertures, count)
+    work, nbytes = _lib.workspace(nbytes, centers.device)
+    _work("dsg_surfel_render_samples", len(positions) * len(centers) * config.adc_samples)
+    call(
+        "dsg_surfel_render_samples", chirp, ptr(positions), apertures, ptr(centers), ptr(normals), ptr(w),
+        count, ptr(out), ptr(work), nbytes, ptr(status), _lib.stream(centers.device),
+    )  # fmt: skip
+    return torch.view_as_complex(out)
+
+
 def _profiles(config, positions, centers, normals, weights, fresnel_n):
     """Range profiles [A, K, 2] of weights [S, 2] (interleaved complex)."""
+    if _RENDER_FORM[0] == "samples":
+        samples = render_samples(config, positions, centers, normals, torch.view_as_complex(weights.contiguous()),
+                                 fresnel_n)  # fmt: skip
+        spectrum = torch.fft.fft(samples, n=config.n_fft, dim=1)[:, : config.num_range_bins]
+        return torch.view_as_real(spectrum.contiguous()).contiguous()
     positions, centers, normals = f32(positions), f32(centers), f32(normals)
     weights = weights.contiguous()
     chirp = _lib.chirp(config, fresnel_n)
@@ -307,6 +355,33 @@ def correlate_orientations(config, positions, centers, normals, bank, residual, 
         ptr(nt), oversample, ptr(out), _lib.stream(centers.device),
     )  # fmt: skip
     return torch.complex(out[..., 0], out[..., 1]), out[..., 2]
+
+
+def orient_best(config, positions, centers, normals, areas, bank, residual, fresnel_n, energy, real_mode,
+                table=None):  # fmt: skip
+    """(which [S] int64, top [S] float32): each candidate's best normal (0 = its own, j = bank
+    row j - 1) and its certificate, as correlate_orientations scaled by the areas and the
+    selection of certificate.orient_candidates, in one launch. energy: a float64 device
+    scalar (the residual's energy)."""
+    positions, centers, normals, bank, areas = f32(positions), f32(centers), f32(normals), f32(bank), f32(areas)
+    chirp = _lib.chirp(config, fresnel_n)
+    count = len(centers)
+    _tuned("orient", config, len(positions), 0, centers.device)
+    which = _outputs(centers, count, dtype=torch.int32)
+    top = _outputs(centers, count)
+    if table is None:
+        r, rt, nt, oversample = real_view(residual), None, None, 1
+    else:
+        r, rt, nt = None, f32(table.correlation), f32(table.norm)
+        oversample = table.oversample
+    energy = energy.to(torch.float64).reshape(1).contiguous()
+    _work("dsg_surfel_orient_best", len(positions) * count * (len(bank) + 1))
+    call(
+        "dsg_surfel_orient_best", chirp, ptr(positions), len(positions), ptr(centers), ptr(normals), ptr(areas),
+        count, ptr(bank) if len(bank) else None, len(bank), ptr(r), ptr(rt), ptr(nt), oversample, ptr(energy),
+        int(bool(real_mode)), ptr(which), ptr(top), _lib.stream(centers.device),
+    )  # fmt: skip
+    return which.long(), top
 
 
 def correlate_gradient(config, positions, centers, normals, residual, fresnel_n, include_normals, tables=None):

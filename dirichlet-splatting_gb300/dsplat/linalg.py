@@ -20,7 +20,7 @@ from __future__ import annotations
 
 import torch
 
-from .graphs import recording
+from .graphs import recording, side_stream
 
 POWER_STEPS = 24  # power iterations for the largest eigenvalue of a Gram
 SHIFT_RETRIES = 4
@@ -249,7 +249,7 @@ def _pcg_graphed(operator, rhs, diagonal, iterations, tolerance):
         live.copy_(going)
 
     device = rhs.device
-    side = torch.cuda.Stream(device)
+    side = side_stream(device)
     side.wait_stream(torch.cuda.current_stream(device))
     timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be recorded inside a capture
     try:
@@ -267,3 +267,78 @@ def _pcg_graphed(operator, rhs, diagonal, iterations, tolerance):
     finally:
         _lib.TIMERS = timers
     return x.clone()
+
+
+class GraphedPCG:
+    """pcg's iterations replayed from one CUDA graph kept across solves of the same shapes.
+
+    The operator must read only tensors whose addresses stay fixed (the caller refills
+    them between solves); the iterates live in static buffers here. Construction runs one
+    iteration eagerly (the capture's warm-up) and captures the next; every solve then
+    reloads the start (x = 0, r = rhs, p = r / diagonal) and replays all iterations, with no
+    device read. The arithmetic is that of pcg.
+    """
+
+    def __init__(self, operator, rhs, diagonal, iterations, tolerance):
+        from .kernels import _lib
+
+        self.iterations, self.tolerance = iterations, tolerance
+        self.diagonal = diagonal.clone()
+        self.x = torch.zeros_like(rhs)
+        self.r = rhs.clone()
+        self.p = torch.zeros_like(rhs)
+        self.rz = rhs.new_zeros(())
+        self.goal = rhs.new_zeros(())
+        self.live = torch.ones((), dtype=torch.bool, device=rhs.device)
+        x, r, p, rz, live, goal, diag = self.x, self.r, self.p, self.rz, self.live, self.goal, self.diagonal
+
+        def iteration():
+            hp = operator(p)
+            curvature = p @ hp
+            moving = live & (curvature > 0)
+            alpha = rz / curvature
+            x.copy_(torch.where(moving, x + alpha * p, x))
+            r_next = torch.where(moving, r - alpha * hp, r)
+            going = moving & (r_next.norm() > goal)
+            z = r_next / diag
+            rz_next = r_next @ z
+            p.copy_(torch.where(going, z + (rz_next / rz) * p, p))
+            rz.copy_(torch.where(going, rz_next, rz))
+            r.copy_(r_next)
+            live.copy_(going)
+
+        device = rhs.device
+        timers, _lib.TIMERS = _lib.TIMERS, None  # events cannot be recorded inside a capture
+        try:
+            self._load(rhs, diagonal)
+            side = side_stream(device)
+            side.wait_stream(torch.cuda.current_stream(device))
+            with torch.cuda.stream(side):
+                iteration()  # warm-up: lazy library set-up happens outside the capture
+            torch.cuda.current_stream(device).wait_stream(side)
+            self.graph = torch.cuda.CUDAGraph()
+            before = _lib.library().dsg_launch_count()
+            with recording(self.graph):
+                iteration()
+            self.per_replay = _lib.library().dsg_launch_count() - before
+        finally:
+            _lib.TIMERS = timers
+
+    def _load(self, rhs, diagonal):
+        self.diagonal.copy_(diagonal)
+        self.x.zero_()
+        self.r.copy_(rhs)
+        torch.div(rhs, diagonal, out=self.p)
+        self.rz.copy_(rhs @ self.p)
+        self.goal.copy_(self.tolerance * rhs.norm())
+        self.live.fill_(True)
+
+    def solve(self, rhs, diagonal):
+        """pcg(operator, rhs, diagonal) over the operator's current static inputs."""
+        from .kernels import _lib
+
+        self._load(rhs, diagonal)
+        for _ in range(self.iterations):
+            self.graph.replay()
+        _lib.REPLAYED_LAUNCHES += self.per_replay * self.iterations
+        return self.x.clone()

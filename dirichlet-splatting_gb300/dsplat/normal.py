@@ -217,19 +217,37 @@ class TensorCoreGram:
         self.store.append(a)
         self.rhs += a.T @ y
 
-    def finish(self, column_from=0):
+    def finish(self, column_from=0, deferred=False):
+        """(total, rhs); deferred also returns the Gram's status word unread (else checked)."""
         from .kernels.gram import check
 
-        check(self.store.accumulate(self.total, column_from=column_from))
+        status = self.store.accumulate(self.total, column_from=column_from)
+        if deferred:
+            return self.total, self.rhs, status
+        check(status)
         return self.total, self.rhs
 
 
-def normal_equations(model, params, target, config):
+def normal_equations(model, params, target, config, deferred=False):
     """(G, q) = (A^H A / M, A^H y / M) of params, streamed over projected row blocks.
 
     Real coefficients return float32 real G and q (float64 accumulation inside);
-    complex coefficients return complex G and q accumulated in complex64.
+    complex coefficients return complex G and q accumulated in complex64. deferred returns
+    ((G, q), statuses) without reading anything back: the kernels' status words, which
+    the caller checks (kernels.gram.check) before it uses G and q.
     """
+    statuses = []
+    out = _normal_equations(model, params, target, config, statuses)
+    if deferred:
+        return out, statuses
+    from .kernels.gram import check
+
+    for status in statuses:
+        check(status)
+    return out
+
+
+def _normal_equations(model, params, target, config, statuses):
     count = len(params["centers"])
     chunk = row_chunk(model, count, config)
     if not config.real:
@@ -248,13 +266,12 @@ def normal_equations(model, params, target, config):
             for a, y in model.blocks(params, target, True, chunk):
                 acc.add(a, y)
         else:
-            from .kernels.gram import check
-
             acc.rhs += model.correlate(params, target)[0].real.double()
-            check(status)
+            statuses.append(status)
             if merged:
                 PROJECTIONS.put(model, params, acc.store, chunk)
-        total, rhs = acc.finish()
+        total, rhs, gram_status = acc.finish(deferred=True)
+        statuses.append(gram_status)
     else:
         acc = Fp32Syrk(count, device)
         for a, y in model.blocks(params, target, True, chunk):

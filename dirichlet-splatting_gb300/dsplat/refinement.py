@@ -18,6 +18,7 @@ from __future__ import annotations
 import torch
 
 from .linalg import pcg, solve
+from .graphs import side_stream
 from .tracing import stage
 from .varpro import accept, fit_coefficients, screen_bar
 
@@ -194,12 +195,12 @@ class _JointLayout:
         return total.sqrt()
 
 
-def joint_system(model, params, coefficients, target, specs, config, seed):
+def joint_system(model, params, coefficients, target, specs, config, seed, pieces=None):
     """Scaled Gauss-Newton system of every trainable geometry component and coefficient.
 
     Returns (matvec, gradient, damped Jacobi diagonal, proposal(vector, fraction)).
     Products use the model's exact JVP and VJP; the Rademacher probes only estimate the
-    diagonal.
+    diagonal. pieces, a dict, receives what matvec reads (b, layout, normalization, shift).
     """
     b = coefficients.to(target.dtype)
     layout = _JointLayout(params, specs, b, not config.real)
@@ -226,6 +227,8 @@ def joint_system(model, params, coefficients, target, specs, config, seed):
     diagonal = diagonal.clamp(min=diagonal.max().clamp(min=1e-30) * 1e-6)
     damping = config.damping * diagonal
     shift = ridge_diagonal + damping
+    if pieces is not None:
+        pieces.update(b=b, layout=layout, normalization=normalization, shift=shift)
 
     def matvec(vector):
         return adjoint(model.jvp(params, b, *layout.unpack(vector))) / normalization + shift * vector
@@ -239,6 +242,60 @@ def joint_system(model, params, coefficients, target, specs, config, seed):
                 for key, value in params.items()}  # fmt: skip
 
     return matvec, gradient, diagonal + damping, proposal
+
+
+class _StaticJoint:
+    """The joint system's matrix-vector product over fixed buffers (sensor positions of the
+    aperture subset, parameters, coefficients, the layout's coefficient scale, the
+    normalization and the damping shift), refilled per slide, so that one CUDA graph of the
+    conjugate-gradient iteration serves every slide of the same shapes."""
+
+    def __init__(self, model, params, specs, pieces, complex_mode):
+        from dataclasses import replace
+
+        self.positions = model.scan.scan_positions_m.clone()
+        self.model = replace(model, scan=replace(model.scan, scan_positions_m=self.positions))
+        self.params = {key: value.clone() for key, value in params.items()}
+        self.b = pieces["b"].clone()
+        self.layout = _JointLayout(self.params, specs, self.b, complex_mode)
+        self.normalization = pieces["normalization"].clone()
+        self.shift = pieces["shift"].clone()
+        self.refill(model, params, pieces)
+
+    def refill(self, model, params, pieces):
+        self.positions.copy_(model.scan.scan_positions_m)
+        for key, value in params.items():
+            self.params[key].copy_(value)
+        self.b.copy_(pieces["b"])
+        self.layout.amplitude.copy_(pieces["layout"].amplitude)
+        self.layout.coefficient_scale.copy_(pieces["layout"].coefficient_scale)
+        self.normalization.copy_(pieces["normalization"])
+        self.shift.copy_(pieces["shift"])
+
+    def matvec(self, vector):
+        grads, coefficient = self.model.vjp(self.params, self.b,
+                                            self.model.jvp(self.params, self.b, *self.layout.unpack(vector)))  # fmt: skip
+        return self.layout.pack_gradient(grads, coefficient) / self.normalization + self.shift * vector
+
+
+_JOINT_GRAPHS: dict = {}
+
+
+def _graphed_joint_pcg(model, params, specs, config, pieces, rhs, diagonal):
+    """The joint slide's conjugate gradients from a CUDA graph kept across slides (batched)."""
+    from .linalg import GraphedPCG
+
+    key = (tuple(model.shape), repr(model.scan.fmcw_config), model.fresnel_n, repr(specs), config.real,
+           config.cg_iterations, config.cg_tolerance, rhs.shape, rhs.dtype, rhs.device,
+           tuple((k, tuple(v.shape), v.dtype) for k, v in params.items()), pieces["b"].dtype)  # fmt: skip
+    entry = _JOINT_GRAPHS.get(key)
+    if entry is None:
+        static = _StaticJoint(model, params, specs, pieces, not config.real)
+        solver = GraphedPCG(static.matvec, rhs, diagonal, config.cg_iterations, config.cg_tolerance)
+        _JOINT_GRAPHS[key] = entry = (static, solver)
+    else:
+        entry[0].refill(model, params, pieces)
+    return entry[1].solve(rhs, diagonal)
 
 
 @torch.no_grad()
@@ -259,19 +316,24 @@ def joint_slide(state, config, screen=None):
         if overlap:  # the state's tensors are complete in stream order here
             ready = torch.cuda.Event()
             ready.record()
+        pieces = {}
         with stage("slide.system"):
             matvec, gradient, diagonal, proposal = joint_system(
                 model, state.params, state.coefficients, target, state.parameters, config,
-                config.seed + state.iteration + inner)  # fmt: skip
+                config.seed + state.iteration + inner, pieces=pieces)  # fmt: skip
         with stage("slide.pcg"):
-            delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations, tolerance=config.cg_tolerance,
-                        capture=getattr(config, "batched", False))  # fmt: skip
+            if getattr(config, "batched", False) and target.is_cuda and config.cg_iterations > 1 and \
+                    hasattr(model, "scan"):  # fmt: skip
+                delta = _graphed_joint_pcg(model, state.params, state.parameters, config, pieces, -gradient, diagonal)
+            else:
+                delta = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations,
+                            tolerance=config.cg_tolerance, capture=getattr(config, "batched", False))  # fmt: skip
         if overlap:
             # The screening objective of the current geometry needs neither the system
             # nor its solution: it runs on a second stream while the conjugate gradients
             # (enqueued above) run on this one, and is simply unused if no step follows.
             current = torch.cuda.current_stream()
-            side = torch.cuda.Stream(current.device)
+            side = side_stream(current.device)
             side.wait_event(ready)
             with torch.cuda.stream(side), stage("slide.screen"):
                 bar = screen_bar(screen, state.params, config)

@@ -109,8 +109,9 @@ class _Proposer:
         """Certificates on the sampled apertures; with a bank, the candidates take their best normal."""
         if not self.banked:
             return certificate(self.model, candidates, self.sub_residual, self.mode)
+        fused = getattr(self.config, "batched", False) and hasattr(self.model, "orient_best")
         oriented, scores = orient_candidates(self.model, candidates, self.sub_residual, self.search.normal_candidates,
-                                             self.mode, self.table)  # fmt: skip
+                                             self.mode, self.table, fused=fused)  # fmt: skip
         candidates["normals"] = oriented["normals"]
         return scores
 

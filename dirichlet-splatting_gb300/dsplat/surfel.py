@@ -103,6 +103,12 @@ def correlate_orientations(config, positions, params, bank, residual, fresnel_n=
     return corr * root, norm * root.square()
 
 
+def orient_best(config, positions, params, bank, residual, energy, real_mode, fresnel_n=0.0, table=None):
+    """(which, top): each surfel's best normal among its own and the bank's, and its certificate."""
+    return kernel.orient_best(config, positions, params["centers"], params["normals"], params["areas"], bank,
+                              residual, fresnel_n, energy, real_mode, table)  # fmt: skip
+
+
 # --- Range / Doppler / azimuth composition (13 degrees of freedom per surfel) ----------------
 # Reference: dsplat/surfel.py:132-196. A surfel has position [3], normal [3], area,
 # complex reflectivity, velocity [3] and complex material impedance; a monostatic

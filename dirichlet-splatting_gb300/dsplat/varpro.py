@@ -29,6 +29,7 @@ from .linalg import (  # noqa: F401  (names of the reference's varpro module)
     solve,
 )
 from .normal import FOLD, fused_rows, normal_equations, projected_rows, row_chunk  # noqa: F401
+from .graphs import side_stream
 from .tracing import stage
 
 
@@ -106,10 +107,16 @@ def _refit(model, params, target, config, gram, rhs):
 
 
 @torch.no_grad()
-def varpro(model, params, target, config):
-    """Coefficients, prediction, objective, Gram and right-hand side of one geometry."""
-    with stage("varpro.normal"):
-        gram, rhs = normal_equations(model, params, target, config)
+def varpro(model, params, target, config, normal=None):
+    """Coefficients, prediction, objective, Gram and right-hand side of one geometry.
+
+    normal, when given, is this geometry's (Gram, right-hand side), already formed.
+    """
+    if normal is not None:
+        gram, rhs = normal
+    else:
+        with stage("varpro.normal"):
+            gram, rhs = normal_equations(model, params, target, config)
     with stage("varpro.solve"):
         coefficients = refined_coefficients(model, params, target, gram, rhs, config)
     with stage("varpro.loss"):
@@ -159,6 +166,35 @@ def changed_slots(params, proposal):
     return total, first
 
 
+def _early_normal(state, proposal, config):
+    """The full normal equations of proposal, enqueued on a second stream (batched mode).
+
+    The screening refit that decides whether they are needed is latency bound (small
+    kernels and a few device reads), so the large projection and Gram launches of the full
+    system run beside it instead of after it; a rejected proposal only wastes them.
+    """
+    current = torch.cuda.current_stream()
+    side = side_stream(current.device)
+    side.wait_stream(current)
+    with torch.cuda.stream(side), stage("varpro.normal"):
+        normal, statuses = normal_equations(state.model, proposal, state.target, config, deferred=True)
+    return side, normal, statuses
+
+
+def _finish_normal(early):
+    """(Gram, right-hand side) of _early_normal, ordered after its stream and checked."""
+    from .kernels.gram import check
+
+    side, normal, statuses = early
+    current = torch.cuda.current_stream()
+    current.wait_stream(side)
+    for tensor in (*normal, *statuses):
+        tensor.record_stream(current)  # made on the side stream, used and freed on this one
+    for status in statuses:
+        check(status)
+    return normal
+
+
 @torch.no_grad()
 def accept(state, proposal, config, screen=None):
     """The state with proposal installed if its refitted objective is lower, else None.
@@ -170,12 +206,19 @@ def accept(state, proposal, config, screen=None):
     total, first = changed_slots(state.params, proposal)
     if total == 0:
         return None
+    early = None
     if screen is not None:
         model, target, bar = screen
+        if total > 1 and getattr(config, "batched", False) and state.target.is_cuda:
+            early = _early_normal(state, proposal, config)
         if varpro(model, proposal, target, config).objective > bar + 1e-4 * state.power:
+            if early is not None:
+                torch.cuda.current_stream().wait_stream(early[0])  # its memory is reused after this
             return None
     if total == 1:
         fit = exchange_varpro(state, proposal, first, config)
+    elif early is not None:
+        fit = varpro(state.model, proposal, state.target, config, normal=_finish_normal(early))
     else:
         fit = varpro(state.model, proposal, state.target, config)
     if not fit.objective < state.objective:

@@ -152,6 +152,23 @@ int dsg_surfel_jvp(const DsgChirp* chirp, const float* positions, int32_t apertu
 size_t dsg_surfel_reduce_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels,
                                          int32_t values_per_surfel);
 
+/* The forward through the ADC samples instead of the range bins (no counterpart in the
+ * reference, whose render_bins sums the closed-form kernel over bins,
+ * dsplat/kernels/surfel.slang:87-142): samples [A, samples] complex receives
+ * y[a][n] = sum_s w_s c_s / samples exp(2 pi i n k0_s / n_fft), whose n_fft-point FFT
+ * (negative exponent, zero padded) has the profiles of dsg_surfel_render as its first
+ * num_bins entries. A pair's samples are a geometric sequence: each lane anchors its run of
+ * samples / 8 consecutive samples exactly and advances by one complex multiply per sample;
+ * surfel chunks are staged in shared memory by bulk copies when centers, normals and
+ * weights are 16-byte aligned. samples / 8 must be 2, 4, 8, 16 or 32. status (one int32,
+ * zeroed by the caller) becomes 1 if a copy never arrived; the affected samples are NaN.
+ * Workspace: dsg_surfel_render_samples_workspace_bytes. */
+size_t dsg_surfel_render_samples_workspace_bytes(const DsgChirp* chirp, int32_t apertures, int32_t surfels);
+int dsg_surfel_render_samples(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                              const float* centers, const float* normals, const float* weights,
+                              int32_t surfels, float* samples, void* workspace, size_t workspace_bytes,
+                              int32_t* status, void* stream);
+
 /* Gradients of Re(conj(upstream) . profiles) (reference: dsplat/kernels/surfel.py:123-137
  * vjp). upstream [A,K] complex; grad_centers/grad_normals [S,3]; grad_weights [S] complex.
  * Summed over apertures in a fixed order, in double precision across aperture chunks. */
@@ -261,6 +278,21 @@ int dsg_surfel_correlate_orientations(const DsgChirp* chirp, const float* positi
                                       int32_t bank_size, const float* residual,
                                       const float* range_table, const float* norm_table,
                                       int32_t oversample, float* out, void* stream);
+
+/* The best normal of each candidate among its own and the bank's, with its certificate, in one
+ * launch: dsg_surfel_correlate_orientations followed by the selection of
+ * dsplat/certificate.py orient_candidates (reference: dsplat/certificate.py, the normal-bank
+ * scoring of the spatial search), without writing the [C, 1 + Nb, 3] scores. Per normal the
+ * certificate is |Re corr|^2 (real_mode) or |corr|^2 over max(norm, 1e-60) * energy in
+ * double precision, corr and norm scaled first by sqrt(area) and area in float32; which [C]
+ * receives the winning index (0 = the candidate's own normal, j = bank row j - 1; NaN
+ * first, then the largest, ties to the lowest index) and top [C] its certificate. energy is
+ * one double on the device (the residual's energy); areas [C]. */
+int dsg_surfel_orient_best(const DsgChirp* chirp, const float* positions, int32_t apertures,
+                           const float* centers, const float* normals, const float* areas, int32_t candidates,
+                           const float* bank, int32_t bank_size, const float* residual, const float* range_table,
+                           const float* norm_table, int32_t oversample, const double* energy, int32_t real_mode,
+                           int32_t* which, float* top, void* stream);
 
 /* Dictionary rows including sqrt(area) (reference: dsplat/kernels/surfel.py:199-220 design).
  * real != 0: out [2*A*K, S] with row (2k+part)*A + a; else out [A*K, S] complex. */

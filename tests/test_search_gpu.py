@@ -101,3 +101,33 @@ def test_peaks_in_every_dimension_and_dense_clusters(dimension, separation):
     for count in (1, 300, 4096):
         got = search.peaks(scores.cuda(), centers.cuda(), count, separation).cpu()
         assert got.tolist() == osearch.peaks(scores, centers, count, separation).tolist(), count
+
+
+@pytest.mark.parametrize("mode,fresnel,with_table,bank", [("real", 0.0, True, 24), ("complex", 0.0, True, 24),
+                                                         ("real", 1.6, False, 7), ("real", 0.0, True, 0),
+                                                         ("complex", 0.0, False, 40)])  # fmt: skip
+def test_fused_best_normal_selection_equals_the_scored_selection(mode, fresnel, with_table, bank):
+    """orient_candidates with the selection inside the normal-bank launch (dsg_surfel_orient_best)
+    against scoring every normal and selecting in PyTorch: the same normal for every candidate
+    whose best certificate is not tied to float64 rounding with another normal, and the same
+    certificates to float32 rounding; banks of 0 and more than 31 normals, exact bin sums and
+    the FFT table, Fresnel."""
+    from conftest import aperture_grid, surfels
+
+    from dsplat import FMCWConfig, FMCWModel, Scan
+    from dsplat.certificate import orient_candidates
+
+    config = FMCWConfig()
+    positions = aperture_grid(12)
+    generator = torch.Generator().manual_seed(3)
+    residual = torch.complex(torch.randn(len(positions), config.num_range_bins, generator=generator),
+                             torch.randn(len(positions), config.num_range_bins, generator=generator)).cuda()  # fmt: skip
+    model = FMCWModel(Scan(residual, positions, config), fresnel_n=fresnel)
+    params = surfels(3000, seed=4, spread=0.02)
+    params["areas"] = params["areas"] * (1 + torch.rand(3000, generator=generator).cuda())
+    table = model.range_table(residual, 8) if with_table else None
+    scored, scores = orient_candidates(model, params, residual, bank, mode, table)
+    fused, fused_scores = orient_candidates(model, params, residual, bank, mode, table, fused=True)
+    same = (scored["normals"] == fused["normals"]).all(1)
+    assert float(same.float().mean()) > 0.999, float(same.float().mean())
+    torch.testing.assert_close(fused_scores[same], scores[same], rtol=1e-6, atol=0)

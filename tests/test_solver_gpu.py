@@ -189,6 +189,30 @@ def test_graph_replayed_pcg_matches_the_eager_loop(fmcw, iterations, tolerance):
     close(replayed, eager, 1e-4)
 
 
+def test_graph_kept_across_slides_matches_the_eager_loop(fmcw):
+    """The batched joint slide's PCG graph, captured once and replayed for a second system
+    after its static inputs are refilled (other geometry, coefficients and aperture subset
+    of the same shapes), against the eager loop of each system."""
+    from dsplat import DSFWConfig
+    from dsplat.refinement import _JOINT_GRAPHS, _graphed_joint_pcg, joint_system
+    from dsplat.varpro import pcg
+
+    model, params, b = fmcw
+    config = DSFWConfig(batched=True)
+    _JOINT_GRAPHS.clear()
+    for shift, seed, scale in ((2e-4, 0, 1.0), (-3e-4, 5, 1.3)):
+        ids, sub = model.sample_apertures(40, seed)
+        trial = {**params, "centers": params["centers"] + shift}
+        pieces = {}
+        matvec, gradient, diagonal, _ = joint_system(sub, trial, b * scale, model.scan.data[ids], fmcw_specs(),
+                                                     config, seed, pieces=pieces)  # fmt: skip
+        eager = pcg(matvec, -gradient, diagonal, iterations=config.cg_iterations, tolerance=config.cg_tolerance)
+        kept = _graphed_joint_pcg(sub, trial, fmcw_specs(), config, pieces, -gradient, diagonal)
+        assert bool(torch.isfinite(kept).all())
+        close(kept, eager, 1e-4)
+    assert len(_JOINT_GRAPHS) == 1  # the second system replayed the first one's graph
+
+
 def test_fmcw_joint_system_is_symmetric(fmcw):
     from dsplat import DSFWConfig
     from dsplat.refinement import joint_system

@@ -330,3 +330,48 @@ def test_synthesize_matches_the_float64_oracle(pad, samples, fresnel):
                                 config, fresnel)  # fmt: skip
     assert scan.data.dtype == torch.complex64 and scan.data.shape == expected.shape
     assert rel_l2(scan.data, expected) < 1e-6
+
+
+@pytest.mark.parametrize("samples,pad,side,count", [(128, 2, 32, 256), (64, 4, 9, 37), (256, 1, 8, 70), (16, 4, 5, 9)])
+def test_forward_through_adc_samples_matches_the_oracle(samples, pad, side, count):
+    """dsg_surfel_render_samples + the n_fft-point FFT against the float64 closed form and the
+    bin-sum forward, with ragged surfel counts (the last chunk by plain loads), several
+    segments and a misaligned weight view (no bulk copies)."""
+    from dsplat.kernels import surfel as kernel
+
+    config = _cfg(adc_samples=samples, pad_factor=pad)
+    positions = aperture_grid(side)
+    params = surfels(count, seed=samples + pad, spread=0.03)
+    w = _weights(count, seed=pad)
+    expected = ofmcw.render(config, positions.cpu(), params["centers"].cpu(), params["normals"].cpu(), w.cpu())
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    y = kernel.render_samples(config, positions, params["centers"], params["normals"], w, 0.0, status=status)
+    via_samples = torch.fft.fft(y, n=config.n_fft, dim=1)[:, : config.num_range_bins]
+    bins = kernel.render(config, positions, params["centers"], params["normals"], w, 0.0)
+    assert int(status.item()) == 0
+    assert rel_l2(via_samples, expected) < FORWARD_TOL
+    assert rel_l2(via_samples, bins) < FORWARD_TOL
+    with kernel.render_form("samples"):
+        same = kernel.render(config, positions, params["centers"], params["normals"], w, 0.0)
+    torch.testing.assert_close(same, via_samples, rtol=0, atol=0)
+    # a weight view that starts 8 bytes into its storage: plain loads, same values
+    padded = torch.zeros(count + 1, dtype=torch.complex64, device="cuda")
+    padded[1:] = w
+    y2 = kernel.render_samples(config, positions, params["centers"], params["normals"], padded[1:], 0.0)
+    close(y2, y, 1e-6)
+
+
+def test_forward_through_adc_samples_at_full_size():
+    """The 128^2-array, 2000-surfel sphere cap: every row within 1e-5 of the bin-sum forward
+    (itself within 1e-5 of float64 at this size, tests/test_full_size_gpu.py)."""
+    from dsplat import FMCWConfig
+    from dsplat.kernels import surfel as kernel
+    from dsplat.workloads import sphere_cap
+
+    config = FMCWConfig()
+    positions, params, reflectivity = sphere_cap(device="cuda")
+    weights = (reflectivity * params["areas"].sqrt()).to(torch.complex64)
+    bins = kernel.render(config, positions, params["centers"], params["normals"], weights, 0.0)
+    with kernel.render_form("samples"):
+        via_samples = kernel.render(config, positions, params["centers"], params["normals"], weights, 0.0)
+    assert rel_l2(via_samples, bins) < FORWARD_TOL
