@@ -706,6 +706,20 @@ def run_kernels(args):
                      "frac_fp32": round(achieved / fp32_peak, 4)})  # fmt: skip
 
     it, wu = args.steps, args.warmup
+    if args.only == "orient":  # the spatial search's normal-bank selection alone (its ncu capture)
+        bank = fibonacci_sphere(24, device)
+        ncand = 200000 if args.case == "full" else 50000
+        grid = centers.repeat(ncand // S + 1, 1)[:ncand].contiguous()
+        grid_n = normals.repeat(ncand // S + 1, 1)[:ncand].contiguous()
+        grid_a = params["areas"].repeat(ncand // S + 1)[:ncand].contiguous()
+        prop = positions[: min(A, 384)].contiguous()
+        table = FMCWModel(Scan(upstream[: len(prop)], prop, config)).range_table(upstream[: len(prop)], 8)
+        energy = upstream[: len(prop)].abs().square().sum().double()
+        ms = _event_time(lambda: kernel.orient_best(config, prop, grid, grid_n, grid_a, bank, upstream[: len(prop)],
+                                                    0.0, energy, True, table), it, wu, flush)  # fmt: skip
+        record("dsg_surfel_orient_best", ms, len(prop) * len(grid) * 25, 12, "pair-normals")
+        print(json.dumps({"case": args.case, "apertures": len(prop), "candidates": ncand, "kernels": rows}), flush=True)
+        return
     ms = _event_time(lambda: kernel.render(config, positions, centers, normals, weights, 0.0), it, wu, flush)
     record("dsg_surfel_render", ms, A * S * K, 16)
     # the forward through the ADC samples: phasor recurrence (6 FP32 flops per pair-sample,
@@ -832,7 +846,8 @@ def main():
     parser.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison run")
     parser.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead")
     parser.add_argument("--case", choices=["small", "medium", "full"], default="full")
-    parser.add_argument("--only", choices=["all", "splat"], default="all", help="with --kernels: which kernels")
+    parser.add_argument("--only", choices=["all", "splat", "orient"], default="all",
+                        help="with --kernels: which kernels")  # fmt: skip
     parser.add_argument("--accuracy", type=int, default=0, help="final-accuracy study of both arms on N seeds")
     parser.add_argument("--no-autotune", action="store_true", help="keep every launch shape automatic")
     parser.add_argument("--workload", choices=["sphere_cap", "uneven"], default="sphere_cap",

@@ -927,7 +927,7 @@ __device__ __forceinline__ bool orient_better(double v, int i, double bv, int bi
 }
 
 template <int P, bool FRESNEL, bool BEST>
-__global__ void __launch_bounds__(kOrientWarps * 32) orientations_kernel(
+__global__ void __launch_bounds__(kOrientWarps * 32, 4) orientations_kernel(
     Consts c, const float* __restrict__ pos, int A, const float* __restrict__ cen,
     const float* __restrict__ nrm, int C, const float* __restrict__ bank, int bank_size,
     const float2* __restrict__ res, const float2* __restrict__ table,
