@@ -186,7 +186,8 @@ __global__ void __launch_bounds__(kPeakThreads, 1) peaks_kernel(const float* __r
   __shared__ float chunk_xyz[kPeakThreads * 3];  // hashed: the chunk's survivors' coordinates
   __shared__ int alive[kPeakThreads];
   __shared__ int alive_list[kPeakThreads];  // the chunk's survivors, in order
-  __shared__ int warp_alive[kPeakThreads / 32];
+  __shared__ int warp_alive[2][kPeakThreads / 32];  // by chunk parity: no barrier before reuse
+  __shared__ int warp_taken[kPeakThreads / 32];
   __shared__ int n_taken;
   const bool hashed = slots > 0;  // uniform
   PeakCells cells;
@@ -196,77 +197,57 @@ __global__ void __launch_bounds__(kPeakThreads, 1) peaks_kernel(const float* __r
   cells.mask = (unsigned)slots - 1u;
   cells.inv_cell = 1.0f / (separation * (1.0f + 1.0f / 65536.0f));
   float* taken_xyz = reinterpret_cast<float*>(cells.next + (hashed ? peaks : 0));  // [peaks][dimension]
-  // hashed: the chunk's survivors filed by cell (kChunkSlots keys and heads, next per survivor)
-  PeakCells chunk_cells;
-  chunk_cells.keys = reinterpret_cast<unsigned long long*>(
-      (reinterpret_cast<uintptr_t>(taken_xyz + (size_t)peaks * dimension) + 7) & ~(uintptr_t)7);
-  chunk_cells.heads = reinterpret_cast<int*>(chunk_cells.keys + kChunkSlots);
-  chunk_cells.next = chunk_cells.heads + kChunkSlots;
-  chunk_cells.mask = kChunkSlots - 1u;
-  chunk_cells.inv_cell = cells.inv_cell;
-  int* state = alive;  // hashed: per survivor, 0 open, 1 taken, 2 suppressed
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float sep2 = separation * separation;
-  for (int i = tid; i < slots; i += kPeakThreads) {
-    cells.keys[i] = kEmptyCell;
-    cells.heads[i] = -1;
-  }
-  if (tid == 0) n_taken = 0;
-  __syncthreads();
-  for (int base = 0; base < count; base += kPeakThreads) {
-    if (n_taken >= peaks) break;  // uniform: shared, stable between barriers
-    const int pos = base + tid;
-    int index = -1;
-    float c[8];
-    bool ok = false;
-    if (pos < count) {
-      index = order[pos];
-      ok = isfinite(scores[index]);
-      for (int j = 0; j < dimension; ++j) c[j] = centers[(size_t)index * dimension + j];
+
+  if (hashed) {
+    // the chunk's survivors filed by cell (kChunkSlots keys and heads, next per survivor)
+    PeakCells chunk_cells;
+    chunk_cells.keys = reinterpret_cast<unsigned long long*>(
+        (reinterpret_cast<uintptr_t>(taken_xyz + (size_t)peaks * dimension) + 7) & ~(uintptr_t)7);
+    chunk_cells.heads = reinterpret_cast<int*>(chunk_cells.keys + kChunkSlots);
+    chunk_cells.next = chunk_cells.heads + kChunkSlots;
+    chunk_cells.mask = kChunkSlots - 1u;
+    chunk_cells.inv_cell = cells.inv_cell;
+    int* state = alive;  // per survivor: 0 open, 1 taken, 2 suppressed
+    float* sxyz = chunk_xyz;
+    for (int i = tid; i < slots; i += kPeakThreads) {
+      cells.keys[i] = kEmptyCell;
+      cells.heads[i] = -1;
     }
-    const int taken_now = n_taken;
-    if (hashed) {
-      if (ok && taken_now > 0) ok = !near_taken(cells, c, dimension, taken_xyz, sep2);
-    } else {
-      // Latest peaks first: a suppressed candidate mostly lies near a recent, slightly
-      // better one, so its scan ends early (the outcome does not depend on the order).
-      for (int t = taken_now - 1; ok && t >= 0; --t) {
-        float d2 = 0.0f;
-        for (int j = 0; j < dimension; ++j) {
-          const float d = c[j] - taken_xyz[t * dimension + j];
-          d2 += d * d;
-        }
-        if (d2 < sep2) ok = false;
-      }
+    for (int i = tid; i < kChunkSlots; i += kPeakThreads) {
+      chunk_cells.keys[i] = kEmptyCell;
+      chunk_cells.heads[i] = -1;
     }
-    alive[tid] = ok ? 1 : 0;
-    const unsigned ballot = __ballot_sync(0xffffffffu, ok);
-    if (lane == 0) warp_alive[warp] = __popc(ballot);
     __syncthreads();
-    int before = __popc(ballot & ((1u << lane) - 1u)), survivors = 0;
-    for (int w = 0; w < kPeakThreads / 32; ++w) {
-      before += w < warp ? warp_alive[w] : 0;
-      survivors += warp_alive[w];
-    }
-    if (ok) alive_list[before] = tid;
-    __syncthreads();
-    if (hashed) {
-      // survivor q's coordinates at q, its cell filed in the chunk hash; every survivor open
-      float* sxyz = chunk_xyz;
-      float mine[3] = {0.f, 0.f, 0.f};
-      if (ok)
-        for (int j = 0; j < dimension; ++j) mine[j] = c[j];
-      for (int i = tid; i < kChunkSlots; i += kPeakThreads) {
-        chunk_cells.keys[i] = kEmptyCell;
-        chunk_cells.heads[i] = -1;
+    int taken = 0;  // the same value in every thread
+    for (int base = 0, chunk = 0; base < count && taken < peaks; base += kPeakThreads, ++chunk) {
+      const int pos = base + tid;
+      float c[3] = {0.f, 0.f, 0.f};
+      bool ok = false;
+      if (pos < count) {
+        const int index = order[pos];
+        ok = isfinite(scores[index]);
+        for (int j = 0; j < dimension; ++j) c[j] = centers[(size_t)index * dimension + j];
       }
+      if (ok && taken > 0) ok = !near_taken(cells, c, dimension, taken_xyz, sep2);
+      int* wa = warp_alive[chunk & 1];
+      const unsigned ballot = __ballot_sync(0xffffffffu, ok);
+      if (lane == 0) wa[warp] = __popc(ballot);
       __syncthreads();
-      if (ok) {
-        for (int j = 0; j < dimension; ++j) sxyz[before * 3 + j] = mine[j];
+      int before = __popc(ballot & ((1u << lane) - 1u)), survivors = 0;
+      for (int w = 0; w < kPeakThreads / 32; ++w) {
+        before += w < warp ? wa[w] : 0;
+        survivors += wa[w];
+      }
+      if (survivors == 0) continue;  // uniform: a chunk the taken peaks suppress entirely
+      if (ok) {  // survivor `before`: its position, coordinates and state
+        alive_list[before] = tid;
+        for (int j = 0; j < 3; ++j) sxyz[before * 3 + j] = c[j];
         state[before] = 0;
       }
       __syncthreads();
-      if (ok) file_peak_shared(chunk_cells, mine, dimension, before);
+      if (ok) file_peak_shared(chunk_cells, c, dimension, before);
       __syncthreads();
       // rounds: each settles at least the earliest open survivor, so survivors + 1 bound them
       for (int round = 0; round <= survivors; ++round) {
@@ -281,26 +262,66 @@ __global__ void __launch_bounds__(kPeakThreads, 1) peaks_kernel(const float* __r
       // the taken survivors in order, up to the peaks still wanted
       const bool took = tid < survivors && state[tid] == 1;
       const unsigned tb = __ballot_sync(0xffffffffu, took);
-      __syncthreads();  // every state read is done before warp_alive is rewritten
-      if (lane == 0) warp_alive[warp] = __popc(tb);
+      if (lane == 0) warp_taken[warp] = __popc(tb);
       __syncthreads();
       int rank = __popc(tb & ((1u << lane) - 1u)), total = 0;
       for (int w = 0; w < kPeakThreads / 32; ++w) {
-        rank += w < warp ? warp_alive[w] : 0;
-        total += warp_alive[w];
+        rank += w < warp ? warp_taken[w] : 0;
+        total += warp_taken[w];
       }
-      const int room = peaks - taken_now;
+      const int room = peaks - taken;
       if (took && rank < room) {
-        const int slot = taken_now + rank;
+        const int slot = taken + rank;
         for (int j = 0; j < dimension; ++j) taken_xyz[slot * dimension + j] = sxyz[tid * 3 + j];
         output[slot] = order[base + alive_list[tid]];
         file_peak_shared(cells, sxyz + tid * 3, dimension, slot);
       }
-      __syncthreads();
-      if (tid == 0) n_taken = taken_now + min(total, room);
-      __syncthreads();
-      continue;
+      // the chunk hash was last read in the rounds: clear it for the next chunk
+      for (int i = tid; i < kChunkSlots; i += kPeakThreads) {
+        chunk_cells.keys[i] = kEmptyCell;
+        chunk_cells.heads[i] = -1;
+      }
+      taken += min(total, room);
+      __syncthreads();  // the new peaks are filed and the chunk hash is clear
     }
+    return;
+  }
+
+  if (tid == 0) n_taken = 0;
+  __syncthreads();
+  for (int base = 0; base < count; base += kPeakThreads) {
+    if (n_taken >= peaks) break;  // uniform: shared, stable between barriers
+    const int pos = base + tid;
+    int index = -1;
+    float c[8];
+    bool ok = false;
+    if (pos < count) {
+      index = order[pos];
+      ok = isfinite(scores[index]);
+      for (int j = 0; j < dimension; ++j) c[j] = centers[(size_t)index * dimension + j];
+    }
+    const int taken_now = n_taken;
+    // Latest peaks first: a suppressed candidate mostly lies near a recent, slightly
+    // better one, so its scan ends early (the outcome does not depend on the order).
+    for (int t = taken_now - 1; ok && t >= 0; --t) {
+      float d2 = 0.0f;
+      for (int j = 0; j < dimension; ++j) {
+        const float d = c[j] - taken_xyz[t * dimension + j];
+        d2 += d * d;
+      }
+      if (d2 < sep2) ok = false;
+    }
+    alive[tid] = ok ? 1 : 0;
+    const unsigned ballot = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) warp_alive[0][warp] = __popc(ballot);
+    __syncthreads();
+    int before = __popc(ballot & ((1u << lane) - 1u)), survivors = 0;
+    for (int w = 0; w < kPeakThreads / 32; ++w) {
+      before += w < warp ? warp_alive[0][w] : 0;
+      survivors += warp_alive[0][w];
+    }
+    if (ok) alive_list[before] = tid;
+    __syncthreads();
     const int limit = min(kPeakThreads, count - base);
     for (int q = 0; q < survivors; ++q) {
       const int k = alive_list[q];
