@@ -495,6 +495,8 @@ TENSOR_KERNELS = ("dsg_gram_bf16x3", "dsg_design_project_bf16x3")
 TRAFFIC_PER_FLOP = {
     # profiles/design_project_bf16x3_2048ap_1000s.md: 327.3 MB of DRAM traffic for 48.2 GFLOP
     "dsg_design_project_bf16x3": 327.3e6 / 48.2e9,
+    # profiles/gram_bf16x3_200k_rows_1000.md: 889.7 MB of DRAM traffic for 200.2 GFLOP
+    "dsg_gram_bf16x3": 889.7e6 / 200.2e9,
 }
 
 
