@@ -19,7 +19,7 @@ from dataclasses import replace
 
 import torch
 
-from .graphs import recording, side_stream
+from .graphs import GraphCache, recording, side_stream
 from .kernels import search
 from .tracing import stage
 
@@ -65,7 +65,7 @@ def _iteration(model, residual, controls, masks, specs, config, mode, fractions,
     return iterate
 
 
-_ASCENTS: dict = {}
+_ASCENTS = GraphCache()
 
 
 def _cached_ascent(model, residual, controls, masks, specs, config, mode, fractions, eye, params, value, grad,

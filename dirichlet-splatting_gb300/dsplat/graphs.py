@@ -11,6 +11,7 @@ pool per graph) without the flush.
 
 from __future__ import annotations
 
+from collections import OrderedDict
 from contextlib import contextmanager
 
 import torch
@@ -47,3 +48,33 @@ def recording(graph):
         finally:
             graph.capture_end()
     current.wait_stream(side)
+
+
+class GraphCache:
+    """Captured graphs (with their static buffers) by shape key, the most recently used kept.
+
+    Every captured graph holds a private memory pool; a process that fits many differently
+    shaped problems (many scenes) would otherwise keep one pool per shape forever.
+    """
+
+    def __init__(self, limit=16):
+        self.limit = limit
+        self.entries = OrderedDict()
+
+    def get(self, key):
+        entry = self.entries.get(key)
+        if entry is not None:
+            self.entries.move_to_end(key)
+        return entry
+
+    def __setitem__(self, key, entry):
+        self.entries[key] = entry
+        self.entries.move_to_end(key)
+        while len(self.entries) > self.limit:
+            self.entries.popitem(last=False)
+
+    def __len__(self):
+        return len(self.entries)
+
+    def clear(self):
+        self.entries.clear()

@@ -18,7 +18,7 @@ from __future__ import annotations
 import torch
 
 from .linalg import pcg, solve
-from .graphs import side_stream
+from .graphs import GraphCache, side_stream
 from .tracing import stage
 from .varpro import accept, fit_coefficients, screen_bar
 
@@ -278,7 +278,7 @@ class _StaticJoint:
         return self.layout.pack_gradient(grads, coefficient) / self.normalization + self.shift * vector
 
 
-_JOINT_GRAPHS: dict = {}
+_JOINT_GRAPHS = GraphCache()
 
 
 def _graphed_joint_pcg(model, params, specs, config, pieces, rhs, diagonal):
