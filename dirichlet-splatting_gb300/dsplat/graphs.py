@@ -20,18 +20,20 @@ import torch
 _SIDE_STREAMS: dict = {}
 
 
-def side_stream(device=None):
-    """This device's one second stream for work beside the current stream.
+def side_stream(device=None, lane=0):
+    """One of this device's fixed second streams for work beside the current stream.
 
-    One stream per device, not a new one per use: PyTorch's caching allocator keeps the
-    blocks freed by a stream for that stream, so work that allocates gigabytes (Gram row
-    stores) on ever new streams would take new device memory every time.
+    A fixed stream per (device, lane), not a new one per use: PyTorch's caching allocator
+    keeps the blocks freed by a stream for that stream, so work that allocates gigabytes
+    (Gram row stores) on ever new streams would take new device memory every time. Lane 0
+    carries the large speculative work (full normal equations, screening refits); lane 1 the
+    short speculative factorizations, so that they never queue behind lane 0.
     """
     device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
-    stream = _SIDE_STREAMS.get(device.index)
+    stream = _SIDE_STREAMS.get((device.index, lane))
     if stream is None:
         stream = torch.cuda.Stream(device)
-        _SIDE_STREAMS[device.index] = stream
+        _SIDE_STREAMS[(device.index, lane)] = stream
     return stream
 
 

@@ -130,14 +130,29 @@ def factored_solver(h, refined=False):
     Cholesky, the shifted refined solve, or the shifted float64 factor); later calls reuse
     it, so a refinement loop costs one factorization.
     """
-    factor, status = torch.linalg.cholesky_ex(h)
-    if int(status) == 0:
-        return lambda rhs: _apply_factor(factor, rhs)
     floor = len(h) * torch.finfo(h.real.dtype).eps
+    speculative = None
     if refined and h.is_cuda:
-        shifted = _wide(h)
-        shifted.diagonal().add_(floor * largest_eigenvalue(shifted))
-        solver = RefinedSolver(shifted)  # factored once for every right-hand side
+        # The shifted system's factor is needed exactly when h has no Cholesky factor, which
+        # only the factorization below tells; both are latency bound, so the shifted one is
+        # enqueued on the side stream first and runs beside it (wasted when h factors).
+        current = torch.cuda.current_stream()
+        side = side_stream(current.device, lane=1)
+        side.wait_stream(current)
+        with torch.cuda.stream(side):
+            shifted = _wide(h)
+            shifted.diagonal().add_(floor * largest_eigenvalue(shifted))
+            speculative = RefinedSolver(shifted)
+    factor, status = torch.linalg.cholesky_ex(h)
+    failed = int(status) != 0
+    if speculative is not None:
+        current.wait_stream(side)
+        for tensor in (speculative.h, speculative.inverse_factor, speculative.status, speculative.norm):
+            tensor.record_stream(current)  # made on the side stream, used and freed on this one
+    if not failed:
+        return lambda rhs: _apply_factor(factor, rhs)
+    if speculative is not None:
+        solver = speculative  # factored once for every right-hand side
 
         def refined_call(rhs):
             q = rhs if rhs.ndim == 2 else rhs[:, None]
