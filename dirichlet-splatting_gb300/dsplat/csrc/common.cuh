@@ -204,8 +204,9 @@ __device__ __forceinline__ void pair_setup(const Consts& c, float px, float py, 
     lobe_f += 1.0f;
     off += 1.0f;
   }
-  int lobe = (int)lobe_f % c.N;
-  if (lobe < 0) lobe += c.N;
+  // N = 2 K is a power of two for every supported chirp (K in {32, 64, 128, 256}): the
+  // residue in [0, N) is a mask, not an integer division
+  const int lobe = (int)lobe_f & (c.N - 1);
   q.lobe = lobe;
   // A zero offset would make nu = 0 meet cot = inf; 1e-20 bins is far below float
   // resolution of the result and keeps every intermediate normal.

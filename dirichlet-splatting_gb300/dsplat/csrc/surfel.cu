@@ -982,8 +982,13 @@ __global__ void __launch_bounds__(kOrientWarps * 32, 4) orientations_kernel(
                                 0.5f * t + 2.0f * t2 - 1.5f * t3, -0.5f * t2 + 0.5f * t3};
           float2 v = make_float2(0.f, 0.f);
           float nn = 0.0f;
-          int first = (base - 1) % size;  // the taps base - 1 .. base + 2, wrapped
-          if (first < 0) first += size;
+          int first;  // the taps base - 1 .. base + 2, wrapped
+          if ((size & (size - 1)) == 0) {
+            first = (base - 1) & (size - 1);  // a power-of-two table (the usual oversample)
+          } else {
+            first = (base - 1) % size;
+            if (first < 0) first += size;
+          }
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int k = first + i < size ? first + i : first + i - size;

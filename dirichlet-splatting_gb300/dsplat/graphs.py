@@ -56,10 +56,13 @@ class GraphCache:
     """Captured graphs (with their static buffers) by shape key, the most recently used kept.
 
     Every captured graph holds a private memory pool; a process that fits many differently
-    shaped problems (many scenes) would otherwise keep one pool per shape forever.
+    shaped problems would otherwise keep one pool per shape forever. The bound is above the
+    shapes one batch of scenes cycles through (the many-scene workload steps 64 scenes of
+    different surfel counts in rounds, each with its own conjugate-gradient graph), so a
+    round replays every scene's graphs instead of capturing them again.
     """
 
-    def __init__(self, limit=16):
+    def __init__(self, limit=128):
         self.limit = limit
         self.entries = OrderedDict()
 
