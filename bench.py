@@ -832,6 +832,31 @@ def run_kernels(args):
                  "achieved_tflops": round(achieved, 2), "tensor_peak_tflops": round(tensor_peak, 1),
                  "frac_tensor": round(achieved / tensor_peak, 4),
                  "peak_source": f"{source} bf16_tflops (burst) / 3"})  # fmt: skip
+    # backward elimination at the pooled size of the fit (2000 support + 256 candidates, 256
+    # removals, factor form, one launch per removal)
+    pooled = S + 256
+    x = torch.randn(pooled + 344, pooled, generator=generator, dtype=torch.float64).to(device)
+    xq = x.mT @ torch.randn(pooled + 344, generator=generator, dtype=torch.float64).to(device)
+    xfac = search.triangular_inverse(torch.linalg.cholesky(x.mT @ x))
+    ms = _event_time(lambda: search.backward_elimination_factor(xfac, xq, 256), it, wu, flush)
+    rows.append({"kernel": f"dsg_backward_elimination_factor ({pooled} unknowns, 256 removals)", "ms": round(ms, 3)})
+    # the spectral model on its 256^2 grid with 80 atoms: per-bin kernel (every atom at every
+    # bin) against the separable form (per-axis tables and complex products)
+    from dsplat import SpectralGrid
+    from dsplat.kernels import spectral as spec
+
+    sgrid = SpectralGrid((256, 256))
+    sbins = sgrid.bins(device)
+    scent = (torch.rand(80, 2, generator=generator) * 256).to(device)
+    scoef = torch.complex(torch.randn(80, generator=generator), torch.randn(80, generator=generator)).to(device)
+    sup = torch.complex(torch.randn(sgrid.size, generator=generator),
+                        torch.randn(sgrid.size, generator=generator)).to(device)  # fmt: skip
+    for label, fn in (("render, per-bin kernel", lambda: spec.render(sgrid, scent, scoef, sbins)),
+                      ("render, separable", lambda: spec.render_grid(sgrid, scent, scoef)),
+                      ("vjp, per-bin kernel", lambda: spec.vjp(sgrid, scent, scoef, sup, sbins)),
+                      ("vjp, separable", lambda: spec.vjp_grid(sgrid, scent, scoef, sup))):  # fmt: skip
+        ms = _event_time(fn, it, wu, flush)
+        rows.append({"kernel": f"spectral {label} (256^2 bins, 80 atoms)", "ms": round(ms, 4)})
     print(json.dumps({"case": args.case, "apertures": A, "surfels": S, "bins": K, "kernels": rows}), flush=True)
 
 
