@@ -663,6 +663,19 @@ def _event_time(fn, iterations, warmup, flush):
     return total / iterations
 
 
+def _time_elimination(rows, support, generator, device, iterations, warmup, flush):
+    """Backward elimination at the pooled size of the fit (support + 256 candidates, 256
+    removals, factor form, one launch per removal), appended to rows."""
+    from dsplat.kernels import search
+
+    pooled = support + 256
+    x = torch.randn(pooled + 344, pooled, generator=generator, dtype=torch.float64).to(device)
+    xq = x.mT @ torch.randn(pooled + 344, generator=generator, dtype=torch.float64).to(device)
+    xfac = search.triangular_inverse(torch.linalg.cholesky(x.mT @ x))
+    ms = _event_time(lambda: search.backward_elimination_factor(xfac, xq, 256), iterations, warmup, flush)
+    rows.append({"kernel": f"dsg_backward_elimination_factor ({pooled} unknowns, 256 removals)", "ms": round(ms, 3)})
+
+
 def run_kernels(args):
     """Per-kernel roofline table on the sphere-cap geometry (the workload of the DSFW bench).
 
@@ -708,6 +721,10 @@ def run_kernels(args):
                      "frac_fp32": round(achieved / fp32_peak, 4)})  # fmt: skip
 
     it, wu = args.steps, args.warmup
+    if args.only == "elimination":  # the pooled backward elimination alone (its ncu capture)
+        _time_elimination(rows, S, generator, device, it, wu, flush)
+        print(json.dumps({"case": args.case, "kernels": rows}), flush=True)
+        return
     if args.only == "orient":  # the spatial search's normal-bank selection alone (its ncu capture)
         bank = fibonacci_sphere(24, device)
         ncand = 200000 if args.case == "full" else 50000
@@ -832,14 +849,7 @@ def run_kernels(args):
                  "achieved_tflops": round(achieved, 2), "tensor_peak_tflops": round(tensor_peak, 1),
                  "frac_tensor": round(achieved / tensor_peak, 4),
                  "peak_source": f"{source} bf16_tflops (burst) / 3"})  # fmt: skip
-    # backward elimination at the pooled size of the fit (2000 support + 256 candidates, 256
-    # removals, factor form, one launch per removal)
-    pooled = S + 256
-    x = torch.randn(pooled + 344, pooled, generator=generator, dtype=torch.float64).to(device)
-    xq = x.mT @ torch.randn(pooled + 344, generator=generator, dtype=torch.float64).to(device)
-    xfac = search.triangular_inverse(torch.linalg.cholesky(x.mT @ x))
-    ms = _event_time(lambda: search.backward_elimination_factor(xfac, xq, 256), it, wu, flush)
-    rows.append({"kernel": f"dsg_backward_elimination_factor ({pooled} unknowns, 256 removals)", "ms": round(ms, 3)})
+    _time_elimination(rows, S, generator, device, it, wu, flush)
     # the spectral model on its 256^2 grid with 80 atoms: per-bin kernel (every atom at every
     # bin) against the separable form (per-axis tables and complex products)
     from dsplat import SpectralGrid
@@ -873,7 +883,7 @@ def main():
     parser.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison run")
     parser.add_argument("--kernels", action="store_true", help="per-kernel roofline table instead")
     parser.add_argument("--case", choices=["small", "medium", "full"], default="full")
-    parser.add_argument("--only", choices=["all", "splat", "orient"], default="all",
+    parser.add_argument("--only", choices=["all", "splat", "orient", "elimination"], default="all",
                         help="with --kernels: which kernels")  # fmt: skip
     parser.add_argument("--accuracy", type=int, default=0, help="final-accuracy study of both arms on N seeds")
     parser.add_argument("--no-autotune", action="store_true", help="keep every launch shape automatic")

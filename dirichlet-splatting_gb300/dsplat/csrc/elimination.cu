@@ -5,14 +5,17 @@
 // continues with W - w w^H / W_jj, w the current column j, kept as rank-one factors
 // U[t] = w_t / sqrt(pivot_t) so a step costs O(n * step).
 //
-// One kernel per step on the caller's stream, in float64 (real or complex), after an
-// initial pick of the first unknown:
-//   step_kernel (n / 32 CTAs) the column w_i = W_ij - sum_t U[t][i] conj(U[t][j]) with the
-//   sum split over 16 warps, then b, U[step] and the diagonal, and each CTA's masked argmin
-//   of the next costs; the last CTA to finish (an atomic count, no waiting) reduces those,
-//   computes the next pivot W_jj - sum_t |U[t][j]|^2 and writes the next pick.
-// The argmin takes the first minimum and counts NaN as minimal, as torch.argmin. The
-// arithmetic is that of the reference's loop; only the order of the float64 sums differs.
+// One kernel per removal on the caller's stream, in float64 (real or complex), after the
+// initial pass and pick. Per row block of 32 unknowns the column
+// w_i = W_ij - sum_t U[t][i] conj(U[t][j]) (in the factor form W_ij itself is a sum over X's
+// rows k >= max(i, j)), then b, U[step], the diagonal and the block's masked argmin; the last
+// CTA to finish (an atomic count, no waiting) reduces the blocks' candidates and writes the
+// next pivot W_jj - sum_t |U[t][j]|^2. FP64 issues at a few lanes per clock on this part and
+// a removal is set by its busiest SM, so the work is spread evenly: row blocks are paired (a
+// long k range with a short one), each pair's sums are split over 8 CTAs, and the argmin
+// compares integer keys instead of doubles. The argmin takes the first minimum and counts
+// NaN as minimal, as torch.argmin. The arithmetic is that of the reference's loop; only the
+// order of the float64 sums differs.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -62,7 +65,7 @@ __device__ __forceinline__ double zero<double>() { return 0.0; }
 template <>
 __device__ __forceinline__ Cplx zero<Cplx>() { return Cplx{0.0, 0.0}; }
 
-// Shared state between the two kernels of a step.
+// State between two launches: the removal being applied.
 struct Pick {
   long long index;  // the unknown removed this step
   double pivot;     // clamp(real(w_j), tiny)
@@ -70,31 +73,123 @@ struct Pick {
   double pad;
 };
 
+// A row block's argmin candidate. key orders the costs as torch.argmin does (NaN first,
+// then by value) with integer compares: the costs are never negative, so their bit
+// patterns order as their values. index is the row, kNone for none.
 struct Candidate {
-  double cost;  // NaN allowed
-  int index;    // 0x7fffffff: none
+  unsigned long long key;
+  int index;
   int pad;
 };
 
 constexpr int kNone = 0x7fffffff;
+constexpr unsigned long long kInfKey = 0x7ff0000000000001ull;  // cost_key(+inf)
+constexpr double kTiny = 2.2250738585072014e-308;              // smallest normal double (torch.finfo.tiny)
 
-// Whether (cost b, index ib) precedes (cost a, index ia) in torch.argmin order.
-__device__ __forceinline__ bool precedes(double b, int ib, double a, int ia) {
-  if (ib == kNone) return false;
-  if (ia == kNone) return true;
-  const bool nb = b != b, na = a != a;
-  if (nb != na) return nb;
-  if (nb) return ib < ia;
-  return b < a || (b == a && ib < ia);
+__device__ __forceinline__ unsigned long long cost_key(double c) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(c);
+  return (bits & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : bits + 1ull;
 }
 
-constexpr int kPickThreads = 1024;
-constexpr int kRows = 32;  // rows per update CTA
-constexpr int kSplit = 16;  // warps sharing one row's sums (over the factor's rows and the earlier steps)
-// CTAs sharing one row block's factor-column sum (factor form): row block b sums over
-// k >= max(j, 32 b), so the first blocks carry most of the triangle; splitting every
-// block's k range into kParts shares bounds the longest CTA at a quarter of it.
-constexpr int kParts = 4;
+// Whether (key kb, index ib) precedes (key ka, index ia): the first minimum wins.
+__device__ __forceinline__ bool precedes(unsigned long long kb, int ib, unsigned long long ka, int ia) {
+  if (ib == kNone) return false;
+  if (ia == kNone) return true;
+  return kb < ka || (kb == ka && ib < ia);
+}
+
+__device__ __forceinline__ void warp_argmin(unsigned long long& key, int& index) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, index, o);
+    if (precedes(ok, oi, key, index)) {
+      key = ok;
+      index = oi;
+    }
+  }
+}
+
+constexpr int kRows = 32;                 // rows per row block (one per lane)
+constexpr int kSplit = 16;                // warps per CTA, sharing each row's sums
+constexpr int kThreads = kRows * kSplit;  // 512
+constexpr int kPickThreads = 512;
+// FP64 issues at a few lanes per clock on this part, so a removal is set by the FP64 work of
+// its busiest SM. The factor form's column sum for a row in block r runs over
+// k >= max(j, 32 r): early blocks carry most of the triangle. Blocks are paired, r with its
+// mirror B - 1 - r, whose k ranges together are about n long, and each pair is split into
+// kPairParts CTAs of equal k work; the sum over the earlier removals is split the same way.
+constexpr int kPairParts = 8;
+
+// Share y of `parts` of the row-block pair p: blocks a = p and b = blocks - 1 - p (b < 0 when
+// they coincide), whose k ranges [ka0, n) and [kb0, n) (k0 = max(first_k, 32 block)) are laid
+// end to end and cut into equal shares; this share is k = ka0 + [sa0, sa1) of block a and
+// k = kb0 + [sb0, sb1) of block b.
+struct PairShare {
+  int a, b, ka0, kb0, sa0, sa1, sb0, sb1;
+};
+
+__device__ __forceinline__ PairShare pair_share(int n, int blocks, int p, int y, int parts, int first_k) {
+  PairShare s;
+  s.a = p;
+  s.b = blocks - 1 - p;
+  if (s.b == s.a) s.b = -1;
+  s.ka0 = max(first_k, s.a * kRows);
+  s.kb0 = s.b >= 0 ? max(first_k, s.b * kRows) : n;
+  const int la = n - s.ka0, total = la + (n - s.kb0);
+  const int share = (total + parts - 1) / parts;
+  const int s0 = min(total, y * share), s1 = min(total, s0 + share);
+  s.sa0 = min(s0, la);
+  s.sa1 = min(s1, la);
+  s.sb0 = max(s0, la) - la;
+  s.sb1 = max(s1, la) - la;
+  return s;
+}
+
+__device__ __forceinline__ double to_real(double v) { return v; }
+__device__ __forceinline__ double to_real(Cplx v) { return v.x; }
+template <typename T>
+__device__ __forceinline__ T from_real(double v);
+template <>
+__device__ __forceinline__ double from_real<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ Cplx from_real<Cplx>(double v) { return Cplx{v, 0.0}; }
+
+// Adds the 4 per-warp quantities in s_sum over the warps (warps 0-3, one quantity each, on
+// separate SM sub-partitions); with parts > 1 the shares go to the pair's slots and the CTA
+// that completes the pair adds them in share order. Returns whether this CTA holds the totals
+// in s_tot.
+template <typename T>
+__device__ __forceinline__ bool combine_pair(T (*s_sum)[kSplit][kRows], T (*s_tot)[kRows], int p, int y, int parts,
+                                             T* pair_parts, unsigned* pair_counter) {
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (warp < 4) {
+    T total = s_sum[warp][0][lane];
+    for (int w = 1; w < kSplit; ++w) total = add(total, s_sum[warp][w][lane]);
+    if (parts > 1) {
+      pair_parts[(((size_t)p * parts + y) * 4 + warp) * kRows + lane] = total;
+      __threadfence();  // the share reaches L2 before the CTA is counted
+    } else {
+      s_tot[warp][lane] = total;
+    }
+  }
+  if (parts > 1) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&pair_counter[p], 1u) == (unsigned)parts - 1;
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    if (threadIdx.x == 0) atomicExch(&pair_counter[p], 0u);
+    if (warp < 4) {
+      T total = zero<T>();
+      for (int z = 0; z < parts; ++z) total = add(total, load_cg(&pair_parts[(((size_t)p * parts + z) * 4 + warp) * kRows + lane]));
+      s_tot[warp][lane] = total;
+    }
+  }
+  __syncthreads();
+  return true;
+}
 
 // b = W q, diag = real(W_ii), alive = 1, spent = 0.
 template <typename T>
@@ -132,297 +227,261 @@ __global__ void factor_rows_kernel(const T* __restrict__ X, const T* __restrict_
   if (lane == 0) y[i] = acc;
 }
 
+// b_i = sum_{k >= i} conj(X_ki) y_k and diag_i = sum_{k >= i} |X_ki|^2 over the pair partition
+// (one CTA per pair share; the pair's last CTA writes b, diag, wdiag and alive).
 template <typename T>
-__global__ void factor_init_kernel(const T* __restrict__ X, const T* __restrict__ y, int n, T* __restrict__ b,
-                                   double* __restrict__ diag, double* __restrict__ wdiag,
-                                   uint8_t* __restrict__ alive, Pick* __restrict__ pick,
-                                   unsigned* __restrict__ counter) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    T acc = zero<T>();  // sum_k conj(X_ki) y_k = conj(sum_k X_ki conj(y_k))
-    double d = 0.0;
-    for (int k = i; k < n; ++k) {
-      const T x = X[(size_t)k * n + i];
-      acc = add(acc, mul_conj(x, y[k]));
-      d += abs2(x);
+__global__ void __launch_bounds__(kThreads) factor_init_kernel(const T* __restrict__ X, const T* __restrict__ y, int n,
+                                                               int blocks, int parts, T* b, double* diag, double* wdiag,
+                                                               uint8_t* alive, T* pair_parts, unsigned* pair_counter,
+                                                               Pick* pick, unsigned* counter) {
+  extern __shared__ __align__(16) uint8_t s_dyn[];
+  __shared__ T s_sum[4][kSplit][kRows];  // per warp: X^H y and |X|^2 of block a, then of block b
+  __shared__ T s_tot[4][kRows];
+  T* s_y = reinterpret_cast<T*>(s_dyn);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p = blockIdx.x / parts, yy = blockIdx.x % parts;
+  const PairShare s = pair_share(n, blocks, p, yy, parts, 0);
+  const int na = s.sa1 - s.sa0, nb = s.sb1 - s.sb0;
+  for (int m = threadIdx.x; m < na + nb; m += blockDim.x)
+    s_y[m] = y[m < na ? s.ka0 + s.sa0 + m : s.kb0 + s.sb0 + (m - na)];
+  __syncthreads();
+  const int ia = s.a * kRows + lane, ib = s.b >= 0 ? s.b * kRows + lane : n;
+  T sa = zero<T>(), sb = zero<T>();
+  double da = 0.0, db = 0.0;
+  if (ia < n)
+    for (int m = warp; m < na; m += kSplit) {
+      const T x = X[(size_t)(s.ka0 + s.sa0 + m) * n + ia];
+      sa = add(sa, mul_conj(x, s_y[m]));
+      da += abs2(x);
     }
-    b[i] = conj_of(acc);
-    diag[i] = wdiag[i] = d;
-    alive[i] = 1;
-  }
+  if (ib < n)
+    for (int m = warp; m < nb; m += kSplit) {
+      const T x = X[(size_t)(s.kb0 + s.sb0 + m) * n + ib];
+      sb = add(sb, mul_conj(x, s_y[na + m]));
+      db += abs2(x);
+    }
+  s_sum[0][warp][lane] = sa;
+  s_sum[1][warp][lane] = from_real<T>(da);
+  s_sum[2][warp][lane] = sb;
+  s_sum[3][warp][lane] = from_real<T>(db);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     pick->spent = 0;
     *counter = 0;
   }
+  if (!combine_pair<T>(s_sum, s_tot, p, yy, parts, pair_parts, pair_counter)) return;
+  if (warp < 2) {
+    const int blk = warp == 0 ? s.a : s.b;
+    const int i = blk * kRows + lane;
+    if (blk >= 0 && i < n) {
+      b[i] = conj_of(s_tot[2 * warp][lane]);  // sum conj(X_ki) y_k = conj(sum X_ki conj(y_k))
+      diag[i] = wdiag[i] = to_real(s_tot[2 * warp + 1][lane]);
+      alive[i] = 1;
+    }
+  }
 }
 
+// The first removal: argmin of |b_i|^2 / W_ii over all unknowns (none removed or marked
+// yet), its pivot W_jj and marked count (one CTA).
 template <typename T>
-__global__ void __launch_bounds__(kPickThreads) pick_kernel(
-    const T* __restrict__ W, int n, int step, const T* __restrict__ b, const double* __restrict__ diag,
-    const uint8_t* __restrict__ alive, const uint8_t* __restrict__ limited, long long limit,
-    const T* __restrict__ U, const double* __restrict__ wdiag, Pick* __restrict__ pick,
-    int64_t* __restrict__ removed) {
-  __shared__ double s_cost[kPickThreads / 32];
-  __shared__ int s_index[kPickThreads / 32];
-  __shared__ double s_sum[kPickThreads / 32];
-  __shared__ int s_choice;
-  const double tiny = 2.2250738585072014e-308;  // smallest normal double (torch.finfo.tiny)
+__global__ void __launch_bounds__(kPickThreads) pick_kernel(int n, const T* __restrict__ b,
+                                                            const double* __restrict__ diag,
+                                                            const uint8_t* __restrict__ alive,
+                                                            const uint8_t* __restrict__ limited, long long limit,
+                                                            const double* __restrict__ wdiag, Pick* __restrict__ pick,
+                                                            int64_t* __restrict__ removed) {
+  __shared__ Candidate s_best[kPickThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool spent_out = limited != nullptr && pick->spent >= limit;
-  // cost and the first minimal index (NaN first, then the smallest cost, then the lowest index)
-  double best = INFINITY;
-  int best_i = 0x7fffffff;
-  bool best_nan = false;
+  unsigned long long key = ~0ull;
+  int index = kNone;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const bool blocked = !alive[i] || (spent_out && limited[i]);
-    double cost = blocked ? INFINITY : abs2(b[i]) / fmax(diag[i], tiny);
-    const bool nan = cost != cost;
-    if (best_i == 0x7fffffff || (nan && !best_nan) || (nan == best_nan && !nan && cost < best)) {
-      best = cost;
-      best_i = i;
-      best_nan = nan;
+    const unsigned long long k = blocked ? kInfKey : cost_key(abs2(b[i]) / fmax(diag[i], kTiny));
+    if (precedes(k, i, key, index)) {
+      key = k;
+      index = i;
     }
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) {
-    const double oc = __shfl_xor_sync(0xffffffffu, best, o);
-    const int oi = __shfl_xor_sync(0xffffffffu, best_i, o);
-    const bool on = __shfl_xor_sync(0xffffffffu, (int)best_nan, o) != 0;
-    const bool take = oi != 0x7fffffff &&
-                      (best_i == 0x7fffffff || (on && !best_nan) ||
-                       (on == best_nan && (on ? oi < best_i : (oc < best || (oc == best && oi < best_i)))));
-    if (take) {
-      best = oc;
-      best_i = oi;
-      best_nan = on;
+  warp_argmin(key, index);
+  if (lane == 0) s_best[warp] = Candidate{key, index, 0};
+  __syncthreads();
+  if (warp == 0) {
+    key = lane < kPickThreads / 32 ? s_best[lane].key : ~0ull;
+    index = lane < kPickThreads / 32 ? s_best[lane].index : kNone;
+    warp_argmin(key, index);
+    if (index == kNone || key == kInfKey) index = 0;  // every cost infinite: torch.argmin gives 0
+    if (lane == 0) {
+      pick->index = index;
+      pick->pivot = fmax(wdiag[index], kTiny);
+      if (limited != nullptr && limited[index]) pick->spent += 1;
+      removed[0] = index;
     }
-  }
-  if (lane == 0) {
-    s_cost[warp] = best_nan ? NAN : best;
-    s_index[warp] = best_i;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double c = INFINITY;
-    int idx = 0x7fffffff;
-    bool cn = false;
-    for (int w = 0; w < kPickThreads / 32; ++w) {
-      const int oi = s_index[w];
-      if (oi == 0x7fffffff) continue;
-      const double oc = s_cost[w];
-      const bool on = oc != oc;
-      if (idx == 0x7fffffff || (on && !cn) || (on == cn && (on ? oi < idx : (oc < c || (oc == c && oi < idx))))) {
-        c = oc;
-        idx = oi;
-        cn = on;
-      }
-    }
-    // Every cost infinite: torch.argmin of an all-inf vector returns 0.
-    if (idx == 0x7fffffff || (!cn && c == INFINITY)) idx = 0;
-    s_choice = idx;
-  }
-  __syncthreads();
-  const int j = s_choice;
-  // pivot = real(W_jj - sum_t U[t][j] conj(U[t][j]))
-  double part = 0.0;
-  for (int t = threadIdx.x; t < step; t += blockDim.x) part += abs2(U[(size_t)t * n + j]);
-  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-  if (lane == 0) s_sum[warp] = part;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double total = 0.0;
-    for (int w = 0; w < kPickThreads / 32; ++w) total += s_sum[w];
-    const double pivot = wdiag[j] - total;
-    pick->index = j;
-    pick->pivot = fmax(pivot, tiny);
-    if (limited != nullptr && limited[j]) pick->spent += 1;
-    removed[step] = j;
   }
 }
 
-// W is the inverse itself, or with FACTOR its lower-triangular factor X (W = X^H X): the
-// column W_ij is then sum_k conj(X_ki) X_kj over k >= max(i, j), X's column j staged in
-// shared memory.
+// One removal per launch, one CTA per pair share. W is the inverse itself, or with FACTOR its
+// lower-triangular factor X (W = X^H X): the column W_ij is then sum_k conj(X_ki) X_kj over
+// k >= max(i, j), split over the pair partition with X's column j staged in shared memory.
+// The sum over the earlier removals sum_t U[t][i] conj(U[t][j]) is split over the pair's CTAs
+// by t. The CTA that completes the pair (the last of its parts) adds the shares in share
+// order and applies the rank-one update to both blocks' rows (b_out, diag, alive, U[step];
+// warp 0 block a, warp 1 block b) and their argmin candidates; the last such CTA of the grid
+// (an atomic count, no waiting) reduces the candidates and writes the next pick. Everything
+// another CTA of the same launch wrote is read from L2 (load_cg).
 template <typename T, bool FACTOR>
-__global__ void __launch_bounds__(kRows * kSplit) step_kernel(
-    const T* __restrict__ W, int n, int step, int count, const T* __restrict__ b_in, T* __restrict__ b_out,
-    double* __restrict__ diag, const double* __restrict__ wdiag, uint8_t* __restrict__ alive,
+__global__ void __launch_bounds__(kThreads) step_kernel(
+    const T* __restrict__ W, int n, int blocks, int parts, int step, int count, const T* __restrict__ b_in,
+    T* __restrict__ b_out, double* __restrict__ diag, const double* __restrict__ wdiag, uint8_t* __restrict__ alive,
     T* __restrict__ U, const uint8_t* __restrict__ limited, long long limit, const Pick* __restrict__ pick_in,
-    Pick* __restrict__ pick_out, Candidate* __restrict__ partials, unsigned* __restrict__ counter,
-    T* __restrict__ column_parts, unsigned* __restrict__ row_counter, int64_t* __restrict__ removed) {
-  extern __shared__ uint8_t s_dyn[];
-  __shared__ bool s_row_last;
-  __shared__ T s_partw[FACTOR ? kSplit : 1][kRows];
-  __shared__ T s_part[kSplit][kRows];
+    Pick* __restrict__ pick_out, Candidate* __restrict__ block_best, unsigned* __restrict__ counter,
+    T* __restrict__ pair_parts, unsigned* __restrict__ pair_counter, int64_t* __restrict__ removed) {
+  extern __shared__ __align__(16) uint8_t s_dyn[];
+  __shared__ T s_sum[4][kSplit][kRows];  // per warp: the k sum and the t sum of block a, then of block b
+  __shared__ T s_tot[4][kRows];
   __shared__ T s_uj[256];
-  __shared__ double s_red[kRows * kSplit / 32];
-  __shared__ Candidate s_best[kRows * kSplit / 32];
   __shared__ bool s_last;
-  const double tiny = 2.2250738585072014e-308;  // smallest normal double (torch.finfo.tiny)
+  __shared__ Candidate s_best[kSplit];
+  T* s_xj = reinterpret_cast<T*>(s_dyn);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int j = (int)pick_in->index;
   const double pivot = pick_in->pivot;
   const long long spent = pick_in->spent;  // marked removals including j
-  const bool spent_out = limited != nullptr && spent >= limit;
-  const int i = blockIdx.x * kRows + lane;
-  T accw = zero<T>();
-  if (FACTOR) {
-    // this CTA's share [kl, kh) of the row block's k range, X's column j staged for it
-    T* s_xj = reinterpret_cast<T*>(s_dyn);
-    const int parts = (int)gridDim.y;
-    const int k0 = max(j, (int)blockIdx.x * kRows);
-    const int share = (n - k0 + parts - 1) / parts;
-    const int kl = min(n, k0 + (int)blockIdx.y * share), kh = min(n, kl + share);
-    for (int k = kl + (int)threadIdx.x; k < kh; k += blockDim.x) s_xj[k - kl] = W[(size_t)k * n + j];
-    __syncthreads();
-    if (i < n)
-      for (int k = kl + warp; k < kh; k += kSplit) accw = add(accw, mul_conj(W[(size_t)k * n + i], s_xj[k - kl]));
-    s_partw[FACTOR ? warp : 0][lane] = accw;
-    if (parts > 1) {
-      // shares go to the row block's slots; the last CTA of the block adds them in share order
-      __syncthreads();
-      if (warp == 0) {
-        T total = s_partw[0][lane];
-        for (int w = 1; w < kSplit; ++w) total = add(total, s_partw[FACTOR ? w : 0][lane]);
-        column_parts[((size_t)blockIdx.x * parts + blockIdx.y) * kRows + lane] = total;
-        __threadfence();  // the share reaches L2 before the CTA is counted
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) s_row_last = atomicAdd(&row_counter[blockIdx.x], 1u) == (unsigned)parts - 1;
-      __syncthreads();
-      if (!s_row_last) return;
-      __threadfence();
-      if (threadIdx.x == 0) row_counter[blockIdx.x] = 0;
-      if (warp == 0) {
-        T total = zero<T>();
-        for (int y = 0; y < parts; ++y) total = add(total, load_cg(&column_parts[((size_t)blockIdx.x * parts + y) * kRows + lane]));
-        s_partw[0][lane] = total;
-        for (int w = 1; w < kSplit; ++w) s_partw[FACTOR ? w : 0][lane] = zero<T>();
-      }
-    }
-  }
-  T acc = zero<T>();
-  for (int t0 = 0; t0 < step; t0 += 256) {
-    const int len = min(256, step - t0);
+  const int p = blockIdx.x / parts, y = blockIdx.x % parts;
+  const PairShare s = pair_share(n, blocks, p, y, parts, j);
+  const int na = FACTOR ? s.sa1 - s.sa0 : 0, nb = FACTOR ? s.sb1 - s.sb0 : 0;
+  const int ia = s.a * kRows + lane, ib = s.b >= 0 ? s.b * kRows + lane : n;
+  const int tshare = (step + parts - 1) / parts;
+  const int tl = min(step, y * tshare), th = min(step, tl + tshare);
+  for (int m = threadIdx.x; m < na + nb; m += blockDim.x)
+    s_xj[m] = W[(size_t)(m < na ? s.ka0 + s.sa0 + m : s.kb0 + s.sb0 + (m - na)) * n + j];
+  T ka = zero<T>(), kb = zero<T>(), ta = zero<T>(), tb = zero<T>();
+  for (int t0 = tl; t0 < th; t0 += 256) {
+    const int len = min(256, th - t0);
     __syncthreads();
     for (int t = threadIdx.x; t < len; t += blockDim.x) s_uj[t] = U[(size_t)(t0 + t) * n + j];
     __syncthreads();
-    if (i < n)
-      for (int t = warp; t < len; t += kSplit) acc = add(acc, mul_conj(U[(size_t)(t0 + t) * n + i], s_uj[t]));
-  }
-  s_part[warp][lane] = acc;
-  __syncthreads();
-  if (warp == 0) {
-    double cost = INFINITY;
-    int index = kNone;
-    if (i < n) {
-      T sum = s_part[0][lane];
-      for (int w = 1; w < kSplit; ++w) sum = add(sum, s_part[w][lane]);
-      T wij;
-      if (FACTOR) {
-        T total = s_partw[0][lane];
-        for (int w = 1; w < kSplit; ++w) total = add(total, s_partw[FACTOR ? w : 0][lane]);
-        wij = conj_of(total);
-      } else {
-        wij = W[(size_t)i * n + j];
-      }
-      const T column = step ? sub(wij, sum) : wij;
-      const T bj = b_in[j];
-      const T scaled = divide(column, sqrt(pivot));
-      // b_i - w_i (b_j / pivot); the removed unknown keeps b = 0 and diag = 1 so that its
-      // masked cost stays finite (as the reference's loop).
-      T bi = sub(b_in[i], mul(column, divide(bj, pivot)));
-      double di = diag[i] - abs2(scaled);
-      bool live = alive[i] != 0;
-      if (i == j) {
-        alive[i] = 0;
-        live = false;
-        di = 1.0;
-        bi = zero<T>();
-      }
-      U[(size_t)step * n + i] = scaled;
-      b_out[i] = bi;
-      diag[i] = di;
-      const bool blocked = !live || (spent_out && limited[i]);
-      cost = blocked ? INFINITY : abs2(bi) / fmax(di, tiny);
-      index = i;
+    for (int t = warp; t < len; t += kSplit) {
+      const T uj = s_uj[t];
+      if (ia < n) ta = add(ta, mul_conj(U[(size_t)(t0 + t) * n + ia], uj));
+      if (ib < n) tb = add(tb, mul_conj(U[(size_t)(t0 + t) * n + ib], uj));
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double oc = __shfl_xor_sync(0xffffffffu, cost, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, index, o);
-      if (precedes(oc, oi, cost, index)) {
-        cost = oc;
-        index = oi;
+  }
+  __syncthreads();  // s_xj staged
+  if (FACTOR) {
+    if (ia < n)
+      for (int m = warp; m < na; m += kSplit) ka = add(ka, mul_conj(W[(size_t)(s.ka0 + s.sa0 + m) * n + ia], s_xj[m]));
+    if (ib < n)
+      for (int m = warp; m < nb; m += kSplit)
+        kb = add(kb, mul_conj(W[(size_t)(s.kb0 + s.sb0 + m) * n + ib], s_xj[na + m]));
+  }
+  s_sum[0][warp][lane] = ka;
+  s_sum[1][warp][lane] = ta;
+  s_sum[2][warp][lane] = kb;
+  s_sum[3][warp][lane] = tb;
+  if (!combine_pair<T>(s_sum, s_tot, p, y, parts, pair_parts, pair_counter)) return;
+  if (warp < 2) {
+    const int blk = warp == 0 ? s.a : s.b;
+    if (blk >= 0) {  // warp-uniform
+      const int i = blk * kRows + lane;
+      const bool spent_out = limited != nullptr && spent >= limit;
+      unsigned long long key = ~0ull;
+      int index = kNone;
+      if (i < n) {
+        const T wij = FACTOR ? conj_of(s_tot[2 * warp][lane]) : W[(size_t)i * n + j];
+        const T column = step ? sub(wij, s_tot[2 * warp + 1][lane]) : wij;
+        const T bj = b_in[j];
+        const T scaled = divide(column, sqrt(pivot));
+        // b_i - w_i (b_j / pivot); the removed unknown keeps b = 0 and diag = 1 so that its
+        // masked cost stays finite (as the reference's loop).
+        T bi = sub(b_in[i], mul(column, divide(bj, pivot)));
+        double di = diag[i] - abs2(scaled);
+        bool live = alive[i] != 0;
+        if (i == j) {
+          alive[i] = 0;
+          live = false;
+          di = 1.0;
+          bi = zero<T>();
+        }
+        U[(size_t)step * n + i] = scaled;
+        b_out[i] = bi;
+        diag[i] = di;
+        const bool blocked = !live || (spent_out && limited[i]);
+        key = blocked ? kInfKey : cost_key(abs2(bi) / fmax(di, kTiny));
+        index = i;
       }
+      warp_argmin(key, index);
+      if (lane == 0) block_best[blk] = Candidate{key, index, 0};
+      __threadfence();  // this lane's writes reach L2 before the CTA is counted
     }
-    if (lane == 0) partials[blockIdx.x] = Candidate{cost, index, 0};
-    __threadfence();  // this lane's writes reach L2 before the CTA is counted
   }
   __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == (unsigned)(gridDim.x / parts) - 1;
   __syncthreads();
   if (!s_last) return;
-  // The last CTA: every other CTA's writes are visible (they fenced before counting).
+  // The last pair: every other CTA's writes are visible (they fenced before counting).
   __threadfence();
   if (threadIdx.x == 0) *counter = 0;
   if (step + 1 >= count) return;
-  double cost = INFINITY;
+  unsigned long long key = ~0ull;
   int index = kNone;
-  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) {
-    const double oc = __ldcg(&partials[c].cost);
-    const int oi = __ldcg(&partials[c].index);
-    if (precedes(oc, oi, cost, index)) {
-      cost = oc;
+  for (int c = threadIdx.x; c < blocks; c += blockDim.x) {
+    const unsigned long long ok = __ldcg(&block_best[c].key);
+    const int oi = __ldcg(&block_best[c].index);
+    if (precedes(ok, oi, key, index)) {
+      key = ok;
       index = oi;
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double oc = __shfl_xor_sync(0xffffffffu, cost, o);
-    const int oi = __shfl_xor_sync(0xffffffffu, index, o);
-    if (precedes(oc, oi, cost, index)) {
-      cost = oc;
-      index = oi;
+  warp_argmin(key, index);
+  if (lane == 0) s_best[warp] = Candidate{key, index, 0};
+  __syncthreads();
+  if (warp == 0) {
+    key = lane < kSplit ? s_best[lane].key : ~0ull;
+    index = lane < kSplit ? s_best[lane].index : kNone;
+    warp_argmin(key, index);
+    if (index == kNone || key == kInfKey) index = 0;  // every cost infinite: torch.argmin gives 0
+    double part = 0.0;  // sum_{t <= step} |U[t][jn]|^2
+    for (int t = lane; t <= step; t += 32) part += abs2(load_cg(&U[(size_t)t * n + index]));
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) {
+      pick_out->index = index;
+      pick_out->pivot = fmax(wdiag[index] - part, kTiny);
+      pick_out->spent = spent + (limited != nullptr && limited[index] ? 1 : 0);
+      removed[step + 1] = index;
     }
   }
-  if (lane == 0) s_best[warp] = Candidate{cost, index, 0};
-  __syncthreads();
-  __shared__ int s_next;
-  if (threadIdx.x == 0) {
-    cost = INFINITY;
-    index = kNone;
-    for (int w = 0; w < kRows * kSplit / 32; ++w)
-      if (precedes(s_best[w].cost, s_best[w].index, cost, index)) {
-        cost = s_best[w].cost;
-        index = s_best[w].index;
-      }
-    // Every cost infinite: torch.argmin of an all-inf vector returns 0.
-    if (index == kNone || (cost == INFINITY)) index = 0;
-    s_next = index;
-  }
-  __syncthreads();
-  const int jn = s_next;
-  double part = 0.0;
-  for (int t = threadIdx.x; t <= step; t += blockDim.x) {
-    const T u = t == step ? load_cg(&U[(size_t)t * n + jn]) : U[(size_t)t * n + jn];
-    part += abs2(u);
-  }
-  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-  if (lane == 0) s_red[warp] = part;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double total = 0.0;
-    for (int w = 0; w < kRows * kSplit / 32; ++w) total += s_red[w];
-    const double pv = wdiag[jn] - total;
-    pick_out->index = jn;
-    pick_out->pivot = fmax(pv, tiny);
-    pick_out->spent = spent + (limited != nullptr && limited[jn] ? 1 : 0);
-    removed[step + 1] = jn;
-  }
+}
+
+inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+inline int blocks_of(int n) { return (n + kRows - 1) / kRows; }
+inline int pairs_of(int n) { return (blocks_of(n) + 1) / 2; }
+
+template <typename K>
+int allow_smem(K kernel, size_t smem) {
+  cudaFuncAttributes attributes;
+  if (cudaFuncGetAttributes(&attributes, kernel) != cudaSuccess) return DSG_ERR_LAUNCH;
+  if (smem + attributes.sharedSizeBytes > 48 * 1024 &&  // dynamic plus static above the default
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return DSG_ERR_LAUNCH;
+  return DSG_OK;
+}
+
+// The workspace, in order: b0, b1 [n] T; diag, wdiag [n] double; U [count][n] T; the two
+// picks; the row blocks' candidates; the grid counter; alive [n]; then (16-byte aligned) the
+// pairs' counters and their share slots (4 sums of 32 rows per share).
+size_t elimination_bytes(int n, int count, bool is_complex) {
+  const size_t elem = is_complex ? 16 : 8;
+  const size_t blocks = blocks_of(n), pairs = pairs_of(n);
+  return elem * 2 * (size_t)n + 16 * (size_t)n + elem * (size_t)count * n + 2 * sizeof(Pick) +
+         blocks * sizeof(Candidate) + 16 + (size_t)n + 15 + align16(pairs * sizeof(unsigned)) +
+         pairs * kPairParts * 4 * kRows * elem;
 }
 
 template <typename T, bool FACTOR>
 int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* limited, long long limit,
         void* workspace, int64_t* removed, cudaStream_t st) {
-  const int blocks = (n + kRows - 1) / kRows;
+  const int blocks = blocks_of(n), pairs = pairs_of(n);
+  const int parts = FACTOR ? kPairParts : 1;
   uint8_t* w = reinterpret_cast<uint8_t*>(workspace);
   T* b0 = reinterpret_cast<T*>(w);
   T* b1 = b0 + n;
@@ -430,40 +489,34 @@ int run(const void* inverse, const void* rhs, int n, int count, const uint8_t* l
   double* wdiag = diag + n;
   T* U = reinterpret_cast<T*>(wdiag + n);
   Pick* picks = reinterpret_cast<Pick*>(U + (size_t)count * n);  // [2]
-  Candidate* partials = reinterpret_cast<Candidate*>(picks + 2);
-  unsigned* counter = reinterpret_cast<unsigned*>(partials + blocks);
+  Candidate* best = reinterpret_cast<Candidate*>(picks + 2);
+  unsigned* counter = reinterpret_cast<unsigned*>(best + blocks);
   uint8_t* alive = reinterpret_cast<uint8_t*>(counter + 4);
-  // after alive: the row blocks' counters and share slots (factor form), 16-byte aligned
-  const size_t tail = (reinterpret_cast<uintptr_t>(alive + n) + 15) & ~(uintptr_t)15;
-  unsigned* row_counter = reinterpret_cast<unsigned*>(tail);
-  T* column_parts = reinterpret_cast<T*>(tail + (((size_t)blocks * sizeof(unsigned) + 15) & ~(size_t)15));
-  const int parts = FACTOR ? kParts : 1;
-  if (FACTOR && cudaMemsetAsync(row_counter, 0, (size_t)blocks * sizeof(unsigned), st) != cudaSuccess)
-    return DSG_ERR_LAUNCH;
+  const uintptr_t tail = align16(reinterpret_cast<uintptr_t>(alive + n));
+  unsigned* pair_counter = reinterpret_cast<unsigned*>(tail);
+  T* pair_parts = reinterpret_cast<T*>(tail + align16((size_t)pairs * sizeof(unsigned)));
+  const size_t smem = FACTOR ? (size_t)((2 * n + parts - 1) / parts + 1) * sizeof(T) : 0;
+  if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
+  if (allow_smem(step_kernel<T, FACTOR>, smem) != DSG_OK) return DSG_ERR_LAUNCH;
+  if (cudaMemsetAsync(pair_counter, 0, (size_t)pairs * sizeof(unsigned), st) != cudaSuccess) return DSG_ERR_LAUNCH;
   const T* W = reinterpret_cast<const T*>(inverse);
   const T* q = reinterpret_cast<const T*>(rhs);
-  size_t smem = 0;
   if (FACTOR) {
-    smem = (size_t)n * sizeof(T);
-    if (smem > 200 * 1024) return DSG_ERR_UNSUPPORTED;
-    cudaFuncAttributes attributes;
-    if (cudaFuncGetAttributes(&attributes, step_kernel<T, FACTOR>) != cudaSuccess) return DSG_ERR_LAUNCH;
-    if (smem + attributes.sharedSizeBytes > 48 * 1024 &&  // dynamic plus static above the default
-        cudaFuncSetAttribute(step_kernel<T, FACTOR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-      return DSG_ERR_LAUNCH;
+    const size_t init_smem = (size_t)((2 * n + kPairParts - 1) / kPairParts + 1) * sizeof(T);
+    if (allow_smem(factor_init_kernel<T>, init_smem) != DSG_OK) return DSG_ERR_LAUNCH;
     factor_rows_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, q, n, b1);  // y = X q in b1
-    factor_init_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(W, b1, n, b0, diag, wdiag, alive, picks, counter);
+    factor_init_kernel<T><<<pairs * kPairParts, kThreads, init_smem, st>>>(
+        W, b1, n, blocks, kPairParts, b0, diag, wdiag, alive, pair_parts, pair_counter, picks, counter);
   } else {
     init_kernel<T><<<(n + 7) / 8, 256, 0, st>>>(W, q, n, b0, diag, wdiag, alive, picks, counter);
   }
-  pick_kernel<T><<<1, kPickThreads, 0, st>>>(W, n, 0, b0, diag, alive, limited, limit, U, wdiag, picks, removed);
+  pick_kernel<T><<<1, kPickThreads, 0, st>>>(n, b0, diag, alive, limited, limit, wdiag, picks, removed);
   for (int step = 0; step < count; ++step) {
     const T* bi = (step & 1) ? b1 : b0;
     T* bo = (step & 1) ? b0 : b1;
-    step_kernel<T, FACTOR><<<dim3(blocks, parts), kRows * kSplit, smem, st>>>(
-        W, n, step, count, bi, bo, diag, wdiag, alive, U, limited, limit, picks + (step & 1),
-        picks + ((step + 1) & 1), partials, counter, column_parts, row_counter, removed);
+    step_kernel<T, FACTOR><<<pairs * parts, kThreads, smem, st>>>(
+        W, n, blocks, parts, step, count, bi, bo, diag, wdiag, alive, U, limited, limit, picks + (step & 1),
+        picks + ((step + 1) & 1), best, counter, pair_parts, pair_counter, removed);
   }
   dsg_count_launches((FACTOR ? 3 : 2) + count);
   return cudaGetLastError() == cudaSuccess ? DSG_OK : DSG_ERR_LAUNCH;
@@ -475,11 +528,7 @@ extern "C" {
 
 size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_complex) {
   if (n <= 0 || count < 0) return 0;
-  const size_t elem = is_complex ? 16 : 8;
-  const size_t blocks = ((size_t)n + kRows - 1) / kRows;
-  return elem * 2 * (size_t)n + 16 * (size_t)n + elem * (size_t)count * n + 2 * sizeof(Pick) +
-         blocks * sizeof(Candidate) + 16 + (size_t)n + 64 + 16 + blocks * sizeof(unsigned) + 16 +
-         blocks * kParts * kRows * elem;
+  return elimination_bytes(n, count, is_complex != 0);
 }
 
 int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, int32_t count,

@@ -523,7 +523,8 @@ size_t dsg_elimination_workspace_bytes(int32_t n, int32_t count, int32_t is_comp
  * at a time, each the cheapest |b_j|^2 / W_jj (b = W q) of those still allowed, continuing
  * with the rank-one-updated inverse; at most limit of the unknowns with limited[j] != 0
  * (uint8 [n], or NULL for no limit) are removed. removed [count] (int64) receives the
- * indices in order. Launches 1 + 2 count kernels; ties go to the lowest index. */
+ * indices in order. Launches 2 + count kernels (3 + count in the factor form); ties go to the
+ * lowest index. */
 int dsg_backward_elimination(const void* inverse, const void* rhs, int32_t n, int32_t count,
                              const uint8_t* limited, int64_t limit, int32_t is_complex, void* workspace,
                              size_t workspace_bytes, int64_t* removed, void* stream);
